@@ -1,0 +1,385 @@
+"""Benchmark: sequential Gaussian simulation throughput (nodes x realizations / s).
+
+One step = one complete simulation of the workload on the GPU: neighbour
+search (kernel a), dependency levels, kriging build + solve (kernel b) and
+the level-scheduled sweep over all realizations (kernel c), from the
+problem already resident in HBM.  Default workload: 3D 200x200x100 grid
+(4M nodes), 5,000 data, exponential variogram with ranges 50/25/5 and a
+30 degree rotation, nugget 0.05, search ellipsoid = the variogram's,
+maxneighbors 48, 256 realizations, RandomPath seed 4, seeded on-device
+standard normals.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank simulates its own 256 realizations on its own GPU
+(replicas: weak scaling, no collective on the data path).
+`--impl reference` times the FP64 CPU restatement of the reference's SEQSIM
+(oracle/, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "geostatsprocesses.jl_gb300"))
+
+METRIC = "SGS nodes×reals/s on 1 GB300: learned+FP32 vs plain FP64 path at ≤1e-6 rel err"
+UNIT = "nodes*reals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"])
+    ap.add_argument("--nreals", type=int, default=None)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 path measurement")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-nodes", type=int, default=60000, help="oracle sample size (nodes)")
+    return ap.parse_args()
+
+
+def workload(name, precision, nreals):
+    from geosgs import workloads
+
+    if name == "c1":
+        wl = workloads.c1(precision)
+    elif name == "c2":
+        wl = workloads.c2(precision)
+    else:
+        wl = workloads.c3(precision)
+    if nreals:
+        wl.nreals = nreals
+    return wl
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 9 and (self.uuid is None or self.uuid in parts[0]):
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------- distributed
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_sample(wl, nodes: int, nthreads: int = 0):
+    """FP64 oracle on a bounded sample of the workload: search + solve of
+    `nodes` path ranks spread over the whole path, and the draw loop of the
+    first `nodes` path ranks for all realizations.  Returns nodes*reals/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import geosgs
+    import oracle
+
+    oracle.build()
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    O = oracle.OraclePlan(p, keep)
+    N, R = O.N, wl.nreals
+    stride = max(1, N // nodes)
+    t0 = time.perf_counter()
+    O.search(oracle.TEMPLATE, stride=stride, nthreads=nthreads)
+    O.solve(stride=stride, nthreads=nthreads)
+    t_ss = time.perf_counter() - t0
+    n_ss = (N + stride - 1) // stride
+    M = min(N, nodes)
+    O.search(oracle.TEMPLATE, t1=M, nthreads=nthreads)
+    O.solve(t1=M, nthreads=nthreads)
+    t0 = time.perf_counter()
+    O.simulate(R, None, seed=1, t_end=M, nthreads=nthreads)
+    t_sw = time.perf_counter() - t0
+    per_node = t_ss / n_ss + t_sw / M  # seconds per node for all R realizations
+    cores = nthreads or os.cpu_count()
+    sample = (f"oracle FP64 on {wl.name}: search+solve of {n_ss} path ranks (every {stride}th) "
+              f"+ draw loop of the first {M} ranks x {R} realizations; {cores} threads")
+    return R / per_node, cores, sample, t_ss + t_sw
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    wl = workload(args.workload, "fp64", args.nreals)
+    vals, secs = [], []
+    for i in range(args.warmup + args.steps):
+        v, cores, sample, s = cpu_sample(wl, args.cpu_nodes)
+        if i >= args.warmup:
+            vals.append(v)
+            secs.append(s)
+    value = statistics.median(vals)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wl.domain.nelements() * wl.nreals / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64 grid data, path and Philox normals)",
+        "config": {"workload": wl.name, "nodes": wl.domain.nelements(), "nreals": wl.nreals,
+                   "maxneighbors": wl.method.maxneighbors},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia reference not runnable on this box (no Julia toolchain); timed the FP64 C++ "
+                "restatement of SEQSIM (oracle/) instead",
+    }
+    print(json.dumps(out))
+
+
+# --------------------------------------------------------------- GPU legs
+def time_device(wl, args, torch, ws):
+    """Device-resident steps: prepare (search, levels, solve) + sweep."""
+    import geosgs
+
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    plan = geosgs.Plan(p, keep)
+    R = wl.nreals
+    Rp = (R + 3) // 4 * 4
+    dt = torch.float64 if wl.method.precision == "fp64" else torch.float32
+    V = torch.empty(plan.N * Rp, dtype=dt, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step(i):
+        plan.prepare()
+        plan.simulate_device(R, None, 1000 + i, V.data_ptr(), stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    launches0 = plan.info().launches
+    sweeps, solves, searches, levels = [], [], [], []
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.steps):
+        step(args.warmup + i)
+        inf = plan.info()  # waits for this step's sweep to time it
+        sweeps.append(inf.ms_sweep)
+        solves.append(inf.ms_solve)
+        searches.append(inf.ms_search)
+        levels.append(inf.ms_levels)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1) / args.steps
+    inf = plan.info()
+    res = dict(ms=max_over_ranks(ws, ms), launches=(inf.launches - launches0), info=inf,
+               ms_sweep=statistics.mean(sweeps), ms_solve=statistics.mean(solves),
+               ms_search=statistics.mean(searches), ms_levels=statistics.mean(levels))
+    plan.close()
+    del V
+    return res
+
+
+def time_e2e(wl, args, torch, ws, steps):
+    """Through the public C ABI with host buffers: create (host -> device
+    copies of the problem), prepare, simulate with the FP64 result copied to
+    pinned host memory, destroy."""
+    import geosgs
+
+    N, R = wl.domain.nelements(), wl.nreals
+    out = torch.empty((R, N), dtype=torch.float64, pin_memory=True).numpy()
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+
+    def step(i):
+        plan = geosgs.Plan(p, keep)
+        plan.prepare()
+        plan._check(plan.lib.sgs_plan_simulate(plan.h, R, None, 77 + i,
+                                               out.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))))
+        inf = plan.info()
+        plan.close()
+        return inf
+
+    step(0)
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    infs = [step(1 + i) for i in range(steps)]
+    torch.cuda.synchronize()
+    dt = max_over_ranks(ws, (time.perf_counter() - t0) / steps)
+    return dt, infs[-1], float(out[0, :8].sum())
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    import geosgs
+    from geosgs import _build
+
+    _build.build()
+    geosgs.load_library()
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        uuid = None
+
+    wl = workload(args.workload, "fp32", args.nreals)
+    N, R = wl.domain.nelements(), wl.nreals
+
+    clocks = ClockSampler(uuid).start()
+    fast = time_device(wl, args, torch, ws)
+    clk = clocks.stop()
+
+    fp64 = None
+    if not args.no_fp64:
+        wl64 = workload(args.workload, "fp64", args.nreals)
+        a64 = argparse.Namespace(**vars(args))
+        a64.steps = max(2, args.steps // 2)
+        a64.warmup = max(1, min(args.warmup, 2))
+        fp64 = time_device(wl64, a64, torch, ws)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e_s, e2e_inf, _ = time_e2e(wl, args, torch, ws, max(1, min(3, args.steps)))
+        e2e = {"value": ws * N * R / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(e2e_inf.h2d_bytes), "d2h_bytes_per_step": int(e2e_inf.d2h_bytes),
+               "ms_per_step": 1e3 * e2e_s,
+               "path": "sgs_plan_create + sgs_plan_prepare + sgs_plan_simulate (FP64 out to pinned host) + sgs_plan_destroy"}
+
+    if rank != 0:
+        return
+
+    # roofline of the sweep (kernel c): algorithmic bytes of one sweep
+    inf = fast["info"]
+    sum_m = int(inf.sum_grid_neighbors)
+    sv = 4
+    alg_bytes = (sum_m + N) * R * sv + sum_m * 8 + N * 16
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg_bytes / (fast["ms_sweep"] * 1e-3) / 1e9
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
+        if tr.get("workload") == wl.name and tr.get("nreals") == R:
+            traffic = tr["dram_bytes_per_sweep"]
+    except Exception:
+        pass
+    roofline = {"kernel": "sweep_fp32_kernel (all level launches of one sweep)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_src, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                "ms": fast["ms_sweep"]}
+
+    cpu = None
+    if not args.no_cpu:
+        v, cores, sample, _ = cpu_sample(wl, args.cpu_nodes)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    value = ws * N * R / (fast["ms"] * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG64 grid data and path; on-device Philox normals)",
+        "config": {"workload": wl.name, "grid": list(wl.domain.dims), "nodes": N,
+                   "ndata": 0 if wl.data is None else wl.data.nrow(), "maxneighbors": wl.method.maxneighbors,
+                   "nreals": R, "precision": "FP32 LHS+Cholesky, FP64 refinement residual and variance",
+                   "warm_start": False, "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (value array %.1f GB)" % (N * R * 4 / 1e9)},
+        "phases_ms": {"search": fast["ms_search"], "levels": fast["ms_levels"], "solve": fast["ms_solve"],
+                      "sweep": fast["ms_sweep"]},
+        "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior), "n_fp64_fallback": int(inf.n_fp64_fallback),
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(fast["launches"]),
+        "clocks": clk,
+    }
+    if fp64:
+        v64 = ws * N * R / (fp64["ms"] * 1e-3)
+        out["fp64_path"] = {"value": v64, "ms_per_step": fp64["ms"],
+                            "phases_ms": {"search": fp64["ms_search"], "levels": fp64["ms_levels"],
+                                          "solve": fp64["ms_solve"], "sweep": fp64["ms_sweep"]}}
+        out["speedup_vs_fp64_path"] = value / v64
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

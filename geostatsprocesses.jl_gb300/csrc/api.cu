@@ -1,0 +1,742 @@
+// api.cu — the C ABI of libgeosgs.so (include/geosgs.h): plan creation,
+// preparation (search, levels, solve), simulation (sweep) and the parity
+// read-backs.  Host-side set-up that has to agree bit for bit with the
+// oracle (the search template's distances) is compiled without FMA
+// contraction (-ffp-contract=off).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/geosgs.h"
+#include "internal.h"
+
+using namespace sgs;
+
+namespace {
+
+thread_local std::string g_create_err;
+const double kSingularTau = 1e-10;  // pivot <= tau*sill -> prior (SGS_NODE_PRIOR_SINGULAR)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct sgs_plan {
+    std::string err;
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    // problem
+    GridDev grid{};
+    MetricDev metric{};
+    VarioDev vario{};
+    double mean = 0.0;
+    int k = 0, nmin = 1;
+    int precision = SGS_PREC_FP32_REFINE;
+    int refine_steps = 2;
+    int warm_start = 0;
+    int64_t N = 0, D = 0;
+    std::vector<int32_t> h_path;
+    std::vector<TmplEntry> h_tmpl;
+    std::vector<double> h_tmpl_d2;
+    int tmpl_ext[3] = {0, 0, 0};
+    // device: geometry and inputs
+    std::vector<DevBuf> bufs;
+    int32_t *d_path = nullptr, *d_rank = nullptr;
+    TmplEntry* d_tmpl = nullptr;
+    double* d_tmpl_d2 = nullptr;
+    double *d_dxyz_b = nullptr, *d_dxyz = nullptr, *d_dval = nullptr;
+    int32_t *d_did = nullptr, *d_bstart = nullptr;
+    int nb[3] = {1, 1, 1};
+    double bw[3] = {1, 1, 1};
+    // device: results
+    int32_t *d_nbr = nullptr, *d_cnt = nullptr, *d_ngrid = nullptr;
+    int32_t *d_level = nullptr, *d_order = nullptr, *d_scratch = nullptr;
+    int8_t* d_status = nullptr;
+    CovLut lut{};
+    double* d_lut64 = nullptr;
+    SweepTables<float> t32{};
+    SweepTables<double> t64{};
+    int32_t *d_fallback = nullptr;
+    std::vector<int32_t> h_loff;  // level offsets (nlevels+1)
+    int nlevels = 0;
+    bool prepared = false;
+    bool sweep_timed = false;     // ev[5]/ev[6] bracket the last sweep
+    unsigned long long* d_sum_m = nullptr;
+    sgs_info info{};
+};
+
+// ---------------------------------------------------------------------------
+namespace {
+
+int set_err(sgs_plan* p, int code, const std::string& msg) {
+    if (p) p->err = msg;
+    else g_create_err = msg;
+    return code;
+}
+
+int cuda_err(sgs_plan* p, cudaError_t e, const char* where) {
+    const int code = (e == cudaErrorMemoryAllocation) ? SGS_ERR_OOM : SGS_ERR_CUDA;
+    return set_err(p, code, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(plan, call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_err(plan, e_, #call); \
+    } while (0)
+
+// check a kernel launch wrapper's status and count the launch
+#define LAUNCH(plan, n, call)                                \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_err(plan, e_, #call); \
+        (plan)->info.launches += (n);                        \
+    } while (0)
+
+template <typename T>
+int dalloc(sgs_plan* p, T** out, size_t count) {
+    *out = nullptr;
+    if (count == 0) count = 1;
+    void* ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(p, SGS_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes failed");
+    }
+    p->bufs.push_back({ptr, count * sizeof(T)});
+    *out = static_cast<T*>(ptr);
+    return SGS_OK;
+}
+
+void dfree(sgs_plan* p, void* ptr) {
+    if (!ptr) return;
+    for (size_t i = 0; i < p->bufs.size(); ++i)
+        if (p->bufs[i].p == ptr) {
+            cudaFree(ptr);
+            p->bufs.erase(p->bufs.begin() + i);
+            return;
+        }
+}
+
+bool is_identity(const double* R, int dim) {
+    for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j)
+            if (R[i + 3 * j] != (i == j ? 1.0 : 0.0)) return false;
+    return true;
+}
+
+void set_metric(MetricDev& m, int dim, int kind, const double* radii, const double* rot) {
+    m.kind = kind;
+    for (int j = 0; j < 3; ++j) m.radii[j] = radii[j];
+    for (int j = 0; j < 9; ++j) m.R[j] = rot[j];
+    m.rr = radii[0] * radii[0];
+    for (int j = 0; j < 3; ++j) m.ext[j] = 0.0;
+    if (kind == METRIC_ISO) {
+        for (int j = 0; j < dim; ++j) m.ext[j] = radii[0];
+    } else if (kind == METRIC_ELLIPSOID) {
+        for (int i = 0; i < dim; ++i) {
+            double s = 0.0;
+            for (int j = 0; j < dim; ++j) {
+                double t = rot[i + 3 * j] * radii[j];
+                s += t * t;
+            }
+            m.ext[i] = std::sqrt(s);
+        }
+    }
+}
+
+// canonical squared distance (host): same operation order as the device's
+// metric_d2 and the oracle; this file is compiled with -ffp-contract=off
+double host_d2(const MetricDev& m, int dim, const double* h) {
+    if (m.kind != METRIC_ELLIPSOID) {
+        double s = h[0] * h[0];
+        s = s + h[1] * h[1];
+        if (dim == 3) s = s + h[2] * h[2];
+        return s;
+    }
+    double s = 0.0;
+    for (int j = 0; j < dim; ++j) {
+        double u = m.R[0 + 3 * j] * h[0];
+        u = u + m.R[1 + 3 * j] * h[1];
+        if (dim == 3) u = u + m.R[2 + 3 * j] * h[2];
+        double q = u / m.radii[j];
+        s = (j == 0) ? q * q : s + q * q;
+    }
+    return s;
+}
+
+bool host_inside(const MetricDev& m, double d2) {
+    if (m.kind == METRIC_ISO) return d2 <= m.rr;
+    if (m.kind == METRIC_ELLIPSOID) return d2 <= 1.0;
+    return true;
+}
+
+template <typename T>
+int upload(sgs_plan* p, T** d, const T* h, size_t count) {
+    int rc = dalloc(p, d, count);
+    if (rc) return rc;
+    if (count) CK(p, cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, p->stream));
+    p->info.h2d_bytes += (int64_t)(count * sizeof(T));
+    return SGS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" const char* sgs_version(void) { return "geosgs 0.1.0 (sm_103a)"; }
+
+extern "C" const char* sgs_last_error(const sgs_plan* plan) {
+    return plan ? plan->err.c_str() : g_create_err.c_str();
+}
+
+extern "C" void sgs_plan_destroy(sgs_plan* p) {
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    for (auto& b : p->bufs) cudaFree(b.p);
+    for (auto& e : p->ev)
+        if (e) cudaEventDestroy(e);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+static int plan_init(sgs_plan* P, const sgs_problem* pr) {
+    const int dim = pr->dim;
+    if (dim != 2 && dim != 3) return set_err(P, SGS_ERR_ARG, "dim must be 2 or 3");
+    GridDev& G = P->grid;
+    G.dim = dim;
+    G.N = 1;
+    for (int j = 0; j < 3; ++j) {
+        G.n[j] = j < dim ? pr->dims[j] : 1;
+        G.origin[j] = j < dim ? pr->origin[j] : 0.0;
+        G.spacing[j] = j < dim ? pr->spacing[j] : 1.0;
+        if (G.n[j] < 1) return set_err(P, SGS_ERR_ARG, "grid dims must be >= 1");
+        if (!(G.spacing[j] > 0.0) || !std::isfinite(G.spacing[j]) || !std::isfinite(G.origin[j]))
+            return set_err(P, SGS_ERR_ARG, "spacing must be finite and > 0");
+        G.N *= G.n[j];
+    }
+    if (G.N > (int64_t)INT32_MAX / 2) return set_err(P, SGS_ERR_ARG, "grid too large (N must be < 2^30)");
+    P->N = G.N;
+    P->D = pr->ndata;
+    if (P->D < 0 || (P->D > 0 && (!pr->data_coords || !pr->data_values)))
+        return set_err(P, SGS_ERR_ARG, "invalid data arrays");
+    if (P->N + P->D > (int64_t)INT32_MAX) return set_err(P, SGS_ERR_ARG, "too many points");
+    for (int64_t i = 0; i < P->D * dim; ++i)
+        if (!std::isfinite(pr->data_coords[i])) return set_err(P, SGS_ERR_ARG, "data coordinates must be finite");
+    for (int64_t i = 0; i < P->D; ++i)
+        if (!std::isfinite(pr->data_values[i])) return set_err(P, SGS_ERR_ARG, "data values must be finite");
+    const sgs_variogram& v = pr->variogram;
+    if (v.type < SGS_SPHERICAL || v.type > SGS_GAUSSIAN) return set_err(P, SGS_ERR_ARG, "unknown variogram type");
+    if (!(v.sill > 0.0) || !(v.nugget >= 0.0) || v.nugget > v.sill || !std::isfinite(v.sill))
+        return set_err(P, SGS_ERR_ARG, "invalid sill/nugget");
+    for (int j = 0; j < dim; ++j)
+        if (!(v.ranges[j] > 0.0) || !std::isfinite(v.ranges[j])) return set_err(P, SGS_ERR_ARG, "ranges must be finite and > 0");
+    if (!std::isfinite(pr->mean)) return set_err(P, SGS_ERR_ARG, "mean must be finite");
+    P->vario.type = v.type;
+    P->vario.sill = v.sill;
+    P->vario.nugget = v.nugget;
+    for (int j = 0; j < 3; ++j) P->vario.inv_range[j] = j < dim ? 1.0 / v.ranges[j] : 1.0;
+    for (int j = 0; j < 9; ++j) P->vario.R[j] = v.rotation[j];
+    P->mean = pr->mean;
+
+    // seqsim.jl:202-208
+    int64_t nmax = pr->maxneighbors, nmin = pr->minneighbors;
+    if (nmax > P->N || nmax < 1) nmax = P->N;
+    if (nmin > nmax || nmin < 1) nmin = 1;
+    if (nmax > KMAX) return set_err(P, SGS_ERR_ARG, "maxneighbors above 64 is not supported on the GPU");
+    P->k = (int)nmax;
+    P->nmin = (int)nmin;
+    if (pr->precision != SGS_PREC_FP64 && pr->precision != SGS_PREC_FP32_REFINE)
+        return set_err(P, SGS_ERR_ARG, "unknown precision");
+    P->precision = pr->precision;
+    if (pr->refine_steps < 0 || pr->refine_steps > 4) return set_err(P, SGS_ERR_ARG, "refine_steps must be in 0..4");
+    P->refine_steps = pr->refine_steps;
+    P->warm_start = pr->warm_start;
+
+    // neighbourhood: seqsim.jl:171-177,221-227
+    static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (pr->search == SGS_SEARCH_RANGE) {
+        double rmax = v.ranges[0];
+        for (int j = 1; j < dim; ++j) rmax = std::max(rmax, v.ranges[j]);
+        double r[3] = {rmax, rmax, rmax};
+        set_metric(P->metric, dim, METRIC_ISO, r, I9);
+    } else if (pr->search == SGS_SEARCH_BALL) {
+        for (int j = 0; j < dim; ++j)
+            if (!(pr->ball.radii[j] > 0.0) || !std::isfinite(pr->ball.radii[j]))
+                return set_err(P, SGS_ERR_ARG, "ball radii must be finite and > 0");
+        bool iso = is_identity(pr->ball.rotation, dim);
+        for (int j = 1; j < dim; ++j) iso = iso && pr->ball.radii[j] == pr->ball.radii[0];
+        set_metric(P->metric, dim, iso ? METRIC_ISO : METRIC_ELLIPSOID, pr->ball.radii, pr->ball.rotation);
+    } else if (pr->search == SGS_SEARCH_NEAREST) {
+        double r[3] = {1, 1, 1};
+        set_metric(P->metric, dim, METRIC_NEAREST, r, I9);
+    } else {
+        return set_err(P, SGS_ERR_ARG, "unknown search kind");
+    }
+
+    // path and ranks
+    P->h_path.resize(P->N);
+    std::vector<int32_t> rank(P->N, -1);
+    for (int64_t t = 0; t < P->N; ++t) {
+        const int64_t g = pr->path ? pr->path[t] : t;
+        if (g < 0 || g >= P->N || rank[g] != -1) return set_err(P, SGS_ERR_ARG, "path is not a permutation of the grid nodes");
+        P->h_path[t] = (int32_t)g;
+        rank[g] = (int32_t)t;
+    }
+
+    // template: cell offsets inside the neighbourhood in canonical order
+    int64_t e[3] = {0, 0, 0};
+    int64_t cells = 1;
+    for (int j = 0; j < dim; ++j) {
+        if (P->metric.kind == METRIC_NEAREST) e[j] = G.n[j] - 1;
+        else e[j] = std::min<int64_t>(G.n[j] - 1, (int64_t)std::floor(P->metric.ext[j] / G.spacing[j]) + 1);
+        cells *= 2 * e[j] + 1;
+    }
+    if (cells > (int64_t)1 << 28) return set_err(P, SGS_ERR_ARG, "search neighbourhood spans too many cells");
+    struct Ent { double d2; int64_t lin; TmplEntry e; };
+    std::vector<Ent> ents;
+    for (int64_t c = -e[2]; c <= e[2]; ++c)
+        for (int64_t b = -e[1]; b <= e[1]; ++b)
+            for (int64_t a = -e[0]; a <= e[0]; ++a) {
+                if (a == 0 && b == 0 && c == 0) continue;
+                double h[3] = {(double)a * G.spacing[0], (double)b * G.spacing[1], dim == 3 ? (double)c * G.spacing[2] : 0.0};
+                double d = host_d2(P->metric, dim, h);
+                if (!host_inside(P->metric, d)) continue;
+                int64_t lin = a + (int64_t)G.n[0] * (b + (int64_t)G.n[1] * c);
+                ents.push_back({d, lin, TmplEntry{(int)a, (int)b, (int)c, (int)lin}});
+            }
+    std::sort(ents.begin(), ents.end(), [](const Ent& x, const Ent& y) {
+        return x.d2 < y.d2 || (x.d2 == y.d2 && x.lin < y.lin);
+    });
+    P->h_tmpl.resize(ents.size());
+    P->h_tmpl_d2.resize(ents.size());
+    for (size_t i = 0; i < ents.size(); ++i) {
+        P->h_tmpl[i] = ents[i].e;
+        P->h_tmpl_d2[i] = ents[i].d2;
+        P->tmpl_ext[0] = std::max(P->tmpl_ext[0], std::abs(ents[i].e.dx));
+        P->tmpl_ext[1] = std::max(P->tmpl_ext[1], std::abs(ents[i].e.dy));
+        P->tmpl_ext[2] = std::max(P->tmpl_ext[2], std::abs(ents[i].e.dz));
+    }
+
+    // device
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(P, SGS_ERR_NODEVICE, "no CUDA device");
+    }
+    if (pr->device < 0 || pr->device >= ndev) return set_err(P, SGS_ERR_ARG, "invalid device ordinal");
+    P->device = pr->device;
+    CK(P, cudaSetDevice(P->device));
+    CK(P, cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->device));
+    CK(P, cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    for (auto& ev : P->ev) CK(P, cudaEventCreate(&ev));
+
+    int rc;
+    if ((rc = upload(P, &P->d_path, P->h_path.data(), P->N))) return rc;
+    if ((rc = upload(P, &P->d_rank, rank.data(), P->N))) return rc;
+    if ((rc = upload(P, &P->d_tmpl, P->h_tmpl.data(), P->h_tmpl.size()))) return rc;
+    if ((rc = upload(P, &P->d_tmpl_d2, P->h_tmpl_d2.data(), P->h_tmpl_d2.size()))) return rc;
+
+    // data: id order (solve) and bucket order (search)
+    std::vector<double> xyz((size_t)P->D * 3, 0.0), val(P->D);
+    for (int64_t i = 0; i < P->D; ++i) {
+        for (int j = 0; j < dim; ++j) xyz[i * 3 + j] = pr->data_coords[i * dim + j];
+        val[i] = pr->data_values[i];
+    }
+    const int B = 8;
+    int64_t nbk = 1;
+    for (int j = 0; j < 3; ++j) {
+        P->nb[j] = (G.n[j] + B - 1) / B;
+        P->bw[j] = G.spacing[j] * (double)B;
+        nbk *= P->nb[j];
+    }
+    std::vector<int64_t> bid(P->D);
+    std::vector<int32_t> bstart(nbk + 1, 0);
+    for (int64_t i = 0; i < P->D; ++i) {
+        int64_t bc[3] = {0, 0, 0};
+        for (int j = 0; j < dim; ++j) {
+            double f = std::floor((xyz[i * 3 + j] - G.origin[j]) / P->bw[j]);
+            f = std::max(0.0, std::min(f, (double)(P->nb[j] - 1)));
+            bc[j] = (int64_t)f;
+        }
+        bid[i] = bc[0] + P->nb[0] * (bc[1] + P->nb[1] * bc[2]);
+        bstart[bid[i] + 1]++;
+    }
+    for (int64_t b = 0; b < nbk; ++b) bstart[b + 1] += bstart[b];
+    std::vector<double> xyz_b((size_t)P->D * 3);
+    std::vector<int32_t> did(P->D);
+    {
+        std::vector<int32_t> cur(bstart.begin(), bstart.end() - 1);
+        for (int64_t i = 0; i < P->D; ++i) {
+            const int32_t q = cur[bid[i]]++;
+            did[q] = (int32_t)i;
+            for (int j = 0; j < 3; ++j) xyz_b[(size_t)q * 3 + j] = xyz[i * 3 + j];
+        }
+    }
+    if ((rc = upload(P, &P->d_dxyz, xyz.data(), xyz.size()))) return rc;
+    if ((rc = upload(P, &P->d_dval, val.data(), val.size()))) return rc;
+    if ((rc = upload(P, &P->d_dxyz_b, xyz_b.data(), xyz_b.size()))) return rc;
+    if ((rc = upload(P, &P->d_did, did.data(), did.size()))) return rc;
+    if ((rc = upload(P, &P->d_bstart, bstart.data(), bstart.size()))) return rc;
+    CK(P, cudaStreamSynchronize(P->stream));
+
+    P->info.nnodes = P->N;
+    P->info.ndata = P->D;
+    P->info.maxneighbors = P->k;
+    P->info.minneighbors = P->nmin;
+    P->info.template_size = (int32_t)P->h_tmpl.size();
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_create(const sgs_problem* problem, sgs_plan** plan) {
+    if (!problem || !plan) return set_err(nullptr, SGS_ERR_ARG, "null argument");
+    *plan = nullptr;
+    sgs_plan* P = new sgs_plan();
+    const int rc = plan_init(P, problem);
+    if (rc != SGS_OK) {
+        g_create_err = P->err.empty() ? g_create_err : P->err;
+        sgs_plan_destroy(P);
+        return rc;
+    }
+    *plan = P;
+    return SGS_OK;
+}
+
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
+    SolveArgs s{};
+    s.grid = P->grid;
+    s.vario = P->vario;
+    s.lut = P->lut;
+    s.k = P->k;
+    s.nmin = P->nmin;
+    s.mu = P->mean;
+    s.tau = kSingularTau * P->vario.sill;
+    s.refine_steps = P->refine_steps;
+    s.P = P->N;
+    s.order = P->d_order;
+    s.nbr = P->d_nbr;
+    s.cnt = P->d_cnt;
+    s.N = P->N;
+    s.data_xyz = P->d_dxyz;
+    s.data_val = P->d_dval;
+    s.status = P->d_status;
+    s.w_full = w_full;
+    s.sigma_full = sigma_full;
+    s.sum_m = P->d_sum_m;
+    CK(P, cudaMemsetAsync(P->d_sum_m, 0, sizeof(unsigned long long), P->stream));
+    if (P->precision == SGS_PREC_FP64) {
+        LAUNCH(P, 1, launch_solve_fp64(s, P->t64, P->stream));
+        P->info.n_fp64_fallback = 0;
+        return SGS_OK;
+    }
+    int32_t* nfb = P->d_scratch;  // scratch[0]
+    CK(P, cudaMemsetAsync(nfb, 0, sizeof(int32_t), P->stream));
+    s.fallback = P->d_fallback;
+    s.nfallback = nfb;
+    LAUNCH(P, 1, launch_solve_fp32(s, P->t32, P->stream));
+    // queued systems: re-solve in FP64 (the canonical decision and accuracy)
+    s.list = P->d_fallback;
+    LAUNCH(P, 1, launch_solve_fp64_into_fp32(s, P->t32, P->stream));
+    int32_t h = 0;
+    CK(P, cudaMemcpyAsync(&h, nfb, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
+    CK(P, cudaStreamSynchronize(P->stream));
+    P->info.d2h_bytes += sizeof(int32_t);
+    P->info.n_fp64_fallback = h;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_prepare(sgs_plan* P) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    CK(P, cudaSetDevice(P->device));
+    const int64_t N = P->N;
+    const int k = P->k;
+    int rc;
+    if (!P->d_nbr) {
+        if ((rc = dalloc(P, &P->d_nbr, (size_t)N * k))) return rc;
+        if ((rc = dalloc(P, &P->d_cnt, N))) return rc;
+        if ((rc = dalloc(P, &P->d_ngrid, N))) return rc;
+        if ((rc = dalloc(P, &P->d_level, N))) return rc;
+        if ((rc = dalloc(P, &P->d_order, N))) return rc;
+        if ((rc = dalloc(P, &P->d_status, N))) return rc;
+        if ((rc = dalloc(P, &P->d_scratch, 16))) return rc;
+        if ((rc = dalloc(P, &P->d_sum_m, 1))) return rc;
+    }
+    cudaStream_t st = P->stream;
+
+    // ---- (a) neighbour search ----
+    SearchArgs sa{};
+    sa.grid = P->grid;
+    sa.metric = P->metric;
+    sa.k = k;
+    sa.T = (int)P->h_tmpl.size();
+    sa.tmpl = P->d_tmpl;
+    sa.tmpl_d2 = P->d_tmpl_d2;
+    sa.path = P->d_path;
+    sa.rank = P->d_rank;
+    sa.D = P->D;
+    sa.dxyz = P->d_dxyz_b;
+    sa.did = P->d_did;
+    sa.bstart = P->d_bstart;
+    for (int j = 0; j < 3; ++j) {
+        sa.nb[j] = P->nb[j];
+        sa.bw[j] = P->bw[j];
+    }
+    sa.nbr = P->d_nbr;
+    sa.cnt = P->d_cnt;
+    sa.ngrid = P->d_ngrid;
+    CK(P, cudaEventRecord(P->ev[0], st));
+    LAUNCH(P, 1, launch_search(sa, st));
+    CK(P, cudaEventRecord(P->ev[1], st));
+
+    // ---- dependency levels and level order ----
+    CK(P, cudaMemsetAsync(P->d_level, 0xff, N * sizeof(int32_t), st));
+    CK(P, cudaMemsetAsync(P->d_scratch, 0, 16 * sizeof(int32_t), st));
+    LevelArgs la{};
+    la.N = N;
+    la.k = k;
+    la.path = P->d_path;
+    la.nbr = P->d_nbr;
+    la.cnt = P->d_cnt;
+    la.level = P->d_level;
+    la.ticket = P->d_scratch + 1;
+    la.maxlevel = P->d_scratch + 2;
+    la.err = P->d_scratch + 3;
+    la.spin_limit = (int64_t)1 << 26;
+    LAUNCH(P, 1, launch_levels(la, P->nsm, st));
+    int32_t hs[4] = {0, 0, 0, 0};
+    CK(P, cudaMemcpyAsync(hs, P->d_scratch, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    CK(P, cudaStreamSynchronize(st));
+    P->info.d2h_bytes += sizeof(hs);
+    if (hs[3]) return set_err(P, SGS_ERR_TIMEOUT, "dependency-level wait exceeded its bound");
+    P->nlevels = hs[2] + 1;
+    int32_t *d_lcount = nullptr, *d_lfill = nullptr, *d_loff = nullptr;
+    if ((rc = dalloc(P, &d_lcount, P->nlevels))) return rc;
+    if ((rc = dalloc(P, &d_lfill, P->nlevels))) return rc;
+    if ((rc = dalloc(P, &d_loff, P->nlevels + 1))) return rc;
+    CK(P, cudaMemsetAsync(d_lcount, 0, P->nlevels * sizeof(int32_t), st));
+    CK(P, cudaMemsetAsync(d_lfill, 0, P->nlevels * sizeof(int32_t), st));
+    LAUNCH(P, 1, launch_level_order(N, P->d_level, P->nlevels, d_lcount, nullptr, nullptr, nullptr, st));
+    std::vector<int32_t> hc(P->nlevels);
+    CK(P, cudaMemcpyAsync(hc.data(), d_lcount, P->nlevels * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(P, cudaStreamSynchronize(st));
+    P->info.d2h_bytes += P->nlevels * sizeof(int32_t);
+    P->h_loff.assign(P->nlevels + 1, 0);
+    for (int l = 0; l < P->nlevels; ++l) P->h_loff[l + 1] = P->h_loff[l] + hc[l];
+    CK(P, cudaMemcpyAsync(d_loff, P->h_loff.data(), (P->nlevels + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    P->info.h2d_bytes += (P->nlevels + 1) * sizeof(int32_t);
+    LAUNCH(P, 1, launch_level_order(N, P->d_level, P->nlevels, d_lcount, d_loff, d_lfill, P->d_order, st));
+    CK(P, cudaEventRecord(P->ev[2], st));
+
+    // ---- covariance table over the pairwise lags of template offsets ----
+    if (!P->d_lut64) {
+        int64_t total = 1;
+        for (int j = 0; j < 3; ++j) {
+            P->lut.e[j] = 2 * P->tmpl_ext[j];
+            P->lut.w[j] = 2 * P->lut.e[j] + 1;
+            total *= P->lut.w[j];
+        }
+        if (total <= ((int64_t)1 << 26)) {
+            if ((rc = dalloc(P, &P->d_lut64, total))) return rc;
+            P->lut.c64 = P->d_lut64;
+            LAUNCH(P, 1, launch_fill_cov_lut(P->grid, P->vario, P->lut, P->d_lut64, nullptr, st));
+        } else {
+            P->lut.c64 = nullptr;
+        }
+    }
+
+    // ---- (b) kriging systems ----
+    if (P->precision == SGS_PREC_FP64) {
+        if (!P->t64.node) {
+            if ((rc = dalloc(P, &P->t64.node, N))) return rc;
+            if ((rc = dalloc(P, &P->t64.m, N))) return rc;
+            if ((rc = dalloc(P, &P->t64.idx, (size_t)N * k))) return rc;
+            if ((rc = dalloc(P, &P->t64.w, (size_t)N * k))) return rc;
+            if ((rc = dalloc(P, &P->t64.b0, N))) return rc;
+            if ((rc = dalloc(P, &P->t64.sigma, N))) return rc;
+        }
+    } else {
+        if (!P->t32.node) {
+            if ((rc = dalloc(P, &P->t32.node, N))) return rc;
+            if ((rc = dalloc(P, &P->t32.m, N))) return rc;
+            if ((rc = dalloc(P, &P->t32.idx, (size_t)N * k))) return rc;
+            if ((rc = dalloc(P, &P->t32.w, (size_t)N * k))) return rc;
+            if ((rc = dalloc(P, &P->t32.b0, N))) return rc;
+            if ((rc = dalloc(P, &P->t32.sigma, N))) return rc;
+            if ((rc = dalloc(P, &P->d_fallback, N))) return rc;
+        }
+    }
+    CK(P, cudaEventRecord(P->ev[3], st));
+    if ((rc = run_solve(P, nullptr, nullptr))) return rc;
+    CK(P, cudaEventRecord(P->ev[4], st));
+    CK(P, cudaStreamSynchronize(st));
+    dfree(P, d_lcount);
+    dfree(P, d_lfill);
+    dfree(P, d_loff);
+    P->info.ms_search = elapsed(P->ev[0], P->ev[1]);
+    P->info.ms_levels = elapsed(P->ev[1], P->ev[2]);
+    P->info.ms_solve = elapsed(P->ev[3], P->ev[4]);
+    P->info.nlevels = P->nlevels;
+    {
+        std::vector<int8_t> st8(N);
+        CK(P, cudaMemcpy(st8.data(), P->d_status, N, cudaMemcpyDeviceToHost));
+        unsigned long long sm = 0;
+        CK(P, cudaMemcpy(&sm, P->d_sum_m, sizeof(sm), cudaMemcpyDeviceToHost));
+        P->info.d2h_bytes += N + sizeof(sm);
+        int64_t np = 0;
+        for (int64_t i = 0; i < N; ++i) np += st8[i] != 0;
+        P->info.n_prior = np;
+        P->info.sum_grid_neighbors = (int64_t)sm;
+    }
+    P->prepared = true;
+    return SGS_OK;
+}
+
+static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, void* V, cudaStream_t st) {
+    for (int l = 0; l < P->nlevels; ++l) {
+        const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
+        cudaError_t e;
+        if (P->precision == SGS_PREC_FP64)
+            e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
+        else
+            e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st);
+        if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
+        if (p1 > p0) P->info.launches++;
+    }
+    (void)R;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_simulate_device(sgs_plan* P, int32_t R, const void* z_dev, uint64_t seed, void* vals_dev,
+                                        void* stream) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "simulate before prepare");
+    if (R < 1 || !vals_dev) return set_err(P, SGS_ERR_ARG, "invalid nreals or output");
+    CK(P, cudaSetDevice(P->device));
+    const int Rp = (R + 3) / 4 * 4;
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->stream;
+    CK(P, cudaEventRecord(P->ev[5], st));
+    int rc = run_sweep(P, R, Rp, z_dev, seed, vals_dev, st);
+    if (rc) return rc;
+    CK(P, cudaEventRecord(P->ev[6], st));
+    P->sweep_timed = true;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64_t seed, double* out) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "simulate before prepare");
+    if (R < 1 || !out) return set_err(P, SGS_ERR_ARG, "invalid nreals or output");
+    CK(P, cudaSetDevice(P->device));
+    const int64_t N = P->N;
+    const int Rp = (R + 3) / 4 * 4;
+    const size_t es = P->precision == SGS_PREC_FP64 ? sizeof(double) : sizeof(float);
+    cudaStream_t st = P->stream;
+    int rc;
+    void* V = nullptr;
+    void* zr = nullptr;
+    double* zin = nullptr;
+    if ((rc = dalloc(P, (unsigned char**)&V, (size_t)N * Rp * es))) return rc;
+    if (z) {
+        if ((rc = dalloc(P, &zin, (size_t)N * R))) { dfree(P, V); return rc; }
+        if ((rc = dalloc(P, (unsigned char**)&zr, (size_t)N * Rp * es))) { dfree(P, V); dfree(P, zin); return rc; }
+        CK(P, cudaMemcpyAsync(zin, z, (size_t)N * R * sizeof(double), cudaMemcpyHostToDevice, st));
+        P->info.h2d_bytes += (int64_t)N * R * sizeof(double);
+        if (P->precision == SGS_PREC_FP64) LAUNCH(P, 1, launch_z_to_rows_fp64(zin, N, R, Rp, (double*)zr, st));
+        else LAUNCH(P, 1, launch_z_to_rows_fp32(zin, N, R, Rp, (float*)zr, st));
+    }
+    CK(P, cudaEventRecord(P->ev[5], st));
+    rc = run_sweep(P, R, Rp, zr, seed, V, st);
+    if (rc) return rc;
+    CK(P, cudaEventRecord(P->ev[6], st));
+    // realization-major FP64 output, in chunks of realizations
+    const int64_t chunk_bytes = (int64_t)1 << 29;
+    int64_t rchunk = std::max<int64_t>(1, std::min<int64_t>(R, chunk_bytes / (N * (int64_t)sizeof(double))));
+    double* ob = nullptr;
+    if ((rc = dalloc(P, &ob, (size_t)N * rchunk))) return rc;
+    for (int64_t r0 = 0; r0 < R; r0 += rchunk) {
+        const int rn = (int)std::min<int64_t>(rchunk, R - r0);
+        // rows_to_out reads realizations [r0, r0+rn) of each row
+        if (P->precision == SGS_PREC_FP64)
+            LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V + r0, N, rn, Rp, P->mean, ob, st));
+        else
+            LAUNCH(P, 1, launch_rows_to_out_fp32((const float*)V + r0, N, rn, Rp, P->mean, ob, st));
+        CK(P, cudaMemcpyAsync(out + r0 * N, ob, (size_t)N * rn * sizeof(double), cudaMemcpyDeviceToHost, st));
+        P->info.d2h_bytes += (int64_t)N * rn * sizeof(double);
+    }
+    CK(P, cudaStreamSynchronize(st));
+    P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
+    P->sweep_timed = false;
+    dfree(P, ob);
+    dfree(P, V);
+    if (zin) dfree(P, zin);
+    if (zr) dfree(P, zr);
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_neighbors(sgs_plan* P, int32_t* idx, int32_t* count) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "neighbors before prepare");
+    CK(P, cudaSetDevice(P->device));
+    if (idx) CK(P, cudaMemcpy(idx, P->d_nbr, (size_t)P->N * P->k * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (count) CK(P, cudaMemcpy(count, P->d_cnt, (size_t)P->N * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    P->info.d2h_bytes += (idx ? (int64_t)P->N * P->k * 4 : 0) + (count ? P->N * 4 : 0);
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_weights(sgs_plan* P, double* weights, double* sigma, int32_t* status) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "weights before prepare");
+    CK(P, cudaSetDevice(P->device));
+    const int64_t N = P->N;
+    int rc;
+    if (weights || sigma) {
+        double *wf = nullptr, *sf = nullptr;
+        if ((rc = dalloc(P, &wf, (size_t)N * P->k))) return rc;
+        if ((rc = dalloc(P, &sf, N))) { dfree(P, wf); return rc; }
+        if ((rc = run_solve(P, wf, sf))) return rc;
+        if (weights) CK(P, cudaMemcpyAsync(weights, wf, (size_t)N * P->k * sizeof(double), cudaMemcpyDeviceToHost, P->stream));
+        if (sigma) CK(P, cudaMemcpyAsync(sigma, sf, (size_t)N * sizeof(double), cudaMemcpyDeviceToHost, P->stream));
+        CK(P, cudaStreamSynchronize(P->stream));
+        dfree(P, wf);
+        dfree(P, sf);
+    }
+    if (status) {
+        std::vector<int8_t> st8(N);
+        CK(P, cudaMemcpy(st8.data(), P->d_status, N, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < N; ++i) status[i] = st8[i];
+    }
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_levels(sgs_plan* P, int32_t* level, int32_t* nlevels) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "levels before prepare");
+    CK(P, cudaSetDevice(P->device));
+    if (level) CK(P, cudaMemcpy(level, P->d_level, (size_t)P->N * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (nlevels) *nlevels = P->nlevels;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_info(const sgs_plan* P, sgs_info* info) {
+    if (!P || !info) return set_err(nullptr, SGS_ERR_ARG, "null argument");
+    *info = P->info;
+    if (P->sweep_timed) {  // a device-resident sweep: time it once it has finished
+        cudaSetDevice(P->device);
+        if (cudaEventSynchronize(P->ev[6]) == cudaSuccess) info->ms_sweep = elapsed(P->ev[5], P->ev[6]);
+    }
+    return SGS_OK;
+}

@@ -1,0 +1,132 @@
+// common.cuh — device helpers shared by the SGS kernels: the canonical FP64
+// lag metric, the variogram covariance, Philox draws and warp utilities.
+//
+// Canonical formulas (identical operation order on host and device; the
+// device uses the _rn intrinsics so nothing is contracted into an FMA):
+//   grid lag      h_j = (double)(i_c - i_p) * spacing_j
+//   data lag      h_j = X_j - (origin_j + ((double)i_j + 0.5) * spacing_j)
+//   isotropic     d2 = h0*h0 + h1*h1 (+ h2*h2), inside iff d2 <= r*r
+//   ellipsoid     u_j = R(0,j)h0 + R(1,j)h1 (+ R(2,j)h2), q_j = u_j / radius_j,
+//                 d2 = sum_j q_j^2, inside iff d2 <= 1
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+#define FULL_MASK 0xffffffffu
+
+namespace sgs {
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// canonical squared distance of a lag under a search metric
+__device__ __forceinline__ double metric_d2(const MetricDev& m, int dim, double h0, double h1, double h2) {
+    if (m.kind != METRIC_ELLIPSOID) {
+        double s = dmul(h0, h0);
+        s = dadd(s, dmul(h1, h1));
+        if (dim == 3) s = dadd(s, dmul(h2, h2));
+        return s;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (j < dim) {
+            double u = dmul(m.R[0 + 3 * j], h0);
+            u = dadd(u, dmul(m.R[1 + 3 * j], h1));
+            if (dim == 3) u = dadd(u, dmul(m.R[2 + 3 * j], h2));
+            double q = ddiv(u, m.radii[j]);
+            s = (j == 0) ? dmul(q, q) : dadd(s, dmul(q, q));
+        }
+    }
+    return s;
+}
+
+__device__ __forceinline__ bool metric_inside(const MetricDev& m, double d2) {
+    if (m.kind == METRIC_ISO) return d2 <= m.rr;
+    if (m.kind == METRIC_ELLIPSOID) return d2 <= 1.0;
+    return true;
+}
+
+// grid centroid coordinate along axis j
+__device__ __forceinline__ double centroid(const GridDev& g, int j, int i) {
+    double t = dadd((double)i, 0.5);
+    t = dmul(t, g.spacing[j]);
+    return dadd(g.origin[j], t);
+}
+
+__device__ __forceinline__ void cell_of(const GridDev& g, int node, int& i0, int& i1, int& i2) {
+    i0 = node % g.n[0];
+    int r = node / g.n[0];
+    i1 = r % g.n[1];
+    i2 = r / g.n[1];
+}
+
+// covariance C(h) = sill - gamma(h) in FP64 (GeoStatsFunctions conventions;
+// the nugget applies for nonzero lags only)
+__device__ __forceinline__ double cov_fp64(const VarioDev& v, int dim, double h0, double h1, double h2) {
+    if (h0 == 0.0 && h1 == 0.0 && (dim == 2 || h2 == 0.0)) return v.sill;
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (j < dim) {
+            double u = v.R[0 + 3 * j] * h0 + v.R[1 + 3 * j] * h1;
+            if (dim == 3) u += v.R[2 + 3 * j] * h2;
+            double q = u * v.inv_range[j];
+            s += q * q;
+        }
+    }
+    double hn = sqrt(s);
+    double f;
+    if (v.type == 1) f = hn < 1.0 ? 1.5 * hn - 0.5 * hn * hn * hn : 1.0;
+    else if (v.type == 2) f = 1.0 - exp(-3.0 * hn);
+    else f = 1.0 - exp(-3.0 * s);
+    return v.sill - (v.nugget + (v.sill - v.nugget) * f);
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw 2011) on counter (c0..c3), key (k0,k1)
+__device__ __forceinline__ uint4 philox10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        uint4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// four standard normals of node g, realizations 4q..4q+3 (Box-Muller on
+// 24-bit uniforms (2m+1)/2^24, exactly representable in float)
+__device__ __forceinline__ float4 normals4(uint64_t seed, int64_t g, int q) {
+    uint4 c = philox10(make_uint4((uint32_t)g, (uint32_t)((uint64_t)g >> 32), (uint32_t)q, 0u),
+                       (uint32_t)seed, (uint32_t)(seed >> 32));
+    const float sc = 1.0f / 16777216.0f;
+    float u0 = (float)((c.x >> 9) * 2u + 1u) * sc;
+    float u1 = (float)((c.y >> 9) * 2u + 1u) * sc;
+    float u2 = (float)((c.z >> 9) * 2u + 1u) * sc;
+    float u3 = (float)((c.w >> 9) * 2u + 1u) * sc;
+    float r0 = sqrtf(-2.0f * logf(u0)), r1 = sqrtf(-2.0f * logf(u2));
+    float s0, c0, s1, c1;
+    sincospif(2.0f * u1, &s0, &c0);
+    sincospif(2.0f * u3, &s1, &c1);
+    return make_float4(r0 * c0, r0 * s0, r1 * c1, r1 * s1);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+}  // namespace sgs

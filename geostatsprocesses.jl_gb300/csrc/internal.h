@@ -1,0 +1,145 @@
+// internal.h — structures and launch wrappers shared by the host side of
+// libgeosgs (api.cu) and the kernel files (search.cu, solve.cu, sweep.cu).
+// Not part of the public ABI (include/geosgs.h is).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sgs {
+
+constexpr int KMAX = 64;           // largest maxneighbors on the GPU
+constexpr int METRIC_ISO = 0;
+constexpr int METRIC_ELLIPSOID = 1;
+constexpr int METRIC_NEAREST = 2;
+constexpr int SGS_NODE_KRIGED_ = 0;          // mirrors SGS_NODE_* of geosgs.h
+constexpr int SGS_NODE_PRIOR_NMIN_ = 1;
+constexpr int SGS_NODE_PRIOR_SINGULAR_ = 2;
+
+struct GridDev {
+    int dim;
+    int n[3];
+    double origin[3];
+    double spacing[3];
+    int64_t N;
+};
+
+struct MetricDev {
+    int kind;
+    double rr;          // r*r (iso)
+    double radii[3];
+    double R[9];        // column-major, leading dimension 3
+    double ext[3];      // bounding-box half extents (physical units)
+};
+
+struct VarioDev {
+    int type;
+    double sill, nugget;
+    double inv_range[3];
+    double R[9];
+};
+
+// Covariance lookup table over integer grid lags L in [-e, e] per axis:
+// entry (L0+e0) + w0*((L1+e1) + w1*(L2+e2)), w = 2e+1.
+struct CovLut {
+    const double* c64;  // nullptr when absent
+    const float* c32;
+    int e[3];
+    int w[3];
+};
+
+// Offset template entry: cell offset and linear offset of a grid candidate.
+struct TmplEntry {
+    int dx, dy, dz, dlin;
+};
+
+struct SearchArgs {
+    GridDev grid;
+    MetricDev metric;
+    int k;
+    int T;                       // template entries
+    const TmplEntry* tmpl;
+    const double* tmpl_d2;
+    const int32_t* path;
+    const int32_t* rank;
+    int64_t D;
+    const double* dxyz;          // data coords, bucket order, D x 3
+    const int32_t* did;          // data id of each bucket-ordered entry
+    const int32_t* bstart;       // bucket start offsets (nb+1)
+    int nb[3];
+    double bw[3];                // bucket widths (physical)
+    int32_t* nbr;                // N x k, node-indexed
+    int32_t* cnt;                // N
+    int32_t* ngrid;              // N: grid neighbours among them
+};
+
+struct LevelArgs {
+    int64_t N;
+    int k;
+    const int32_t* path;
+    const int32_t* nbr;
+    const int32_t* cnt;
+    int32_t* level;              // N, -1 = not yet known
+    int32_t* ticket;             // 1 counter
+    int32_t* maxlevel;           // 1 counter
+    int32_t* err;                // 1 flag
+    int64_t spin_limit;
+};
+
+// Sweep tables, indexed by position in level order.
+template <typename T>
+struct SweepTables {
+    int32_t* node;               // P -> node id
+    int32_t* m;                  // grid neighbours used
+    int32_t* idx;                // P x k grid neighbour node ids
+    T* w;                        // P x k weights of those
+    T* b0;                       // data term sum_i w_i (d_i - mu)
+    T* sigma;                    // conditional std (sqrt(sill) for the prior)
+};
+
+struct SolveArgs {
+    GridDev grid;
+    VarioDev vario;
+    CovLut lut;
+    int k;
+    int nmin;
+    double mu;
+    double tau;                  // singular pivot threshold (absolute)
+    int refine_steps;
+    int64_t P;                   // positions to solve
+    const int32_t* order;        // P -> node
+    const int32_t* nbr;
+    const int32_t* cnt;
+    int64_t N;
+    const double* data_xyz;      // D x 3, data id order
+    const double* data_val;
+    int8_t* status;              // node-indexed
+    double* w_full;              // optional N x k export of all weights (node-indexed)
+    double* sigma_full;          // optional N
+    int32_t* fallback;           // FP32 path: list of positions that need FP64
+    int32_t* nfallback;
+    const int32_t* list;         // FP64 re-solve: positions to solve (nullptr = all)
+    unsigned long long* sum_m;   // accumulates the grid neighbours written to the tables
+};
+
+// ---- launch wrappers (return cudaError_t of the launch) ----
+cudaError_t launch_search(const SearchArgs& a, cudaStream_t s);
+cudaError_t launch_levels(const LevelArgs& a, int nsm, cudaStream_t s);
+cudaError_t launch_level_order(int64_t N, const int32_t* level, int nlevels, int32_t* lcount,
+                               int32_t* loff, int32_t* lfill, int32_t* order, cudaStream_t s);
+cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, cudaStream_t s);
+cudaError_t launch_solve_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s);
+cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s);
+cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp,
+                              const float* z, uint64_t seed, float* V, cudaStream_t s);
+cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
+                              const double* z, uint64_t seed, double* V, cudaStream_t s);
+// host z (R x N, realization-major double) on device -> node-major [N][Rp] of T
+cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s);
+cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, double* z, cudaStream_t s);
+// node-major centred values -> realization-major double with the mean added
+cudaError_t launch_rows_to_out_fp32(const float* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
+cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
+cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float* c32, cudaStream_t s);
+
+}  // namespace sgs

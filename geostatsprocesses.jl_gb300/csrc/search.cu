@@ -1,0 +1,295 @@
+// search.cu — kernel (a): k-nearest neighbours among the data and the
+// earlier-visited grid nodes inside the search neighbourhood, plus the
+// dependency levels of the path's DAG and the level-ordered node list.
+//
+// Replaces search!(neighbors, center, searcher, mask=simulated)
+// (src/simulation/field/seqsim.jl:107) for every node of the path at once:
+// with the path fixed, node p's candidates are the data (always simulated,
+// seqsim.jl:267-271) and the grid nodes of smaller path rank.
+//
+// One warp per node.  Grid candidates come from a template of cell offsets
+// pre-sorted by (canonical FP64 d2, linear offset); scanning it 32 entries at
+// a time and keeping offsets whose node is in the grid and has a smaller rank
+// yields them in (d2, node id) order, so the first k kept are the k nearest.
+// Data candidates come from a bucket grid, are tested with the same FP64
+// metric and sorted in shared memory.  Both sorted lists merge into the
+// node's neighbour row (ties: grid nodes first, their ids are smaller).
+#include <climits>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace sgs {
+
+constexpr int SEARCH_WARPS = 8;
+constexpr int DCAP = 256;  // data candidate buffer per warp
+
+// Bitonic sort of n (<= DCAP) (key, idx) pairs in shared memory by one warp.
+__device__ void warp_sort_pairs(double* key, int32_t* idx, int n, int lane) {
+    int P = 1;
+    while (P < n) P <<= 1;
+    for (int i = n + lane; i < P; i += 32) {
+        key[i] = INFINITY;
+        idx[i] = INT_MAX;
+    }
+    __syncwarp();
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < (P >> 1); t += 32) {
+                int i = (t / stride) * stride * 2 + (t % stride);
+                int j = i + stride;
+                bool asc = (i & size) == 0;
+                double ki = key[i], kj = key[j];
+                int32_t ii = idx[i], ij = idx[j];
+                bool gt = ki > kj || (ki == kj && ii > ij);
+                if (gt == asc) {
+                    key[i] = kj; key[j] = ki;
+                    idx[i] = ij; idx[j] = ii;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SEARCH_WARPS * 32)
+search_kernel(const SearchArgs a) {
+    __shared__ double s_gd2[SEARCH_WARPS][KMAX];
+    __shared__ int32_t s_gidx[SEARCH_WARPS][KMAX];
+    __shared__ double s_dd2[SEARCH_WARPS][DCAP];
+    __shared__ int32_t s_didx[SEARCH_WARPS][DCAP];
+
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    double* gd2 = s_gd2[wib];
+    int32_t* gidx = s_gidx[wib];
+    double* dd2 = s_dd2[wib];
+    int32_t* didx = s_didx[wib];
+    const GridDev& G = a.grid;
+    const int k = a.k;
+    const unsigned lt = lanemask_lt();
+    const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
+
+    for (int64_t t = (int64_t)blockIdx.x * SEARCH_WARPS + wib; t < G.N; t += nwarps) {
+        const int g = a.path[t];
+        int i0, i1, i2;
+        cell_of(G, g, i0, i1, i2);
+
+        // ---- data candidates inside the neighbourhood, sorted ----
+        int nd = 0;
+        if (a.D > 0) {
+            double x[3];
+            x[0] = centroid(G, 0, i0);
+            x[1] = centroid(G, 1, i1);
+            x[2] = G.dim == 3 ? centroid(G, 2, i2) : 0.0;
+            int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+            for (int j = 0; j < G.dim; ++j) {
+                if (a.metric.kind == METRIC_NEAREST) {
+                    lo[j] = 0;
+                    hi[j] = a.nb[j] - 1;
+                } else {
+                    double l = floor((x[j] - a.metric.ext[j] - G.origin[j]) / a.bw[j]) - 1.0;
+                    double h = floor((x[j] + a.metric.ext[j] - G.origin[j]) / a.bw[j]) + 1.0;
+                    lo[j] = (int)fmax(0.0, fmin(l, (double)(a.nb[j] - 1)));
+                    hi[j] = (int)fmax(0.0, fmin(h, (double)(a.nb[j] - 1)));
+                }
+            }
+            int nbuf = 0;
+            for (int bz = lo[2]; bz <= hi[2]; ++bz)
+                for (int by = lo[1]; by <= hi[1]; ++by) {
+                    const int row = a.nb[0] * (by + a.nb[1] * bz);
+                    const int s = a.bstart[row + lo[0]], e = a.bstart[row + hi[0] + 1];
+                    for (int base = s; base < e; base += 32) {
+                        const int i = base + lane;
+                        bool ok = false;
+                        double d2 = 0.0;
+                        if (i < e) {
+                            double h0 = dsub(a.dxyz[3 * (int64_t)i + 0], x[0]);
+                            double h1 = dsub(a.dxyz[3 * (int64_t)i + 1], x[1]);
+                            double h2 = G.dim == 3 ? dsub(a.dxyz[3 * (int64_t)i + 2], x[2]) : 0.0;
+                            d2 = metric_d2(a.metric, G.dim, h0, h1, h2);
+                            ok = metric_inside(a.metric, d2);
+                        }
+                        const unsigned b = __ballot_sync(FULL_MASK, ok);
+                        if (ok) {
+                            const int p = nbuf + __popc(b & lt);
+                            dd2[p] = d2;
+                            didx[p] = (int32_t)(G.N + a.did[i]);
+                        }
+                        nbuf += __popc(b);
+                        __syncwarp();
+                        if (nbuf > DCAP - 32) {
+                            warp_sort_pairs(dd2, didx, nbuf, lane);
+                            nbuf = min(nbuf, k);
+                        }
+                    }
+                }
+            if (nbuf > 0) warp_sort_pairs(dd2, didx, nbuf, lane);
+            nd = min(nbuf, k);
+        }
+
+        // ---- grid candidates from the sorted template ----
+        int ng = 0;
+        for (int base = 0; base < a.T && ng < k; base += 32) {
+            // no template entry from here on can enter the k nearest once
+            // ng grid + the data strictly nearer than this entry fill k
+            if (nd > 0) {
+                const double dcur = a.tmpl_d2[base];
+                int before = 0;
+                for (int q = lane; q < nd; q += 32) before += dd2[q] < dcur ? 1 : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(FULL_MASK, before, o);
+                if (ng + before >= k) break;
+            }
+            const int j = base + lane;
+            bool ok = false;
+            int c = 0;
+            if (j < a.T) {
+                const TmplEntry e = a.tmpl[j];
+                const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
+                if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {
+                    c = g + e.dlin;
+                    ok = a.rank[c] < t;
+                }
+            }
+            const unsigned b = __ballot_sync(FULL_MASK, ok);
+            if (ok) {
+                const int p = ng + __popc(b & lt);
+                if (p < k) {
+                    gidx[p] = c;
+                    gd2[p] = a.tmpl_d2[j];
+                }
+            }
+            ng += __popc(b);
+        }
+        ng = min(ng, k);
+        __syncwarp();
+
+        // ---- merge (d2, id): grid entries precede data entries at equal d2 ----
+        int32_t* out = a.nbr + (int64_t)g * k;
+        int ngrid = 0;
+        for (int q = lane; q < ng; q += 32) {
+            const double d = gd2[q];
+            int lo = 0, hi = nd;  // data strictly nearer
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (dd2[mid] < d) lo = mid + 1; else hi = mid;
+            }
+            const int p = q + lo;
+            if (p < k) {
+                out[p] = gidx[q];
+                ++ngrid;
+            }
+        }
+        for (int q = lane; q < nd; q += 32) {
+            const double d = dd2[q];
+            int lo = 0, hi = ng;  // grid at distance <= d
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (gd2[mid] <= d) lo = mid + 1; else hi = mid;
+            }
+            const int p = q + lo;
+            if (p < k) out[p] = didx[q];
+        }
+        const int total = min(ng + nd, k);
+        for (int p = total + lane; p < k; p += 32) out[p] = -1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ngrid += __shfl_xor_sync(FULL_MASK, ngrid, o);
+        if (lane == 0) {
+            a.cnt[g] = total;
+            a.ngrid[g] = ngrid;
+        }
+        __syncwarp();
+    }
+}
+
+cudaError_t launch_search(const SearchArgs& a, cudaStream_t s) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int64_t want = (a.grid.N + SEARCH_WARPS - 1) / SEARCH_WARPS;
+    int blocks = (int)(want < (int64_t)nsm * 8 ? want : (int64_t)nsm * 8);
+    if (blocks < 1) blocks = 1;
+    search_kernel<<<blocks, SEARCH_WARPS * 32, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Dependency levels: level(p) = 1 + max level of p's grid neighbours (0 when
+// it has none).  Warps take path ranks in increasing order from a ticket
+// counter; a node's neighbours all have smaller ranks, whose tickets were
+// taken earlier by warps that are resident and running, so every wait ends.
+// Each wait is still bounded: past `spin_limit` polls the kernel raises the
+// error flag and goes on (the host reports SGS_ERR_TIMEOUT).
+__global__ void __launch_bounds__(256) levels_kernel(const LevelArgs a) {
+    const int lane = threadIdx.x & 31;
+    volatile int32_t* vlevel = a.level;
+    while (true) {
+        int64_t t = 0;
+        if (lane == 0) t = atomicAdd(a.ticket, 1);
+        t = __shfl_sync(FULL_MASK, t, 0);
+        if (t >= a.N) break;
+        const int g = a.path[t];
+        const int n = a.cnt[g];
+        int lv = 0;
+        for (int q = lane; q < n; q += 32) {
+            const int c = a.nbr[(int64_t)g * a.k + q];
+            if (c < a.N) {
+                int l = vlevel[c];
+                int64_t spins = 0;
+                while (l < 0) {
+                    if (++spins > a.spin_limit) {
+                        atomicExch(a.err, 1);
+                        l = 0;
+                        break;
+                    }
+                    __nanosleep(64);
+                    l = vlevel[c];
+                }
+                lv = max(lv, l + 1);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) lv = max(lv, __shfl_xor_sync(FULL_MASK, lv, o));
+        if (lane == 0) {
+            atomicExch(&a.level[g], lv);
+            atomicMax(a.maxlevel, lv);
+        }
+    }
+}
+
+cudaError_t launch_levels(const LevelArgs& a, int nsm, cudaStream_t s) {
+    levels_kernel<<<nsm * 8, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void level_count_kernel(int64_t N, const int32_t* level, int32_t* lcount) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&lcount[level[g]], 1);
+}
+
+__global__ void level_fill_kernel(int64_t N, const int32_t* level, const int32_t* loff, int32_t* lfill,
+                                  int32_t* order) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+        const int l = level[g];
+        order[loff[l] + atomicAdd(&lfill[l], 1)] = (int32_t)g;
+    }
+}
+
+cudaError_t launch_level_order(int64_t N, const int32_t* level, int nlevels, int32_t* lcount, int32_t* loff,
+                               int32_t* lfill, int32_t* order, cudaStream_t s) {
+    // lcount is counted here; the caller scans it into loff on the host
+    // between the two phases (see api.cu), so this runs in two calls:
+    // order == nullptr -> count, otherwise fill.
+    int blocks = (int)((N + 255) / 256);
+    if (blocks > 65535) blocks = 65535;
+    if (order == nullptr) {
+        level_count_kernel<<<blocks, 256, 0, s>>>(N, level, lcount);
+    } else {
+        level_fill_kernel<<<blocks, 256, 0, s>>>(N, level, loff, lfill, order);
+    }
+    (void)nlevels;
+    return cudaGetLastError();
+}
+
+}  // namespace sgs

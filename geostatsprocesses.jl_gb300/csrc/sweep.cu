@@ -1,0 +1,195 @@
+// sweep.cu — kernel (c): the level-scheduled value sweep over all
+// realizations, and the layout conversions around it.
+//
+// Replaces the draw of randsingle's loop, v = mu_hat + sigma_hat * z
+// (src/simulation/field/seqsim.jl:132,335-340, prior :109-111), for every
+// realization at once.  Values are centred (v - mu) and node-major,
+// V[node][Rp] with realizations contiguous, so one node's update reads each
+// grid neighbour's row of realizations with coalesced vector loads:
+//   V[g][r] = b0 + sum_j w_j V[nb_j][r] + sigma * z[g][r]
+// All nodes of one dependency level are independent; levels run in order.
+// The data's fixed values enter through b0 (computed by the solve).
+#include "common.cuh"
+
+namespace sgs {
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+    __device__ static float4 load(const float* p) { return *reinterpret_cast<const float4*>(p); }
+    __device__ static void store(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+};
+
+__device__ __forceinline__ float4 fma4(float w, float4 v, float4 a) {
+    return make_float4(fmaf(w, v.x, a.x), fmaf(w, v.y, a.y), fmaf(w, v.z, a.z), fmaf(w, v.w, a.w));
+}
+
+struct D4 {
+    double x, y, z, w;
+};
+__device__ __forceinline__ D4 load_d4(const double* p) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    return {a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void store_d4(double* p, D4 v) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v.x, v.y);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v.z, v.w);
+}
+
+// One thread per (node, chunk of 4 realizations).
+__global__ void __launch_bounds__(256) sweep_fp32_kernel(const SweepTables<float> t, int k, int64_t p0,
+                                                         int64_t p1, int Rp, const float* __restrict__ z,
+                                                         uint64_t seed, float* __restrict__ V) {
+    const int cpn = Rp >> 2;
+    const int64_t total = (p1 - p0) * cpn;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = p0 + i / cpn;
+        const int ch = (int)(i % cpn);
+        const int g = t.node[pos];
+        const int m = t.m[pos];
+        const float b0 = t.b0[pos];
+        float4 acc = make_float4(b0, b0, b0, b0);
+        const int32_t* idx = t.idx + pos * k;
+        const float* w = t.w + pos * k;
+#pragma unroll 4
+        for (int j = 0; j < m; ++j) {
+            const float4 v = Vec4<float>::load(V + (int64_t)idx[j] * Rp + 4 * ch);
+            acc = fma4(w[j], v, acc);
+        }
+        const float4 zz = z ? Vec4<float>::load(z + (int64_t)g * Rp + 4 * ch) : normals4(seed, g, ch);
+        acc = fma4(t.sigma[pos], zz, acc);
+        Vec4<float>::store(V + (int64_t)g * Rp + 4 * ch, acc);
+    }
+}
+
+__global__ void __launch_bounds__(256) sweep_fp64_kernel(const SweepTables<double> t, int k, int64_t p0,
+                                                         int64_t p1, int Rp, const double* __restrict__ z,
+                                                         uint64_t seed, double* __restrict__ V) {
+    const int cpn = Rp >> 2;
+    const int64_t total = (p1 - p0) * cpn;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = p0 + i / cpn;
+        const int ch = (int)(i % cpn);
+        const int g = t.node[pos];
+        const int m = t.m[pos];
+        const double b0 = t.b0[pos];
+        D4 acc = {b0, b0, b0, b0};
+        const int32_t* idx = t.idx + pos * k;
+        const double* w = t.w + pos * k;
+#pragma unroll 4
+        for (int j = 0; j < m; ++j) {
+            const D4 v = load_d4(V + (int64_t)idx[j] * Rp + 4 * ch);
+            const double wj = w[j];
+            acc.x = fma(wj, v.x, acc.x);
+            acc.y = fma(wj, v.y, acc.y);
+            acc.z = fma(wj, v.z, acc.z);
+            acc.w = fma(wj, v.w, acc.w);
+        }
+        D4 zz;
+        if (z) {
+            zz = load_d4(z + (int64_t)g * Rp + 4 * ch);
+        } else {
+            const float4 f = normals4(seed, g, ch);
+            zz = {(double)f.x, (double)f.y, (double)f.z, (double)f.w};
+        }
+        const double s = t.sigma[pos];
+        acc.x = fma(s, zz.x, acc.x);
+        acc.y = fma(s, zz.y, acc.y);
+        acc.z = fma(s, zz.z, acc.z);
+        acc.w = fma(s, zz.w, acc.w);
+        store_d4(V + (int64_t)g * Rp + 4 * ch, acc);
+    }
+}
+
+static int sweep_blocks(int64_t total) {
+    int64_t b = (total + 255) / 256;
+    if (b > (1 << 20)) b = 1 << 20;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp, const float* z,
+                              uint64_t seed, float* V, cudaStream_t s) {
+    if (p1 <= p0) return cudaSuccess;
+    sweep_fp32_kernel<<<sweep_blocks((p1 - p0) * (Rp / 4)), 256, 0, s>>>(t, k, p0, p1, Rp, z, seed, V);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp, const double* z,
+                              uint64_t seed, double* V, cudaStream_t s) {
+    if (p1 <= p0) return cudaSuccess;
+    sweep_fp64_kernel<<<sweep_blocks((p1 - p0) * (Rp / 4)), 256, 0, s>>>(t, k, p0, p1, Rp, z, seed, V);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Tiled transposes between the caller's realization-major [R][N] double
+// arrays and the node-major [N][Rp] rows (32x32 tiles through shared memory).
+template <typename T>
+__global__ void z_to_rows_kernel(const double* __restrict__ zin, int64_t N, int R, int Rp, T* __restrict__ z) {
+    __shared__ double tile[32][33];
+    const int64_t g0 = (int64_t)blockIdx.x * 32;
+    const int r0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int r = r0 + j;
+        const int64_t g = g0 + threadIdx.x;
+        tile[j][threadIdx.x] = (r < R && g < N) ? zin[(int64_t)r * N + g] : 0.0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int64_t g = g0 + j;
+        const int r = r0 + threadIdx.x;
+        if (g < N && r < Rp) z[g * Rp + r] = (T)tile[threadIdx.x][j];
+    }
+}
+
+template <typename T>
+__global__ void rows_to_out_kernel(const T* __restrict__ V, int64_t N, int R, int Rp, double mu,
+                                   double* __restrict__ out) {
+    __shared__ double tile[32][33];
+    const int64_t g0 = (int64_t)blockIdx.x * 32;
+    const int r0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int64_t g = g0 + j;
+        const int r = r0 + threadIdx.x;
+        tile[j][threadIdx.x] = (g < N && r < R) ? (double)V[g * Rp + r] : 0.0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int r = r0 + j;
+        const int64_t g = g0 + threadIdx.x;
+        if (r < R && g < N) out[(int64_t)r * N + g] = tile[threadIdx.x][j] + mu;
+    }
+}
+
+template <typename T>
+static cudaError_t z_rows(const double* zin, int64_t N, int R, int Rp, T* z, cudaStream_t s) {
+    dim3 grid((unsigned)((N + 31) / 32), (unsigned)((Rp + 31) / 32));
+    z_to_rows_kernel<T><<<grid, dim3(32, 8), 0, s>>>(zin, N, R, Rp, z);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t rows_out(const T* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s) {
+    dim3 grid((unsigned)((N + 31) / 32), (unsigned)((R + 31) / 32));
+    rows_to_out_kernel<T><<<grid, dim3(32, 8), 0, s>>>(V, N, R, Rp, mu, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s) {
+    return z_rows<float>(zin, N, R, Rp, z, s);
+}
+cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, double* z, cudaStream_t s) {
+    return z_rows<double>(zin, N, R, Rp, z, s);
+}
+cudaError_t launch_rows_to_out_fp32(const float* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s) {
+    return rows_out<float>(V, N, R, Rp, mu, out, s);
+}
+cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s) {
+    return rows_out<double>(V, N, R, Rp, mu, out, s);
+}
+
+}  // namespace sgs

@@ -1,0 +1,37 @@
+"""geosgs — GB300-native sequential Gaussian simulation behind the
+GeoStatsProcesses.jl SEQSIM method API.
+
+Import with the package folder on sys.path:
+
+    sys.path.insert(0, "<repo>/geostatsprocesses.jl_gb300")
+    import geosgs
+"""
+from ._abi import GeoSGSError, load_library
+from .model import (
+    ArgumentError,
+    CartesianGrid,
+    ExplicitPath,
+    ExponentialVariogram,
+    GaussianProcess,
+    GaussianVariogram,
+    GeoTable,
+    LinearPath,
+    MetricBall,
+    RandomPath,
+    RotX,
+    RotY,
+    RotZ,
+    SphericalVariogram,
+    georef,
+)
+from .plan import Plan
+from .problem import build_problem, clamped_neighbors
+from .simulation import GPUSEQSIM, Ensemble, FieldSimulationMethod, preprocess, rand, randsingle
+
+__all__ = [
+    "ArgumentError", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
+    "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
+    "GeoTable", "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
+    "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
+    "preprocess", "rand", "randsingle",
+]

@@ -1,0 +1,179 @@
+"""ctypes mirror of include/geosgs.h and the loader of libgeosgs.so.
+
+The structs below are field-for-field copies of the C declarations; the
+library is loaded from this package's ``lib/`` folder, where ``build()``
+places it.  Loading fails loudly: there is no CPU fallback for the product
+path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+SGS_OK = 0
+SGS_ERR_ARG = -1
+SGS_ERR_CUDA = -2
+SGS_ERR_OOM = -3
+SGS_ERR_TIMEOUT = -4
+SGS_ERR_NUMERIC = -5
+SGS_ERR_STATE = -6
+SGS_ERR_NODEVICE = -7
+
+SGS_SPHERICAL = 1
+SGS_EXPONENTIAL = 2
+SGS_GAUSSIAN = 3
+
+SGS_SEARCH_RANGE = 0
+SGS_SEARCH_BALL = 1
+SGS_SEARCH_NEAREST = 2
+
+SGS_PREC_FP64 = 0
+SGS_PREC_FP32_REFINE = 1
+
+SGS_NODE_KRIGED = 0
+SGS_NODE_PRIOR_NMIN = 1
+SGS_NODE_PRIOR_SINGULAR = 2
+
+
+class SgsVariogram(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("reserved", C.c_int32),
+        ("sill", C.c_double),
+        ("nugget", C.c_double),
+        ("ranges", C.c_double * 3),
+        ("rotation", C.c_double * 9),
+    ]
+
+
+class SgsBall(C.Structure):
+    _fields_ = [("radii", C.c_double * 3), ("rotation", C.c_double * 9)]
+
+
+class SgsProblem(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("dims", C.c_int32 * 3),
+        ("origin", C.c_double * 3),
+        ("spacing", C.c_double * 3),
+        ("ndata", C.c_int64),
+        ("data_coords", C.POINTER(C.c_double)),
+        ("data_values", C.POINTER(C.c_double)),
+        ("variogram", SgsVariogram),
+        ("mean", C.c_double),
+        ("minneighbors", C.c_int32),
+        ("maxneighbors", C.c_int32),
+        ("search", C.c_int32),
+        ("precision", C.c_int32),
+        ("ball", SgsBall),
+        ("path", C.POINTER(C.c_int32)),
+        ("refine_steps", C.c_int32),
+        ("warm_start", C.c_int32),
+        ("device", C.c_int32),
+        ("flags", C.c_int32),
+    ]
+
+
+class SgsInfo(C.Structure):
+    _fields_ = [
+        ("nnodes", C.c_int64),
+        ("ndata", C.c_int64),
+        ("maxneighbors", C.c_int32),
+        ("minneighbors", C.c_int32),
+        ("nlevels", C.c_int32),
+        ("template_size", C.c_int32),
+        ("n_prior", C.c_int64),
+        ("n_fp64_fallback", C.c_int64),
+        ("n_warm_accepted", C.c_int64),
+        ("ms_search", C.c_double),
+        ("ms_levels", C.c_double),
+        ("ms_solve", C.c_double),
+        ("ms_sweep", C.c_double),
+        ("launches", C.c_int64),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+        ("sum_grid_neighbors", C.c_int64),
+    ]
+
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(PKG_DIR, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libgeosgs.so")
+
+# Every entry point declared in include/geosgs.h.
+EXPORTS = (
+    "sgs_plan_create",
+    "sgs_plan_prepare",
+    "sgs_plan_simulate",
+    "sgs_plan_simulate_device",
+    "sgs_plan_neighbors",
+    "sgs_plan_weights",
+    "sgs_plan_levels",
+    "sgs_plan_info",
+    "sgs_plan_destroy",
+    "sgs_last_error",
+    "sgs_version",
+)
+
+_lib = None
+
+
+class GeoSGSError(RuntimeError):
+    """A libgeosgs call returned a negative status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"libgeosgs error {code}: {message}")
+        self.code = code
+
+
+def _declare(lib):
+    P = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int32)
+    lib.sgs_plan_create.argtypes = [C.POINTER(SgsProblem), C.POINTER(P)]
+    lib.sgs_plan_create.restype = C.c_int
+    lib.sgs_plan_prepare.argtypes = [P]
+    lib.sgs_plan_prepare.restype = C.c_int
+    lib.sgs_plan_simulate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp]
+    lib.sgs_plan_simulate.restype = C.c_int
+    lib.sgs_plan_simulate_device.argtypes = [P, C.c_int32, P, C.c_uint64, P, P]
+    lib.sgs_plan_simulate_device.restype = C.c_int
+    lib.sgs_plan_neighbors.argtypes = [P, ip, ip]
+    lib.sgs_plan_neighbors.restype = C.c_int
+    lib.sgs_plan_weights.argtypes = [P, dp, dp, ip]
+    lib.sgs_plan_weights.restype = C.c_int
+    lib.sgs_plan_levels.argtypes = [P, ip, ip]
+    lib.sgs_plan_levels.restype = C.c_int
+    lib.sgs_plan_info.argtypes = [P, C.POINTER(SgsInfo)]
+    lib.sgs_plan_info.restype = C.c_int
+    lib.sgs_plan_destroy.argtypes = [P]
+    lib.sgs_plan_destroy.restype = None
+    lib.sgs_last_error.argtypes = [P]
+    lib.sgs_last_error.restype = C.c_char_p
+    lib.sgs_version.argtypes = []
+    lib.sgs_version.restype = C.c_char_p
+    return lib
+
+
+def load_library(path: str | None = None):
+    """Load libgeosgs.so (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"libgeosgs.so not found at {p}: build it first "
+            "(python -c 'import __graft_entry__ as g; g.build()')"
+        )
+    lib = _declare(C.CDLL(p))
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(lib, code: int, plan=None):
+    if code != SGS_OK:
+        msg = lib.sgs_last_error(plan)
+        raise GeoSGSError(code, msg.decode() if msg else "")
+    return code

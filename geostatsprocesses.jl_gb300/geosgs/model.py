@@ -1,0 +1,269 @@
+"""Host-side mirror of the reference's objects on the SEQSIM path.
+
+GaussianProcess            src/processes/field/gaussian.jl:22-35
+variograms / MetricBall    GeoStatsFunctions 0.15 / Meshes 0.57 (the reference's
+                           dependencies): practical-range spherical, exponential
+                           and gaussian variograms with nugget, anisotropy by a
+                           rotated ellipsoid
+CartesianGrid, paths       Meshes 0.57 CartesianGrid, LinearPath, RandomPath
+georef / GeoTable          GeoTables: values + point coordinates
+
+Only what the GPU SEQSIM path consumes is mirrored.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+from . import _abi
+
+
+class ArgumentError(ValueError):
+    """Invalid argument (the reference raises Julia's ArgumentError)."""
+
+
+# ---------------------------------------------------------------- rotations
+def RotZ(deg: float) -> np.ndarray:
+    """Counter-clockwise rotation by `deg` degrees about +z (Rotations.jl RotZ)."""
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+
+
+def RotY(deg: float) -> np.ndarray:
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[c, 0.0, s], [0.0, 1.0, 0.0], [-s, 0.0, c]])
+
+
+def RotX(deg: float) -> np.ndarray:
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+
+
+def _rot3(rotation) -> np.ndarray:
+    if rotation is None:
+        return np.eye(3)
+    R = np.asarray(rotation, dtype=np.float64)
+    if R.shape == (2, 2):
+        R3 = np.eye(3)
+        R3[:2, :2] = R
+        return R3
+    if R.shape != (3, 3):
+        raise ArgumentError("rotation must be a 2x2 or 3x3 matrix")
+    return R
+
+
+# -------------------------------------------------------------- neighbourhoods
+@dataclass
+class MetricBall:
+    """Ellipsoid |diag(1/radii) R^T h| <= 1 (isotropic ball when one radius)."""
+
+    radii: Sequence[float] | float
+    rotation: np.ndarray | None = None
+
+    def __post_init__(self):
+        r = np.atleast_1d(np.asarray(self.radii, dtype=np.float64))
+        self.radii = tuple(float(x) for x in r)
+        self.rotation = _rot3(self.rotation)
+
+    def radius(self) -> float:
+        return self.radii[0]
+
+    def padded_radii(self, dim: int) -> tuple:
+        r = list(self.radii)
+        if len(r) == 1:
+            r = r * dim
+        if len(r) < dim:
+            raise ArgumentError("MetricBall has fewer radii than the domain's dimension")
+        return tuple(r[:dim]) + (1.0,) * (3 - dim)
+
+
+# ----------------------------------------------------------------- variograms
+@dataclass
+class _Variogram:
+    ball: MetricBall = field(default_factory=lambda: MetricBall(1.0))
+    sill: float = 1.0
+    nugget: float = 0.0
+    TYPE = 0
+
+    def __init__(self, ball=None, *, range=None, ranges=None, rotation=None, sill=1.0, nugget=0.0):
+        if ball is None:
+            if ranges is not None:
+                ball = MetricBall(ranges, rotation)
+            else:
+                ball = MetricBall(1.0 if range is None else range, rotation)
+        self.ball = ball
+        self.sill = float(sill)
+        self.nugget = float(nugget)
+
+    def range(self) -> float:
+        """Largest radius of the variogram's ellipsoid (GeoStatsFunctions `range`)."""
+        return max(self.ball.radii)
+
+    def _f(self, h):
+        raise NotImplementedError
+
+    def __call__(self, h):
+        """gamma(h) for a normalized lag h (h = 1 at the range)."""
+        h = np.asarray(h, dtype=np.float64)
+        return np.where(h > 0, self.nugget + (self.sill - self.nugget) * self._f(h), 0.0)
+
+    def to_c(self, dim: int) -> _abi.SgsVariogram:
+        v = _abi.SgsVariogram()
+        v.type = self.TYPE
+        v.sill = self.sill
+        v.nugget = self.nugget
+        for j, r in enumerate(self.ball.padded_radii(dim)):
+            v.ranges[j] = r
+        R = self.ball.rotation
+        for i in range(3):
+            for j in range(3):
+                v.rotation[i + 3 * j] = R[i, j]
+        return v
+
+
+class SphericalVariogram(_Variogram):
+    TYPE = _abi.SGS_SPHERICAL
+
+    def _f(self, h):
+        return np.where(h < 1, 1.5 * h - 0.5 * h**3, 1.0)
+
+
+class ExponentialVariogram(_Variogram):
+    TYPE = _abi.SGS_EXPONENTIAL
+
+    def _f(self, h):
+        return 1.0 - np.exp(-3.0 * h)
+
+
+class GaussianVariogram(_Variogram):
+    TYPE = _abi.SGS_GAUSSIAN
+
+    def _f(self, h):
+        return 1.0 - np.exp(-3.0 * h * h)
+
+
+# ------------------------------------------------------------------- process
+class GaussianProcess:
+    """GaussianProcess(func, mean=0) — src/processes/field/gaussian.jl:22-35.
+
+    Univariate only on the GPU path (a variogram and a scalar mean)."""
+
+    def __init__(self, func, mean: float = 0.0):
+        if not isinstance(func, _Variogram):
+            raise ArgumentError("GaussianProcess on the GPU path takes a variogram")
+        if np.ndim(mean) != 0:
+            raise ArgumentError("mean must be a scalar (univariate process)")
+        self.func = func
+        self.mean = float(mean)
+
+
+# -------------------------------------------------------------------- domain
+class CartesianGrid:
+    """Regular grid: CartesianGrid(dims) or CartesianGrid(start, finish, dims=...)
+    or CartesianGrid(dims, origin=..., spacing=...)."""
+
+    def __init__(self, *args, dims=None, origin=None, spacing=None):
+        if len(args) == 1:
+            d = args[0]
+            dims = (d,) if np.ndim(d) == 0 else tuple(d)
+            origin = origin if origin is not None else (0.0,) * len(dims)
+            spacing = spacing if spacing is not None else (1.0,) * len(dims)
+        elif len(args) == 2:
+            start, finish = (np.asarray(a, dtype=np.float64) for a in args)
+            if dims is None:
+                raise ArgumentError("dims is required with start/finish")
+            dims = tuple(dims)
+            origin = tuple(start)
+            spacing = tuple((finish - start) / np.asarray(dims, dtype=np.float64))
+        elif dims is not None:
+            dims = tuple(dims)
+            origin = origin if origin is not None else (0.0,) * len(dims)
+            spacing = spacing if spacing is not None else (1.0,) * len(dims)
+        else:
+            raise ArgumentError("invalid CartesianGrid arguments")
+        self.dims = tuple(int(x) for x in dims)
+        self.origin = tuple(float(x) for x in origin)
+        self.spacing = tuple(float(x) for x in spacing)
+        if len(self.dims) not in (2, 3) or len(self.origin) != len(self.dims) or len(self.spacing) != len(self.dims):
+            raise ArgumentError("the GPU path supports 2D and 3D grids")
+
+    @property
+    def dim(self) -> int:
+        return len(self.dims)
+
+    def nelements(self) -> int:
+        return int(np.prod(self.dims))
+
+    def centroids(self) -> np.ndarray:
+        """Cell centres, node-major (first axis fastest)."""
+        axes = [self.origin[j] + (np.arange(self.dims[j]) + 0.5) * self.spacing[j] for j in range(self.dim)]
+        mesh = np.meshgrid(*axes, indexing="ij")
+        return np.stack([m.reshape(-1, order="F") for m in mesh], axis=1)
+
+    def linear_index(self, *ijk) -> int:
+        """0-based node id of (0-based) cell indices."""
+        g, mult = 0, 1
+        for j, i in enumerate(ijk):
+            g += int(i) * mult
+            mult *= self.dims[j]
+        return g
+
+
+class GeoTable:
+    """Point data: one variable per column and D x dim coordinates."""
+
+    def __init__(self, values: dict, coords):
+        self.values = {k: np.asarray(v, dtype=np.float64) for k, v in values.items()}
+        c = np.asarray(coords, dtype=np.float64)
+        if c.ndim == 1:
+            c = c[:, None]
+        self.coords = np.ascontiguousarray(c)
+        for k, v in self.values.items():
+            if v.shape != (self.coords.shape[0],):
+                raise ArgumentError(f"column {k} does not match the number of points")
+
+    def nrow(self) -> int:
+        return self.coords.shape[0]
+
+
+def georef(values: dict, coords) -> GeoTable:
+    return GeoTable(values, coords)
+
+
+# --------------------------------------------------------------------- paths
+class LinearPath:
+    """Visit nodes in linear index order (SEQSIM's default path)."""
+
+    def permutation(self, n: int):
+        return None
+
+
+class RandomPath:
+    """A random visiting order from a seeded generator (numpy PCG64).
+
+    The permutation is drawn once per plan and shared by all realizations
+    of that plan; Julia's randperm stream is not reproduced."""
+
+    def __init__(self, seed: int = 0):
+        self.seed = int(seed)
+
+    def permutation(self, n: int):
+        return np.random.Generator(np.random.PCG64(self.seed)).permutation(n).astype(np.int32)
+
+
+class ExplicitPath:
+    """A caller-given permutation of the grid nodes (0-based)."""
+
+    def __init__(self, perm):
+        self.perm = np.ascontiguousarray(np.asarray(perm, dtype=np.int32))
+
+    def permutation(self, n: int):
+        if self.perm.shape != (n,):
+            raise ArgumentError("path length does not match the domain")
+        return self.perm

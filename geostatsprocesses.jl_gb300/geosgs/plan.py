@@ -1,0 +1,92 @@
+"""Python handle on a libgeosgs plan (the C-ABI in include/geosgs.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Plan:
+    """Owns one sgs_plan: geometry, neighbour/weight tables and the sweep schedule
+    on the GPU.  `prepare()` runs the neighbour search, the level schedule and
+    the kriging solves; `simulate()` runs the batched sweep."""
+
+    def __init__(self, problem: _abi.SgsProblem, keepalive=None):
+        self.lib = _abi.load_library()
+        self._keep = keepalive
+        h = C.c_void_p()
+        _abi.check(self.lib, self.lib.sgs_plan_create(C.byref(problem), C.byref(h)))
+        self.h = h
+        self.dim = int(problem.dim)
+        self.N = int(np.prod([problem.dims[j] for j in range(self.dim)]))
+        info = self.info()
+        self.k = int(info.maxneighbors)
+        self.prepared = False
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sgs_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        return _abi.check(self.lib, rc, self.h)
+
+    def prepare(self):
+        self._check(self.lib.sgs_plan_prepare(self.h))
+        self.prepared = True
+        return self
+
+    def simulate(self, nreals: int, z=None, seed: int = 0) -> np.ndarray:
+        """nreals x N realization-major FP64 array of simulated values."""
+        out = np.empty((nreals, self.N), dtype=np.float64)
+        zp = None
+        if z is not None:
+            z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).reshape(nreals, self.N))
+            zp = _dp(z)
+        self._check(self.lib.sgs_plan_simulate(self.h, nreals, zp, C.c_uint64(seed), _dp(out)))
+        return out
+
+    def simulate_device(self, nreals: int, z_ptr: int | None, seed: int, vals_ptr: int, stream: int | None = None):
+        self._check(self.lib.sgs_plan_simulate_device(
+            self.h, nreals, C.c_void_p(z_ptr) if z_ptr else None, C.c_uint64(seed),
+            C.c_void_p(vals_ptr), C.c_void_p(stream) if stream else None))
+
+    def neighbors(self):
+        idx = np.empty((self.N, self.k), dtype=np.int32)
+        cnt = np.empty(self.N, dtype=np.int32)
+        self._check(self.lib.sgs_plan_neighbors(self.h, _ip(idx), _ip(cnt)))
+        return idx, cnt
+
+    def weights(self):
+        w = np.empty((self.N, self.k), dtype=np.float64)
+        s = np.empty(self.N, dtype=np.float64)
+        st = np.empty(self.N, dtype=np.int32)
+        self._check(self.lib.sgs_plan_weights(self.h, _dp(w), _dp(s), _ip(st)))
+        return w, s, st
+
+    def levels(self):
+        lv = np.empty(self.N, dtype=np.int32)
+        n = C.c_int32()
+        self._check(self.lib.sgs_plan_levels(self.h, _ip(lv), C.byref(n)))
+        return lv, int(n.value)
+
+    def info(self) -> _abi.SgsInfo:
+        inf = _abi.SgsInfo()
+        self._check(self.lib.sgs_plan_info(self.h, C.byref(inf)))
+        return inf

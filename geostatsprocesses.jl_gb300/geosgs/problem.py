@@ -1,0 +1,91 @@
+"""Translate (process, domain, data, method) into the C struct sgs_problem.
+
+This mirrors what preprocess(rng, process, ::SEQSIM, init, domain, data)
+(src/simulation/field/seqsim.jl:50-70) derives from the same objects: the
+search neighbourhood (`:range`, a MetricBall or nothing, seqsim.jl:171-177,
+221-227), min/max neighbours, the data appended after the grid nodes
+(seqsim.jl:211-218, 267-271) and the path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, MetricBall
+
+_PREC = {"fp64": _abi.SGS_PREC_FP64, "fp32": _abi.SGS_PREC_FP32_REFINE}
+
+
+def build_problem(process: GaussianProcess, domain: CartesianGrid, data: GeoTable | None, method):
+    """Return (sgs_problem, keepalive) — keepalive owns the arrays it points to."""
+    if not isinstance(process, GaussianProcess):
+        raise ArgumentError("the GPU SEQSIM path simulates GaussianProcess")
+    if not isinstance(domain, CartesianGrid):
+        raise ArgumentError("the GPU SEQSIM path simulates on a CartesianGrid")
+    dim = domain.dim
+    p = _abi.SgsProblem()
+    p.dim = dim
+    for j in range(3):
+        p.dims[j] = domain.dims[j] if j < dim else 1
+        p.origin[j] = domain.origin[j] if j < dim else 0.0
+        p.spacing[j] = domain.spacing[j] if j < dim else 1.0
+    keep = []
+    if data is not None and data.nrow() > 0:
+        if data.coords.shape[1] != dim:
+            raise ArgumentError("data coordinates do not match the domain's dimension")
+        if len(data.values) != 1:
+            raise ArgumentError("the GPU path simulates one variable")
+        xy = np.ascontiguousarray(data.coords, dtype=np.float64)
+        val = np.ascontiguousarray(next(iter(data.values.values())), dtype=np.float64)
+        keep += [xy, val]
+        p.ndata = xy.shape[0]
+        p.data_coords = xy.ctypes.data_as(C.POINTER(C.c_double))
+        p.data_values = val.ctypes.data_as(C.POINTER(C.c_double))
+    else:
+        p.ndata = 0
+    p.variogram = process.func.to_c(dim)
+    p.mean = process.mean
+    p.minneighbors = int(method.minneighbors)
+    p.maxneighbors = int(method.maxneighbors)
+    nb = method.neighborhood
+    if isinstance(nb, str) and nb == "range":
+        p.search = _abi.SGS_SEARCH_RANGE
+    elif nb is None:
+        p.search = _abi.SGS_SEARCH_NEAREST
+    elif isinstance(nb, MetricBall):
+        p.search = _abi.SGS_SEARCH_BALL
+        for j, r in enumerate(nb.padded_radii(dim)):
+            p.ball.radii[j] = r
+        for i in range(3):
+            for j in range(3):
+                p.ball.rotation[i + 3 * j] = nb.rotation[i, j]
+    else:
+        raise ArgumentError("neighborhood must be 'range', a MetricBall or None")
+    if getattr(method, "distance", "euclidean") not in ("euclidean", None):
+        raise ArgumentError("only the Euclidean distance is supported")
+    prec = getattr(method, "precision", "fp32")
+    if prec not in _PREC:
+        raise ArgumentError("precision must be 'fp32' or 'fp64'")
+    p.precision = _PREC[prec]
+    p.refine_steps = int(getattr(method, "refine_steps", 2))
+    p.warm_start = 1 if getattr(method, "warm_start", False) else 0
+    p.device = int(getattr(method, "device", 0))
+    perm = method.path.permutation(domain.nelements())
+    if perm is not None:
+        perm = np.ascontiguousarray(perm, dtype=np.int32)
+        keep.append(perm)
+        p.path = perm.ctypes.data_as(C.POINTER(C.c_int32))
+    keep.append(perm)
+    return p, keep
+
+
+def clamped_neighbors(method, nnodes: int):
+    """(nmin, nmax) after the reference's clamps, seqsim.jl:202-208."""
+    nmax, nmin = int(method.maxneighbors), int(method.minneighbors)
+    if nmax > nnodes or nmax < 1:
+        nmax = nnodes
+    if nmin > nmax or nmin < 1:
+        nmin = 1
+    return nmin, nmax

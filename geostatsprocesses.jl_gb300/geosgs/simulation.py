@@ -1,0 +1,158 @@
+"""The reference's field-simulation API with the GPU SEQSIM method plugged in.
+
+rand(...)                 src/simulation/field.jl:47-124
+FieldSimulationMethod     src/simulation/field.jl:135
+preprocess / randsingle   src/simulation/field/seqsim.jl:50-156 (SEQSIM's pair)
+Ensemble                  src/ensembles.jl:10-52 (container + per-node mean/var)
+
+GPUSEQSIM carries SEQSIM's options (seqsim.jl:42-48: path, minneighbors,
+maxneighbors, neighborhood, distance) plus the GPU options (precision,
+refine_steps, warm_start, device).  The path is drawn once per `rand` call
+and shared by all realizations of that call: with it fixed, neighbour sets
+and kriging weights are the same for every realization, so `preprocess`
+computes them once on the GPU and the first `randsingle` simulates the whole
+block of realizations in one batched sweep; later calls hand out the
+remaining columns.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any
+
+import numpy as np
+
+from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, LinearPath
+from .plan import Plan
+from .problem import build_problem
+
+
+class FieldSimulationMethod:
+    """A method for simulating field processes (src/simulation/field.jl:135)."""
+
+
+@dataclass
+class GPUSEQSIM(FieldSimulationMethod):
+    """Sequential Gaussian simulation on one GB300 (drop-in for SEQSIM)."""
+
+    path: Any = field(default_factory=LinearPath)
+    minneighbors: int = 1
+    maxneighbors: int = 26
+    neighborhood: Any = "range"
+    distance: str = "euclidean"
+    precision: str = "fp32"
+    refine_steps: int = 2
+    warm_start: bool = False
+    device: int = 0
+
+
+class Ensemble:
+    """Realizations of a field process over a domain (src/ensembles.jl:10-16)."""
+
+    def __init__(self, domain, reals):
+        self.domain = domain
+        self.reals = list(reals)
+
+    def __len__(self):
+        return len(self.reals)
+
+    def __getitem__(self, i):
+        return self.reals[i]
+
+    def _stack(self, var=None):
+        var = var or next(iter(self.reals[0]))
+        return np.stack([r[var] for r in self.reals])
+
+    def mean(self, var=None):
+        """Per-node mean over realizations (src/ensembles.jl:42-52)."""
+        return self._stack(var).mean(axis=0)
+
+    def var(self, var=None):
+        return self._stack(var).var(axis=0, ddof=1)
+
+
+@dataclass
+class _Preproc:
+    plan: Plan
+    var: str
+    seed: int
+    z: Any = None
+    block: Any = None
+    cursor: int = 0
+    nreals: int = 1
+
+
+def _varname(process, data):
+    if data is not None and len(data.values) == 1:
+        return next(iter(data.values))
+    return "field"
+
+
+def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: CartesianGrid,
+               data: GeoTable | None, *, nreals: int = 1, z=None) -> _Preproc:
+    """Realization-independent work: problem upload, neighbour search, level
+    schedule and kriging solves (seqsim.jl:50-70 plus the hoisted search!/fit
+    of seqsim.jl:107-131).  `init` is ignored like SEQSIM ignores it
+    (seqsim.jl:267-271 always uses ExplicitInit with data appended)."""
+    problem, keep = build_problem(process, domain, data, method)
+    plan = Plan(problem, keep).prepare()
+    seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
+    return _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+
+
+def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc) -> dict:
+    """One realization as {var: values} (seqsim.jl:72-156).  The first call
+    simulates the whole block of `preproc.nreals` realizations on the GPU."""
+    if preproc.block is None:
+        preproc.block = preproc.plan.simulate(preproc.nreals, z=preproc.z, seed=preproc.seed)
+        preproc.cursor = 0
+    if preproc.cursor >= preproc.block.shape[0]:
+        raise ArgumentError("more realizations requested than the prepared block holds")
+    col = preproc.block[preproc.cursor]
+    preproc.cursor += 1
+    return {preproc.var: col}
+
+
+def _rng_of(x):
+    if x is None:
+        return np.random.default_rng()
+    if isinstance(x, np.random.Generator):
+        return x
+    return np.random.default_rng(int(x))
+
+
+def rand(*args, data=None, method=None, init=None, workers=None, async_=False,
+         showprogress=False, z=None):
+    """rand([rng], process, domain, [nreals]; data, method, init, workers, async)
+    (src/simulation/field.jl:47-124).
+
+    Returns a {var: values} dict for a single realization, or an Ensemble.
+    `z` (nreals x N standard normals, realization-major) replaces the
+    generator's draws, for reproducible comparisons."""
+    args = list(args)
+    rng = None
+    if args and not isinstance(args[0], GaussianProcess):
+        rng = _rng_of(args.pop(0))
+    if len(args) not in (2, 3):
+        raise ArgumentError("rand([rng], process, domain, [nreals]; kwargs...)")
+    process, domain = args[0], args[1]
+    nreals = args[2] if len(args) == 3 else None
+    rng = rng if rng is not None else _rng_of(None)
+    smethod = method if method is not None else GPUSEQSIM()
+    if not isinstance(smethod, GPUSEQSIM):
+        raise ArgumentError("this package provides the GPUSEQSIM method only")
+    if workers not in (None, [0], (0,)):
+        # the plan lives on this process's GPU and is not serializable
+        raise ArgumentError("GPUSEQSIM runs in the calling process; workers must be the master only")
+    if async_:
+        raise ArgumentError("the `async` option is not allowed when the master process is in the `workers`")
+    n = 1 if nreals is None else int(nreals)
+    if n < 1:
+        raise ArgumentError("nreals must be >= 1")
+    pre = preprocess(rng, process, smethod, init, domain, data, nreals=n, z=z)
+    try:
+        reals = [randsingle(rng, process, smethod, domain, data, pre) for _ in range(n)]
+    finally:
+        pre.plan.close()
+    if nreals is None:
+        return reals[0]
+    return Ensemble(domain, reals)

@@ -1,0 +1,196 @@
+/*
+ * geosgs.h — C ABI of libgeosgs.so: sequential Gaussian simulation (SGS) of a
+ * GaussianProcess on a Cartesian grid, on one GB300 GPU.
+ *
+ * This is the drop-in boundary for the SEQSIM method of GeoStatsProcesses.jl
+ * (src/simulation/field/seqsim.jl).  The reference splits a simulation into
+ *   preprocess(rng, process, method, init, domain, data)   seqsim.jl:50-70
+ *   randsingle(rng, process, method, domain, data, preproc) seqsim.jl:72-156
+ * called from rand(rng, process, domain, nreals; data, method)
+ * (src/simulation/field.jl:73-124).  With one simulation path shared by all
+ * realizations, everything randsingle computes per node except the draw
+ * (neighbour search seqsim.jl:107, kriging fit seqsim.jl:124, conditional
+ * seqsim.jl:127-131) depends only on geometry and path rank, so it moves into
+ * a plan that is prepared once; the per-realization work becomes one batched,
+ * level-scheduled sweep over all realizations.
+ *
+ * Conventions
+ *  - All host buffers are owned by the caller; the library copies in and out
+ *    and keeps no host pointer after a call returns.  A plan owns all device
+ *    memory and one CUDA stream.  One host thread uses a plan at a time.
+ *  - Every entry point returns 0 (SGS_OK) or a negative SGS_ERR_* code and
+ *    never aborts; sgs_last_error() gives the message of the last failure.
+ *  - Indices are 0-based.  Grid node id g = i0 + n0*(i1 + n1*i2) (first axis
+ *    fastest, like Julia's LinearIndices).  The "augmented" point set of the
+ *    reference (seqsim.jl:211-218) is grid nodes 0..N-1 followed by data
+ *    points N..N+D-1 (seqsim.jl:267-271, ExplicitInit).
+ *  - Host matrices of realizations are realization-major: element (r, g) at
+ *    [r*N + g], i.e. an N x R column-major Julia matrix.
+ */
+#ifndef GEOSGS_H
+#define GEOSGS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SGS_OK            0
+#define SGS_ERR_ARG      -1  /* invalid argument (reference: ArgumentError / @assert) */
+#define SGS_ERR_CUDA     -2  /* CUDA runtime error */
+#define SGS_ERR_OOM      -3  /* device allocation failed */
+#define SGS_ERR_TIMEOUT  -4  /* a bounded device wait ran out */
+#define SGS_ERR_NUMERIC  -5  /* non-finite result */
+#define SGS_ERR_STATE    -6  /* call out of order (e.g. simulate before prepare) */
+#define SGS_ERR_NODEVICE -7  /* no CUDA device / library built without one */
+
+/* ---- variogram families (GeoStatsFunctions, practical-range convention) - */
+#define SGS_SPHERICAL    1
+#define SGS_EXPONENTIAL  2
+#define SGS_GAUSSIAN     3
+
+/* ---- neighbourhood kinds (SEQSIM `neighborhood` option, seqsim.jl:171-177,221-227) */
+#define SGS_SEARCH_RANGE   0  /* :range  -> isotropic ball of radius max(variogram ranges) */
+#define SGS_SEARCH_BALL    1  /* MetricBall(radii, rotation)                               */
+#define SGS_SEARCH_NEAREST 2  /* nothing -> k nearest with the Euclidean distance          */
+
+/* ---- solve precision ---------------------------------------------------- */
+#define SGS_PREC_FP64        0  /* FP64 LHS, Cholesky, weights and sweep          */
+#define SGS_PREC_FP32_REFINE 1  /* FP32 LHS + Cholesky, FP64 refinement residual and
+                                   variance, FP32 weights and sweep                 */
+
+/* ---- per-node solve status (sgs_plan_weights) --------------------------- */
+#define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */
+#define SGS_NODE_PRIOR_NMIN   1  /* fewer than minneighbors neighbours: prior     */
+#define SGS_NODE_PRIOR_SINGULAR 2/* Cholesky pivot <= 1e-10*sill: prior          */
+
+/* Variogram gamma(h) = nugget*(h>0) + (sill-nugget)*f(h) with the
+ * normalized anisotropic lag h = |diag(1/ranges) * R^T * lag|;
+ * covariance C = sill - gamma (src/utils.jl:50-62). */
+typedef struct sgs_variogram {
+    int32_t type;          /* SGS_SPHERICAL / SGS_EXPONENTIAL / SGS_GAUSSIAN */
+    int32_t reserved;
+    double  sill;
+    double  nugget;
+    double  ranges[3];     /* principal ranges (unused trailing entries ignored in 2D) */
+    double  rotation[9];   /* column-major dim x dim (stride 3); column j = principal axis j */
+} sgs_variogram;
+
+/* Search neighbourhood for SGS_SEARCH_BALL: the ellipsoid
+ * |diag(1/radii) * R^T * lag| <= 1.  Radii all equal with R = I is the
+ * isotropic ball |lag| <= radius. */
+typedef struct sgs_ball {
+    double radii[3];
+    double rotation[9];    /* same layout as sgs_variogram.rotation */
+} sgs_ball;
+
+/* Problem description: GaussianProcess(variogram, mean) on a CartesianGrid,
+ * conditioned on point data, simulated with SEQSIM options. */
+typedef struct sgs_problem {
+    int32_t dim;              /* 2 or 3 */
+    int32_t dims[3];          /* cells per axis */
+    double  origin[3];        /* grid minimum corner */
+    double  spacing[3];       /* cell sizes */
+    int64_t ndata;            /* D >= 0 conditioning points */
+    const double* data_coords;/* D x dim, row-major (point-major) */
+    const double* data_values;/* D */
+    sgs_variogram variogram;
+    double  mean;             /* process mean mu (GaussianProcess.mean) */
+    int32_t minneighbors;     /* SEQSIM.minneighbors (clamped as seqsim.jl:202-208) */
+    int32_t maxneighbors;     /* SEQSIM.maxneighbors (<= 64 on the GPU) */
+    int32_t search;           /* SGS_SEARCH_* */
+    int32_t precision;        /* SGS_PREC_* */
+    sgs_ball ball;            /* used when search == SGS_SEARCH_BALL */
+    const int32_t* path;      /* N grid node ids, a permutation; NULL = LinearPath */
+    int32_t refine_steps;     /* refinement steps for SGS_PREC_FP32_REFINE (0..4, default 2) */
+    int32_t warm_start;       /* 1 = learned warm start of the kriging weights */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t flags;            /* reserved, 0 */
+} sgs_problem;
+
+typedef struct sgs_plan sgs_plan;
+
+typedef struct sgs_info {
+    int64_t nnodes;           /* N */
+    int64_t ndata;            /* D */
+    int32_t maxneighbors;     /* after clamping */
+    int32_t minneighbors;
+    int32_t nlevels;          /* depth of the path's dependency DAG */
+    int32_t template_size;    /* grid offsets inside the search neighbourhood */
+    int64_t n_prior;          /* nodes drawn from the prior */
+    int64_t n_fp64_fallback;  /* FP32 systems re-solved in FP64 */
+    int64_t n_warm_accepted;  /* systems whose learned warm start was accepted */
+    double  ms_search, ms_levels, ms_solve, ms_sweep;  /* last device timings (CUDA events) */
+    int64_t launches;         /* kernels launched by this plan so far */
+    int64_t h2d_bytes;        /* bytes copied host -> device by this plan so far */
+    int64_t d2h_bytes;        /* bytes copied device -> host by this plan so far */
+    int64_t sum_grid_neighbors; /* sum over nodes of grid neighbours used by the sweep */
+} sgs_info;
+
+/* Validate the problem, copy geometry, data and path to the device.
+ * Replaces preprocess(rng, process, ::SEQSIM, init, domain, data),
+ * src/simulation/field/seqsim.jl:50-70 (_scale :162-189, _search :195-230,
+ * _probmodel :277-290, _initialization :267-271). */
+int sgs_plan_create(const sgs_problem* problem, sgs_plan** plan);
+
+/* Run the realization-independent work on the device: neighbour search
+ * (kernel a), dependency levels, simple-kriging build + solve (kernel b).
+ * Replaces the per-node search!/fit/status/predictprob calls of the
+ * randsingle loop, seqsim.jl:98-131, hoisted out of the realization loop. */
+int sgs_plan_prepare(sgs_plan* plan);
+
+/* Simulate nreals realizations (kernel c) and copy them to out (nreals x N,
+ * realization-major, double).  z: standard-normal draws, nreals x N
+ * realization-major (z[r*N+g] is the draw of node g in realization r), or
+ * NULL to draw them on the device from `seed` (Philox4x32-10 + Box-Muller).
+ * Replaces randsingle, seqsim.jl:72-156 (_draw! :335-340, prior :109-111,
+ * output assembly :141-155), for a block of realizations. */
+int sgs_plan_simulate(sgs_plan* plan, int32_t nreals, const double* z,
+                      uint64_t seed, double* out);
+
+/* Device-resident variant of sgs_plan_simulate: z_dev (node-major
+ * [N][nreals], float for SGS_PREC_FP32_REFINE or double for SGS_PREC_FP64,
+ * or NULL for seeded draws) and vals_dev (node-major [N][nreals], same type,
+ * centred values v - mean) are device pointers; stream is a cudaStream_t
+ * (NULL = the plan's stream).  Same reference counterpart as
+ * sgs_plan_simulate. */
+int sgs_plan_simulate_device(sgs_plan* plan, int32_t nreals, const void* z_dev,
+                             uint64_t seed, void* vals_dev, void* stream);
+
+/* Neighbour table: idx (N x maxneighbors, node-major, -1 padded) holds, for
+ * each grid node, its neighbours in nearest-first order, and count (N) their
+ * number.  Replaces search!(neighbors, center, searcher, mask=simulated),
+ * seqsim.jl:107.  Either pointer may be NULL. */
+int sgs_plan_neighbors(sgs_plan* plan, int32_t* idx, int32_t* count);
+
+/* Kriging results per node: weights (N x maxneighbors, aligned with the
+ * neighbour table, 0 padded), sigma (N, conditional standard deviation),
+ * status (N, SGS_NODE_*).  Replaces GeoStatsModels.fit + status +
+ * predictprob, seqsim.jl:124-131,302-304.  Any pointer may be NULL. */
+int sgs_plan_weights(sgs_plan* plan, double* weights, double* sigma, int32_t* status);
+
+/* Dependency level of every node (N) in the path's DAG; nlevels may be NULL.
+ * Replaces the sequential visiting order of `for ind in traverse(domain,
+ * path)`, seqsim.jl:98. */
+int sgs_plan_levels(sgs_plan* plan, int32_t* level, int32_t* nlevels);
+
+/* Plan statistics and last device timings. */
+int sgs_plan_info(const sgs_plan* plan, sgs_info* info);
+
+/* Release all device memory of the plan.  NULL is ignored. */
+void sgs_plan_destroy(sgs_plan* plan);
+
+/* Message of the last failure on this plan, or of the last failed
+ * sgs_plan_create on this thread when plan is NULL. */
+const char* sgs_last_error(const sgs_plan* plan);
+
+/* Library version string. */
+const char* sgs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEOSGS_H */

@@ -1,0 +1,196 @@
+"""CUDA path (through the C ABI) against the FP64 oracle.
+
+Bars: neighbour indices and counts bit-exact; node status identical; values
+within 1e-6 relative, rel = max |v_gpu - v_oracle| / max(|v_oracle|, 1) per
+element, for both precisions (FP64 and FP32 + FP64 refinement); weights
+within 1e-9 (FP64) and 1e-6 (FP32 refined; stored FP32 in the sweep
+tables but exported in FP64)."""
+import numpy as np
+import pytest
+
+import geosgs
+from conftest import golden_cases, golden_problem, load_golden
+from geosgs import workloads
+
+pytestmark = pytest.mark.gpu
+
+VALUE_TOL = 1e-6
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0))) if a.size else 0.0
+
+
+def gpu_plan(problem, keep):
+    return geosgs.Plan(problem, keep).prepare()
+
+
+def both(wl, oracle_mod, precision, t_end=None, stride=None):
+    wl.method.precision = precision
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = gpu_plan(p, keep)
+    O = oracle_mod.OraclePlan(p, keep)
+    if stride:
+        O.search(oracle_mod.TEMPLATE, stride=stride)
+        O.solve(stride=stride)
+    if t_end:
+        O.search(oracle_mod.TEMPLATE, t1=t_end)
+        O.solve(t1=t_end)
+    if not stride and not t_end:
+        O.prepare()
+    return G, O
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", golden_cases())
+def test_golden_fixtures_on_gpu(name, precision, geosgs_lib):
+    g = load_golden(name)
+    p, keep = golden_problem(g, precision)
+    G = gpu_plan(p, keep)
+    idx, cnt = G.neighbors()
+    np.testing.assert_array_equal(cnt, g["cnt"])
+    np.testing.assert_array_equal(idx, g["nbr"])
+    w, s, st = G.weights()
+    np.testing.assert_array_equal(st, g["status"])
+    np.testing.assert_allclose(w, g["w"], rtol=0, atol=1e-9 if precision == 0 else 1e-6)
+    out = G.simulate(g["z"].shape[0], g["z"])
+    assert rel_err(out, g["out"]) <= VALUE_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_c1_full_parity(precision, oracle_mod, geosgs_lib):
+    wl = workloads.c1()
+    G, O = both(wl, oracle_mod, precision)
+    ig, cg = G.neighbors()
+    io, co = O.neighbors()
+    np.testing.assert_array_equal(cg, co)
+    np.testing.assert_array_equal(ig, io)
+    wg, sg, stg = G.weights()
+    wo, so, sto = O.weights()
+    np.testing.assert_array_equal(stg, sto)
+    np.testing.assert_allclose(wg, wo, rtol=0, atol=1e-9 if precision == "fp64" else 1e-6)
+    z = np.random.default_rng(77).standard_normal((wl.nreals, O.N))
+    assert rel_err(G.simulate(wl.nreals, z), O.simulate(wl.nreals, z)) <= VALUE_TOL
+    lg, nlg = G.levels()
+    lo, nlo = O.levels()
+    np.testing.assert_array_equal(lg, lo)
+    assert nlg == nlo
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_c2_full_parity(precision, oracle_mod, geosgs_lib):
+    """500x500 grid, 1,000 data on cell centres, gaussian variogram with a
+    0.01 nugget (duplicate locations -> singular systems), k=32, 64 reals."""
+    wl = workloads.c2(nreals=64)
+    G, O = both(wl, oracle_mod, precision)
+    ig, cg = G.neighbors()
+    io, co = O.neighbors()
+    np.testing.assert_array_equal(cg, co)
+    np.testing.assert_array_equal(ig, io)
+    _, _, stg = G.weights()
+    _, _, sto = O.weights()
+    np.testing.assert_array_equal(stg, sto)
+    z = np.random.default_rng(5).standard_normal((wl.nreals, O.N))
+    err = rel_err(G.simulate(wl.nreals, z), O.simulate(wl.nreals, z))
+    print(f"c2 {precision} max rel err {err:.3e}")
+    assert err <= VALUE_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_3d_anisotropic_with_data(precision, oracle_mod, geosgs_lib):
+    wl = workloads.small(dim=3, n=40, nz=12, k=24, ndata=150, vario="exp", ranges=(12.0, 6.0, 3.0),
+                         rotation=geosgs.RotZ(30.0), nugget=0.05,
+                         ball=geosgs.MetricBall((12.0, 6.0, 3.0), geosgs.RotZ(30.0)), nreals=8)
+    G, O = both(wl, oracle_mod, precision)
+    np.testing.assert_array_equal(G.neighbors()[0], O.neighbors()[0])
+    np.testing.assert_array_equal(G.weights()[2], O.weights()[2])
+    z = np.random.default_rng(9).standard_normal((wl.nreals, O.N))
+    assert rel_err(G.simulate(wl.nreals, z), O.simulate(wl.nreals, z)) <= VALUE_TOL
+
+
+def test_seeded_draws_match_oracle(oracle_mod, geosgs_lib):
+    """On-device Philox draws (float Box-Muller) against the oracle's FP64
+    draws of the same counters: equal up to float rounding of the normals."""
+    wl = workloads.small(n=30, k=10, ndata=10, nreals=12)
+    G, O = both(wl, oracle_mod, "fp64")
+    out_g = G.simulate(12, None, seed=99)
+    out_o = O.simulate(12, None, seed=99)
+    assert rel_err(out_g, out_o) <= 2e-5
+
+
+def test_c3_sampled_neighbours_and_prefix_values(oracle_mod, geosgs_lib):
+    """Full 200x200x100 grid, 5,000 data, rotated ellipsoid, k=48: the oracle
+    searches and solves every 997th path rank plus the first 4,000 ranks;
+    neighbours of all those nodes are bit-exact and the values of the first
+    4,000 path nodes (which depend only on earlier ones) agree within 1e-6."""
+    wl = workloads.c3(precision="fp32", nreals=8)
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = gpu_plan(p, keep)
+    O = oracle_mod.OraclePlan(p, keep)
+    T = 4000
+    O.search(oracle_mod.TEMPLATE, stride=997)
+    O.search(oracle_mod.TEMPLATE, t1=T)
+    O.solve(t1=T)
+    path = wl.method.path.permutation(O.N)
+    ranks = np.unique(np.concatenate([np.arange(0, O.N, 997), np.arange(T)]))
+    nodes = path[ranks]
+    ig, cg = G.neighbors()
+    io, co = O.neighbors()
+    np.testing.assert_array_equal(cg[nodes], co[nodes])
+    np.testing.assert_array_equal(ig[nodes], io[nodes])
+    z = np.random.default_rng(3).standard_normal((wl.nreals, O.N))
+    vg = G.simulate(wl.nreals, z)
+    vo = O.simulate(wl.nreals, z, t_end=T)
+    first = path[:T]
+    assert rel_err(vg[:, first], vo[:, first]) <= VALUE_TOL
+
+
+def test_levels_schedule_is_valid(geosgs_lib):
+    wl = workloads.small(n=50, k=16, ndata=30, precision="fp32")
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = gpu_plan(p, keep)
+    lv, nl = G.levels()
+    idx, cnt = G.neighbors()
+    N = G.N
+    nb = np.where((idx >= 0) & (idx < N), idx, -1)
+    prev = np.where(nb >= 0, lv[np.maximum(nb, 0)], -1).max(axis=1)
+    np.testing.assert_array_equal(lv, prev + 1)
+    assert nl == lv.max() + 1
+
+
+def test_reference_datum_reproduction_gpu(geosgs_lib):
+    """test/field.jl:79-86 through the public rand API on the GPU."""
+    grid = geosgs.CartesianGrid((0.5, 0.5), (100.5, 100.5), dims=(100, 100))
+    data = geosgs.georef({"Z": [1.0, 0.0, 1.0]}, [(25.0, 25.0), (50.0, 75.0), (75.0, 50.0)])
+    proc = geosgs.GaussianProcess(geosgs.SphericalVariogram(range=35.0))
+    for prec in ("fp64", "fp32"):
+        real = geosgs.rand(np.random.default_rng(2017), proc, grid, data=data,
+                           method=geosgs.GPUSEQSIM(maxneighbors=3, precision=prec))
+        assert real["Z"].dtype == np.float64
+        assert abs(real["Z"][grid.linear_index(24, 24)] - 1.0) <= 1e-4
+        ens = geosgs.rand(np.random.default_rng(1), proc, grid, 3, data=data,
+                          method=geosgs.GPUSEQSIM(maxneighbors=3, precision=prec))
+        assert len(ens) == 3 and ens[2]["Z"].shape == (grid.nelements(),)
+
+
+def test_error_codes(geosgs_lib):
+    from geosgs import _abi
+
+    wl = workloads.small(n=10, k=4)
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = geosgs.Plan(p, keep)
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        G.simulate(2)
+    assert e.value.code == _abi.SGS_ERR_STATE
+    p.maxneighbors = 65
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        geosgs.Plan(p, keep)
+    assert e.value.code == _abi.SGS_ERR_ARG
+    p.maxneighbors = 4
+    bad = np.zeros(100, dtype=np.int32)
+    import ctypes as C
+
+    p.path = bad.ctypes.data_as(C.POINTER(C.c_int32))
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        geosgs.Plan(p, (keep, bad))
+    assert e.value.code == _abi.SGS_ERR_ARG
