@@ -46,16 +46,21 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-nodes", type=int, default=60000, help="oracle sample size (nodes)")
+    ap.add_argument("--grid", default=None, help="override the 3D grid, e.g. 200,200,50 (profiling a smaller case)")
+    ap.add_argument("--ndata", type=int, default=None, help="override the number of data (with --grid)")
     return ap.parse_args()
 
 
-def workload(name, precision, nreals):
+def workload(name, precision, nreals, grid=None, ndata=None):
     from geosgs import workloads
 
     if name == "c1":
         wl = workloads.c1(precision)
     elif name == "c2":
         wl = workloads.c2(precision)
+    elif grid:
+        dims = tuple(int(x) for x in grid.split(","))
+        wl = workloads.c3(precision, dims=dims, ndata=ndata if ndata is not None else 5000)
     else:
         wl = workloads.c3(precision)
     if nreals:
@@ -178,7 +183,7 @@ def run_reference(args):
     ws, rank, _ = dist_setup(args)
     if rank != 0:
         return
-    wl = workload(args.workload, "fp64", args.nreals)
+    wl = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
     vals, secs = [], []
     for i in range(args.warmup + args.steps):
         v, cores, sample, s = cpu_sample(wl, args.cpu_nodes)
@@ -297,7 +302,7 @@ def main():
     except Exception:
         uuid = None
 
-    wl = workload(args.workload, "fp32", args.nreals)
+    wl = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
     N, R = wl.domain.nelements(), wl.nreals
 
     clocks = ClockSampler(uuid).start()
@@ -306,7 +311,7 @@ def main():
 
     fp64 = None
     if not args.no_fp64:
-        wl64 = workload(args.workload, "fp64", args.nreals)
+        wl64 = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
         a64 = argparse.Namespace(**vars(args))
         a64.steps = max(2, args.steps // 2)
         a64.warmup = max(1, min(args.warmup, 2))

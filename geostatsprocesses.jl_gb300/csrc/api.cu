@@ -53,6 +53,7 @@ struct sgs_plan {
     TmplEntry* d_tmpl = nullptr;
     double* d_tmpl_d2 = nullptr;
     double *d_dxyz_b = nullptr, *d_dxyz = nullptr, *d_dval = nullptr;
+    float4* d_dxyz_f = nullptr;
     int32_t *d_did = nullptr, *d_bstart = nullptr;
     int nb[3] = {1, 1, 1};
     double bw[3] = {1, 1, 1};
@@ -62,6 +63,7 @@ struct sgs_plan {
     int8_t* d_status = nullptr;
     CovLut lut{};
     double* d_lut64 = nullptr;
+    float2* d_lut2 = nullptr;
     SweepTables<float> t32{};
     SweepTables<double> t64{};
     int32_t *d_fallback = nullptr;
@@ -135,9 +137,17 @@ bool is_identity(const double* R, int dim) {
 
 void set_metric(MetricDev& m, int dim, int kind, const double* radii, const double* rot) {
     m.kind = kind;
-    for (int j = 0; j < 3; ++j) m.radii[j] = radii[j];
-    for (int j = 0; j < 9; ++j) m.R[j] = rot[j];
+    for (int j = 0; j < 3; ++j) {
+        m.radii[j] = radii[j];
+        m.inv[j] = 1.0 / radii[j];
+    }
+    for (int j = 0; j < 9; ++j) {
+        m.R[j] = rot[j];
+        m.Rf[j] = (float)rot[j];
+    }
+    for (int j = 0; j < 3; ++j) m.invf[j] = (float)m.inv[j];
     m.rr = radii[0] * radii[0];
+    m.bound_f = (float)((kind == METRIC_ISO ? m.rr : 1.0) * (1.0 + 1e-3));
     for (int j = 0; j < 3; ++j) m.ext[j] = 0.0;
     if (kind == METRIC_ISO) {
         for (int j = 0; j < dim; ++j) m.ext[j] = radii[0];
@@ -167,7 +177,7 @@ double host_d2(const MetricDev& m, int dim, const double* h) {
         double u = m.R[0 + 3 * j] * h[0];
         u = u + m.R[1 + 3 * j] * h[1];
         if (dim == 3) u = u + m.R[2 + 3 * j] * h[2];
-        double q = u / m.radii[j];
+        double q = u * m.inv[j];
         s = (j == 0) ? q * q : s + q * q;
     }
     return s;
@@ -386,6 +396,37 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     if ((rc = upload(P, &P->d_dxyz_b, xyz_b.data(), xyz_b.size()))) return rc;
     if ((rc = upload(P, &P->d_did, did.data(), did.size()))) return rc;
     if ((rc = upload(P, &P->d_bstart, bstart.data(), bstart.size()))) return rc;
+    // FP32 copies relative to the grid origin for the search's screen, and a
+    // bound that covers their rounding: lags are off by at most dh per axis
+    {
+        std::vector<float4> xf(P->D);
+        double amax = 0.0;
+        for (int j = 0; j < dim; ++j) amax = std::max(amax, (double)G.n[j] * G.spacing[j]);
+        for (int64_t i = 0; i < P->D; ++i) {
+            double r[3] = {0, 0, 0};
+            for (int j = 0; j < dim; ++j) {
+                r[j] = xyz_b[(size_t)i * 3 + j] - G.origin[j];
+                amax = std::max(amax, std::fabs(r[j]));
+            }
+            xf[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
+        }
+        if ((rc = upload(P, &P->d_dxyz_f, xf.data(), xf.size()))) return rc;
+        const double dh = 4.0 * amax * std::ldexp(1.0, -24) + 1e-30;
+        MetricDev& m = P->metric;
+        double slack = 0.0;
+        if (m.kind == METRIC_ISO) {
+            const double r = std::sqrt(m.rr);
+            slack = 2.0 * r * dh * std::sqrt((double)dim) + dim * dh * dh;
+        } else if (m.kind == METRIC_ELLIPSOID) {
+            for (int j = 0; j < dim; ++j) {
+                double dq = 0.0;
+                for (int i = 0; i < dim; ++i) dq += std::fabs(m.R[i + 3 * j]);
+                dq *= dh * m.inv[j];
+                slack += 2.02 * dq + dq * dq;
+            }
+        }
+        m.bound_f = (float)((m.kind == METRIC_ISO ? m.rr : 1.0) * (1.0 + 1e-3) + slack);
+    }
     CK(P, cudaStreamSynchronize(P->stream));
 
     P->info.nnodes = P->N;
@@ -425,6 +466,7 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     s.nmin = P->nmin;
     s.mu = P->mean;
     s.tau = kSingularTau * P->vario.sill;
+    s.inv_sill = 1.0 / P->vario.sill;
     s.refine_steps = P->refine_steps;
     s.P = P->N;
     s.order = P->d_order;
@@ -489,11 +531,15 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     sa.rank = P->d_rank;
     sa.D = P->D;
     sa.dxyz = P->d_dxyz_b;
+    sa.dxyz_f = P->d_dxyz_f;
     sa.did = P->d_did;
     sa.bstart = P->d_bstart;
     for (int j = 0; j < 3; ++j) {
         sa.nb[j] = P->nb[j];
         sa.bw[j] = P->bw[j];
+        sa.inv_bw_f[j] = (float)(1.0 / P->bw[j]);
+        sa.ext_f[j] = (float)P->metric.ext[j];
+        sa.spacing_f[j] = (float)P->grid.spacing[j];
     }
     sa.nbr = P->d_nbr;
     sa.cnt = P->d_cnt;
@@ -551,10 +597,13 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         }
         if (total <= ((int64_t)1 << 26)) {
             if ((rc = dalloc(P, &P->d_lut64, total))) return rc;
+            if ((rc = dalloc(P, &P->d_lut2, total))) return rc;
             P->lut.c64 = P->d_lut64;
-            LAUNCH(P, 1, launch_fill_cov_lut(P->grid, P->vario, P->lut, P->d_lut64, nullptr, st));
+            P->lut.c2 = P->d_lut2;
+            LAUNCH(P, 1, launch_fill_cov_lut(P->grid, P->vario, P->lut, P->d_lut64, P->d_lut2, st));
         } else {
             P->lut.c64 = nullptr;
+            P->lut.c2 = nullptr;
         }
     }
 
@@ -573,9 +622,9 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
             if ((rc = dalloc(P, &P->t32.node, N))) return rc;
             if ((rc = dalloc(P, &P->t32.m, N))) return rc;
             if ((rc = dalloc(P, &P->t32.idx, (size_t)N * k))) return rc;
-            if ((rc = dalloc(P, &P->t32.w, (size_t)N * k))) return rc;
-            if ((rc = dalloc(P, &P->t32.b0, N))) return rc;
-            if ((rc = dalloc(P, &P->t32.sigma, N))) return rc;
+            if ((rc = dalloc(P, &P->t32.w, (size_t)N * k * 2))) return rc;
+            if ((rc = dalloc(P, &P->t32.b0, 2 * N))) return rc;
+            if ((rc = dalloc(P, &P->t32.sigma, 2 * N))) return rc;
             if ((rc = dalloc(P, &P->d_fallback, N))) return rc;
         }
     }

@@ -6,8 +6,9 @@
 //   grid lag      h_j = (double)(i_c - i_p) * spacing_j
 //   data lag      h_j = X_j - (origin_j + ((double)i_j + 0.5) * spacing_j)
 //   isotropic     d2 = h0*h0 + h1*h1 (+ h2*h2), inside iff d2 <= r*r
-//   ellipsoid     u_j = R(0,j)h0 + R(1,j)h1 (+ R(2,j)h2), q_j = u_j / radius_j,
-//                 d2 = sum_j q_j^2, inside iff d2 <= 1
+//   ellipsoid     u_j = R(0,j)h0 + R(1,j)h1 (+ R(2,j)h2), q_j = u_j * inv_j
+//                 with inv_j = 1 / radius_j rounded once, d2 = sum_j q_j^2,
+//                 inside iff d2 <= 1
 #pragma once
 
 #include <cstdint>
@@ -39,11 +40,33 @@ __device__ __forceinline__ double metric_d2(const MetricDev& m, int dim, double 
             double u = dmul(m.R[0 + 3 * j], h0);
             u = dadd(u, dmul(m.R[1 + 3 * j], h1));
             if (dim == 3) u = dadd(u, dmul(m.R[2 + 3 * j], h2));
-            double q = ddiv(u, m.radii[j]);
+            double q = dmul(u, m.inv[j]);
             s = (j == 0) ? dmul(q, q) : dadd(s, dmul(q, q));
         }
     }
     return s;
+}
+
+// FP32 evaluation of the same metric, used only to discard candidates that
+// are clearly outside (bound_f carries a 1e-3 relative margin, far above the
+// FP32 rounding of these few operations), so the FP64 decision is unchanged.
+__device__ __forceinline__ bool metric_maybe_inside(const MetricDev& m, int dim, float h0, float h1, float h2) {
+    if (m.kind == METRIC_NEAREST) return true;
+    float s;
+    if (m.kind != METRIC_ELLIPSOID) {
+        s = h0 * h0 + h1 * h1 + (dim == 3 ? h2 * h2 : 0.0f);
+    } else {
+        s = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            if (j < dim) {
+                float u = m.Rf[0 + 3 * j] * h0 + m.Rf[1 + 3 * j] * h1 + (dim == 3 ? m.Rf[2 + 3 * j] * h2 : 0.0f);
+                float q = u * m.invf[j];
+                s += q * q;
+            }
+        }
+    }
+    return s <= m.bound_f;
 }
 
 __device__ __forceinline__ bool metric_inside(const MetricDev& m, double d2) {
@@ -121,6 +144,79 @@ __device__ __forceinline__ float4 normals4(uint64_t seed, int64_t g, int q) {
     sincospif(2.0f * u1, &s0, &c0);
     sincospif(2.0f * u3, &s1, &c1);
     return make_float4(r0 * c0, r0 * s0, r1 * c1, r1 * s1);
+}
+
+// ---- double-FP32 ("float-float") arithmetic: a value is an unevaluated sum
+// hi + lo of two floats, |lo| <= ulp(hi)/2, about 48 significant bits.  Error-
+// free transformations after Knuth (TwoSum), Dekker (Fast2Sum) and the FMA
+// form of TwoProduct; every operation is an explicit _rn intrinsic so the
+// compiler cannot contract or reorder them.
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+    return {s, e};
+}
+
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ DF df_from_double(double v) {
+    const float hi = (float)v;
+    return {hi, (float)(v - (double)hi)};
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const DF s = df_two_sum(a.hi, b.hi);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.hi, -a.lo}; }
+
+// Compensated dot-product accumulator (Dot2, Ogita-Rump-Oishi 2005) with
+// double-FP32 operands: adds (xh + xl) * (yh + yl) dropping only xl*yl.
+struct DFAcc {
+    float s, c;
+    __device__ __forceinline__ void init(DF v) {
+        s = v.hi;
+        c = v.lo;
+    }
+    __device__ __forceinline__ void add_prod(DF x, DF y) {
+        const float p = __fmul_rn(x.hi, y.hi);
+        const float pe = __fmaf_rn(x.hi, y.hi, -p);
+        const DF t = df_two_sum(s, p);
+        s = t.hi;
+        const float cross = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.hi));
+        c = __fadd_rn(c, __fadd_rn(t.lo, __fadd_rn(pe, cross)));
+    }
+    __device__ __forceinline__ DF value() const { return df_two_sum(s, c); }
+};
+
+// square root of a non-negative double-FP32 value: FP32 root plus one
+// Newton correction evaluated with an exact square (TwoProduct)
+__device__ __forceinline__ DF df_sqrt(DF v) {
+    if (!(v.hi > 0.0f)) return {0.0f, 0.0f};
+    const float r = sqrtf(v.hi);
+    const float p = __fmul_rn(r, r);
+    const float pe = __fmaf_rn(r, r, -p);
+    const float d = __fadd_rn(__fsub_rn(__fsub_rn(v.hi, p), pe), v.lo);
+    return df_fast_two_sum(r, __fdiv_rn(d, __fmul_rn(2.0f, r)));
+}
+
+__device__ __forceinline__ DF shfl_xor_df(DF v, int o) {
+    return {__shfl_xor_sync(FULL_MASK, v.hi, o), __shfl_xor_sync(FULL_MASK, v.lo, o)};
+}
+
+__device__ __forceinline__ DF warp_sum_df(DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = df_add(v, shfl_xor_df(v, o));
+    return v;
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {

@@ -28,8 +28,12 @@ struct MetricDev {
     int kind;
     double rr;          // r*r (iso)
     double radii[3];
+    double inv[3];      // 1 / radii, rounded once
     double R[9];        // column-major, leading dimension 3
     double ext[3];      // bounding-box half extents (physical units)
+    float Rf[9];        // FP32 copies for the conservative prefilter
+    float invf[3];
+    float bound_f;      // FP32 prefilter bound: (1 + 1e-3) * (r*r or 1)
 };
 
 struct VarioDev {
@@ -43,7 +47,7 @@ struct VarioDev {
 // entry (L0+e0) + w0*((L1+e1) + w1*(L2+e2)), w = 2e+1.
 struct CovLut {
     const double* c64;  // nullptr when absent
-    const float* c32;
+    const float2* c2;   // the covariances / sill as FP32 (hi, lo) pairs
     int e[3];
     int w[3];
 };
@@ -64,10 +68,14 @@ struct SearchArgs {
     const int32_t* rank;
     int64_t D;
     const double* dxyz;          // data coords, bucket order, D x 3
+    const float4* dxyz_f;        // the same relative to the grid origin, FP32 (screen)
     const int32_t* did;          // data id of each bucket-ordered entry
     const int32_t* bstart;       // bucket start offsets (nb+1)
     int nb[3];
     double bw[3];                // bucket widths (physical)
+    float inv_bw_f[3];           // FP32 1 / bucket width, for the bucket range
+    float ext_f[3];              // FP32 bounding-box half extents
+    float spacing_f[3];
     int32_t* nbr;                // N x k, node-indexed
     int32_t* cnt;                // N
     int32_t* ngrid;              // N: grid neighbours among them
@@ -86,15 +94,19 @@ struct LevelArgs {
     int64_t spin_limit;
 };
 
-// Sweep tables, indexed by position in level order.
+// Sweep tables, indexed by position in level order.  For T = double one
+// value per entry; for T = float every weight, b0 and sigma is stored as an
+// unevaluated FP32 pair (hi, lo) with hi + lo equal to the FP64 value to
+// about 2^-48 relative, consumed by the compensated (Dot2) FP32 sweep.
 template <typename T>
 struct SweepTables {
+    static constexpr int S = sizeof(T) == 4 ? 2 : 1;  // entries per value
     int32_t* node;               // P -> node id
     int32_t* m;                  // grid neighbours used
     int32_t* idx;                // P x k grid neighbour node ids
-    T* w;                        // P x k weights of those
-    T* b0;                       // data term sum_i w_i (d_i - mu)
-    T* sigma;                    // conditional std (sqrt(sill) for the prior)
+    T* w;                        // P x k x S weights of those
+    T* b0;                       // P x S: data term sum_i w_i (d_i - mu)
+    T* sigma;                    // P x S: conditional std (sqrt(sill) for the prior)
 };
 
 struct SolveArgs {
@@ -105,6 +117,7 @@ struct SolveArgs {
     int nmin;
     double mu;
     double tau;                  // singular pivot threshold (absolute)
+    double inv_sill;             // 1 / sill (the FP32 path works on the correlation matrix)
     int refine_steps;
     int64_t P;                   // positions to solve
     const int32_t* order;        // P -> node
@@ -140,6 +153,6 @@ cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, d
 // node-major centred values -> realization-major double with the mean added
 cudaError_t launch_rows_to_out_fp32(const float* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
 cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
-cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float* c32, cudaStream_t s);
+cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2, cudaStream_t s);
 
 }  // namespace sgs

@@ -24,12 +24,17 @@ namespace sgs {
 constexpr int SEARCH_WARPS = 8;
 constexpr int DCAP = 256;  // data candidate buffer per warp
 
+// Squared distances are non-negative doubles, whose IEEE bit patterns order
+// exactly like the values when read as int64, so the kernel compares and
+// sorts them as integers (the integer ALU instead of GB300's narrow FP64 pipe).
+__device__ __forceinline__ long long key_of(double d2) { return __double_as_longlong(d2); }
+
 // Bitonic sort of n (<= DCAP) (key, idx) pairs in shared memory by one warp.
-__device__ void warp_sort_pairs(double* key, int32_t* idx, int n, int lane) {
+__device__ void warp_sort_pairs(long long* key, int32_t* idx, int n, int lane) {
     int P = 1;
     while (P < n) P <<= 1;
     for (int i = n + lane; i < P; i += 32) {
-        key[i] = INFINITY;
+        key[i] = LLONG_MAX;
         idx[i] = INT_MAX;
     }
     __syncwarp();
@@ -39,7 +44,7 @@ __device__ void warp_sort_pairs(double* key, int32_t* idx, int n, int lane) {
                 int i = (t / stride) * stride * 2 + (t % stride);
                 int j = i + stride;
                 bool asc = (i & size) == 0;
-                double ki = key[i], kj = key[j];
+                long long ki = key[i], kj = key[j];
                 int32_t ii = idx[i], ij = idx[j];
                 bool gt = ki > kj || (ki == kj && ii > ij);
                 if (gt == asc) {
@@ -54,24 +59,31 @@ __device__ void warp_sort_pairs(double* key, int32_t* idx, int n, int lane) {
 
 __global__ void __launch_bounds__(SEARCH_WARPS * 32)
 search_kernel(const SearchArgs a) {
-    __shared__ double s_gd2[SEARCH_WARPS][KMAX];
+    __shared__ long long s_gd2[SEARCH_WARPS][KMAX];
     __shared__ int32_t s_gidx[SEARCH_WARPS][KMAX];
-    __shared__ double s_dd2[SEARCH_WARPS][DCAP];
+    __shared__ long long s_dd2[SEARCH_WARPS][DCAP];
     __shared__ int32_t s_didx[SEARCH_WARPS][DCAP];
+    __shared__ int32_t s_squ[SEARCH_WARPS][64];  // screened data candidates
 
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    double* gd2 = s_gd2[wib];
+    long long* gd2 = s_gd2[wib];
     int32_t* gidx = s_gidx[wib];
-    double* dd2 = s_dd2[wib];
+    long long* dd2 = s_dd2[wib];
+    const long long* tkey = reinterpret_cast<const long long*>(a.tmpl_d2);
     int32_t* didx = s_didx[wib];
+    int32_t* squ = s_squ[wib];
     const GridDev& G = a.grid;
     const int k = a.k;
     const unsigned lt = lanemask_lt();
     const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
 
-    for (int64_t t = (int64_t)blockIdx.x * SEARCH_WARPS + wib; t < G.N; t += nwarps) {
-        const int g = a.path[t];
+    // Nodes go in id order, so the warps of a block take neighbouring cells
+    // and share the rank and data cache lines they scan; the result of a
+    // node depends only on its path rank, not on when it is processed.
+    for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < G.N; gg += nwarps) {
+        const int g = (int)gg;
+        const int64_t t = a.rank[g];
         int i0, i1, i2;
         cell_of(G, g, i0, i1, i2);
 
@@ -88,42 +100,77 @@ search_kernel(const SearchArgs a) {
                     lo[j] = 0;
                     hi[j] = a.nb[j] - 1;
                 } else {
-                    double l = floor((x[j] - a.metric.ext[j] - G.origin[j]) / a.bw[j]) - 1.0;
-                    double h = floor((x[j] + a.metric.ext[j] - G.origin[j]) / a.bw[j]) + 1.0;
-                    lo[j] = (int)fmax(0.0, fmin(l, (double)(a.nb[j] - 1)));
-                    hi[j] = (int)fmax(0.0, fmin(h, (double)(a.nb[j] - 1)));
+                    // bucket range of the neighbourhood's bounding box, in FP32
+                    // with one bucket of margin on each side (a superset)
+                    const int ij = j == 0 ? i0 : (j == 1 ? i1 : i2);
+                    const float xr = ((float)ij + 0.5f) * a.spacing_f[j];
+                    const float l = floorf((xr - a.ext_f[j]) * a.inv_bw_f[j]) - 1.0f;
+                    const float h = floorf((xr + a.ext_f[j]) * a.inv_bw_f[j]) + 1.0f;
+                    lo[j] = (int)fmaxf(0.0f, fminf(l, (float)(a.nb[j] - 1)));
+                    hi[j] = (int)fmaxf(0.0f, fminf(h, (float)(a.nb[j] - 1)));
                 }
             }
-            int nbuf = 0;
+            float xr[3];
+            xr[0] = ((float)i0 + 0.5f) * a.spacing_f[0];
+            xr[1] = ((float)i1 + 0.5f) * a.spacing_f[1];
+            xr[2] = ((float)i2 + 0.5f) * a.spacing_f[2];
+            int nbuf = 0, nq = 0;
+            // exact FP64 test of queued candidates, one per lane (full warps,
+            // so the FP64 path is not issued for a lone surviving lane)
+            auto exact = [&](int cnt) {
+                bool ok = false;
+                double d2 = 0.0;
+                int i = 0;
+                if (lane < cnt) {
+                    i = squ[lane];
+                    const double h0 = dsub(a.dxyz[3 * (int64_t)i + 0], x[0]);
+                    const double h1 = dsub(a.dxyz[3 * (int64_t)i + 1], x[1]);
+                    const double h2 = G.dim == 3 ? dsub(a.dxyz[3 * (int64_t)i + 2], x[2]) : 0.0;
+                    d2 = metric_d2(a.metric, G.dim, h0, h1, h2);
+                    ok = metric_inside(a.metric, d2);
+                }
+                const unsigned b = __ballot_sync(FULL_MASK, ok);
+                if (ok) {
+                    const int p = nbuf + __popc(b & lt);
+                    dd2[p] = key_of(d2);
+                    didx[p] = (int32_t)(G.N + a.did[i]);
+                }
+                nbuf += __popc(b);
+                __syncwarp();
+                if (nbuf > DCAP - 32) {
+                    warp_sort_pairs(dd2, didx, nbuf, lane);
+                    nbuf = min(nbuf, k);
+                }
+            };
             for (int bz = lo[2]; bz <= hi[2]; ++bz)
                 for (int by = lo[1]; by <= hi[1]; ++by) {
                     const int row = a.nb[0] * (by + a.nb[1] * bz);
                     const int s = a.bstart[row + lo[0]], e = a.bstart[row + hi[0] + 1];
                     for (int base = s; base < e; base += 32) {
                         const int i = base + lane;
-                        bool ok = false;
-                        double d2 = 0.0;
+                        bool maybe = false;
                         if (i < e) {
-                            double h0 = dsub(a.dxyz[3 * (int64_t)i + 0], x[0]);
-                            double h1 = dsub(a.dxyz[3 * (int64_t)i + 1], x[1]);
-                            double h2 = G.dim == 3 ? dsub(a.dxyz[3 * (int64_t)i + 2], x[2]) : 0.0;
-                            d2 = metric_d2(a.metric, G.dim, h0, h1, h2);
-                            ok = metric_inside(a.metric, d2);
+                            // FP32 screen on origin-relative FP32 coordinates;
+                            // bound_f includes a slack above their rounding
+                            const float4 p = a.dxyz_f[i];
+                            maybe = metric_maybe_inside(a.metric, G.dim, p.x - xr[0], p.y - xr[1], p.z - xr[2]);
                         }
-                        const unsigned b = __ballot_sync(FULL_MASK, ok);
-                        if (ok) {
-                            const int p = nbuf + __popc(b & lt);
-                            dd2[p] = d2;
-                            didx[p] = (int32_t)(G.N + a.did[i]);
-                        }
-                        nbuf += __popc(b);
+                        const unsigned b = __ballot_sync(FULL_MASK, maybe);
+                        if (maybe) squ[nq + __popc(b & lt)] = i;
+                        nq += __popc(b);
                         __syncwarp();
-                        if (nbuf > DCAP - 32) {
-                            warp_sort_pairs(dd2, didx, nbuf, lane);
-                            nbuf = min(nbuf, k);
+                        if (nq >= 32) {
+                            exact(32);
+                            const int rest = nq - 32;
+                            const int v = lane < rest ? squ[32 + lane] : 0;
+                            __syncwarp();
+                            if (lane < rest) squ[lane] = v;
+                            __syncwarp();
+                            nq = rest;
                         }
                     }
                 }
+            if (nq > 0) exact(nq);
             if (nbuf > 0) warp_sort_pairs(dd2, didx, nbuf, lane);
             nd = min(nbuf, k);
         }
@@ -134,7 +181,7 @@ search_kernel(const SearchArgs a) {
             // no template entry from here on can enter the k nearest once
             // ng grid + the data strictly nearer than this entry fill k
             if (nd > 0) {
-                const double dcur = a.tmpl_d2[base];
+                const long long dcur = tkey[base];
                 int before = 0;
                 for (int q = lane; q < nd; q += 32) before += dd2[q] < dcur ? 1 : 0;
 #pragma unroll
@@ -157,7 +204,7 @@ search_kernel(const SearchArgs a) {
                 const int p = ng + __popc(b & lt);
                 if (p < k) {
                     gidx[p] = c;
-                    gd2[p] = a.tmpl_d2[j];
+                    gd2[p] = tkey[j];
                 }
             }
             ng += __popc(b);
@@ -169,7 +216,7 @@ search_kernel(const SearchArgs a) {
         int32_t* out = a.nbr + (int64_t)g * k;
         int ngrid = 0;
         for (int q = lane; q < ng; q += 32) {
-            const double d = gd2[q];
+            const long long d = gd2[q];
             int lo = 0, hi = nd;  // data strictly nearer
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;
@@ -182,7 +229,7 @@ search_kernel(const SearchArgs a) {
             }
         }
         for (int q = lane; q < nd; q += 32) {
-            const double d = dd2[q];
+            const long long d = dd2[q];
             int lo = 0, hi = ng;  // grid at distance <= d
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;

@@ -7,17 +7,17 @@
 // the prior fallback when the factorization fails or the node has fewer
 // than minneighbors neighbours (seqsim.jl:109-111,127-131).
 //
-// One warp per system, LHS in shared memory.  Grid-grid covariances come
-// from an FP64 table over integer lags (every neighbour of a node is a cell
-// offset inside the search template, so pairwise lags are bounded); lags
-// involving data points are evaluated directly in FP64.
+// One warp per system.  Grid-grid covariances come from a table over integer
+// lags (every neighbour of a node is a cell offset inside the search
+// template, so pairwise lags are bounded); lags involving data points are
+// evaluated directly in FP64, 32 per warp pass.
 //
 // Precision modes:
-//   FP64          FP64 LHS, Cholesky, weights (the plain path)
-//   FP32+refine   FP32 LHS + Cholesky; iterative refinement with the FP64
-//                 residual r = c - C w; FP64 variance.  A system whose FP32
-//                 pivot falls below 1e-3*sill or whose refinement does not
-//                 contract is queued and re-solved in FP64.
+//   FP64          FP64 LHS, right-looking Cholesky in shared memory, FP64
+//                 weights (the plain path; also re-solves queued systems)
+//   FP32+refine   register-resident Gauss-Jordan inverse of the FP32 LHS,
+//                 refinement against a double-FP32 LHS with a compensated
+//                 residual, double-FP32 variance (solve_fp32_kernel below)
 // Results are written in level order (the sweep's layout): the grid
 // neighbours with their weights, and the data neighbours folded into the
 // constant b0 = sum_data w_i (d_i - mu).
@@ -65,6 +65,21 @@ __device__ __forceinline__ double kcov(const SolveArgs& a, const NbInfo& p, cons
     point_of(a, p, xp);
     point_of(a, q, xq);
     return cov_fp64(a.vario, a.grid.dim, dsub(xq[0], xp[0]), dsub(xq[1], xp[1]), dsub(xq[2], xp[2]));
+}
+
+// Indices of the neighbours that are data points, in order, into dl; returns
+// their number (warp-uniform).
+__device__ __forceinline__ int collect_data(const NbInfo* info, int n, int* dl, int lane) {
+    int nd = 0;
+    for (int b = 0; b < n; b += 32) {
+        const int q = b + lane;
+        const bool isdata = q < n && info[q].did >= 0;
+        const unsigned bal = __ballot_sync(FULL_MASK, isdata);
+        if (isdata) dl[nd + __popc(bal & lanemask_lt())] = q;
+        nd += __popc(bal);
+    }
+    __syncwarp();
+    return nd;
 }
 
 // Right-looking Cholesky of the lower triangle of A (leading dimension ld)
@@ -127,6 +142,14 @@ __host__ __device__ constexpr size_t warp_smem_bytes(int k) {
            ((size_t)k * sizeof(T) + 15) / 16 * 16 + (size_t)k * sizeof(NbInfo);
 }
 
+// Store an FP64 value into a table entry: as is, or as an FP32 (hi, lo) pair.
+__device__ __forceinline__ void put(double* t, int64_t i, double v) { t[i] = v; }
+__device__ __forceinline__ void put(float* t, int64_t i, double v) {
+    const float hi = (float)v;
+    t[2 * i] = hi;
+    t[2 * i + 1] = (float)(v - (double)hi);
+}
+
 // Write one position's sweep-table row (and the optional node-indexed export).
 template <typename O>
 __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t pos, int g, int n,
@@ -142,7 +165,7 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
             if (isgrid) {
                 const int j = m + __popc(b & lanemask_lt());
                 tab.idx[pos * k + j] = a.nbr[(int64_t)g * k + q];
-                tab.w[pos * k + j] = (O)w[q];
+                put(tab.w, pos * k + j, w[q]);
             } else if (q < n) {
                 b0 += w[q] * (a.data_val[info[q].did] - a.mu);
             }
@@ -154,8 +177,8 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
         if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
         tab.node[pos] = g;
         tab.m[pos] = m;
-        tab.b0[pos] = (O)b0;
-        tab.sigma[pos] = (O)sigma;
+        put(tab.b0, pos, b0);
+        put(tab.sigma, pos, sigma);
         a.status[g] = (int8_t)status;
     }
     if (a.w_full) {
@@ -165,9 +188,11 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
     }
 }
 
-// T: factorization type; O: table type; REFINE: FP32 + FP64 refinement with
-// fallback queue.  With a.list set, solves only the queued positions.
-template <typename T, typename O, bool REFINE>
+// The plain FP64 path (T = double): FP64 LHS, Cholesky and weights.  O is the
+// table type: double for the FP64 path, float (hi, lo pairs) when it re-solves
+// the systems the FP32 path queued.  With a.list set, solves only the queued
+// positions.
+template <typename T, typename O>
 __global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs a, const SweepTables<O> tab) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -211,62 +236,33 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs
         }
         __syncwarp();
         for (int q = lane; q < n; q += 32) c[q] = kcov(a, info[q], self);
-        for (int r = 0; r < n; ++r)
-            for (int q = lane; q <= r; q += 32) A[r * ld + q] = (T)kcov(a, info[q], info[r]);
+        for (int r = 0; r < n; ++r) {
+            const NbInfo ir = info[r];
+            if (ir.did >= 0) continue;
+            for (int q = lane; q <= r; q += 32) {
+                const NbInfo iq = info[q];
+                if (iq.did < 0) A[r * ld + q] = (T)kcov(a, iq, ir);
+            }
+        }
+        {
+            int* dl = reinterpret_cast<int*>(rhs);
+            const int nd = collect_data(info, n, dl, lane);
+            for (int item = lane; item < nd * n; item += 32) {
+                const int da = dl[item / n], q = item % n;
+                const NbInfo iq = info[q];
+                if (iq.did >= 0 && q > da) continue;
+                A[(da >= q ? da : q) * ld + (da >= q ? q : da)] = (T)kcov(a, iq, info[da]);
+            }
+        }
         __syncwarp();
 
-        bool ok;
-        if (!REFINE) {
-            ok = warp_cholesky<T>(A, ld, n, (T)a.tau, lane);
-            if (ok) {
-                for (int q = lane; q < n; q += 32) rhs[q] = (T)c[q];
-                __syncwarp();
-                warp_chol_solve<T>(A, ld, n, rhs, lane);
-                for (int q = lane; q < n; q += 32) w[q] = (double)rhs[q];
-                __syncwarp();
-            }
-        } else {
-            const T guard = (T)(1e-3 * sill);
-            ok = warp_cholesky<T>(A, ld, n, guard, lane);
-            bool accept = ok;
-            if (ok) {
-                for (int q = lane; q < n; q += 32) rhs[q] = (T)c[q];
-                __syncwarp();
-                warp_chol_solve<T>(A, ld, n, rhs, lane);
-                for (int q = lane; q < n; q += 32) w[q] = (double)rhs[q];
-                __syncwarp();
-                double prev = 0.0, last = 0.0;
-                for (int s = 0; s < a.refine_steps; ++s) {
-                    // FP64 residual r = c - C w, one row per lane
-                    for (int i = lane; i < n; i += 32) {
-                        double r = c[i];
-                        for (int j = 0; j < n; ++j) r -= kcov(a, info[j], info[i]) * w[j];
-                        rhs[i] = (T)r;
-                    }
-                    __syncwarp();
-                    warp_chol_solve<T>(A, ld, n, rhs, lane);
-                    double dmax = 0.0;
-                    for (int q = lane; q < n; q += 32) {
-                        const double dq = (double)rhs[q];
-                        w[q] += dq;
-                        dmax = fmax(dmax, fabs(dq));
-                    }
-                    __syncwarp();
-                    prev = last;
-                    last = warp_max(dmax);
-                }
-                // remaining error ~ contraction * last correction
-                if (a.refine_steps >= 2) {
-                    const double rho = prev > 0.0 ? last / prev : 0.0;
-                    accept = rho < 0.5 && rho * last <= 1e-9 && isfinite(last);
-                } else {
-                    accept = isfinite(last);
-                }
-            }
-            if (!accept) {
-                if (lane == 0) a.fallback[atomicAdd(a.nfallback, 1)] = (int32_t)pos;
-                continue;
-            }
+        const bool ok = warp_cholesky<T>(A, ld, n, (T)a.tau, lane);
+        if (ok) {
+            for (int q = lane; q < n; q += 32) rhs[q] = (T)c[q];
+            __syncwarp();
+            warp_chol_solve<T>(A, ld, n, rhs, lane);
+            for (int q = lane; q < n; q += 32) w[q] = (double)rhs[q];
+            __syncwarp();
         }
         if (!ok) {
             write_row<O>(a, tab, pos, g, n, info, w, prior_sd, SGS_NODE_PRIOR_SINGULAR_, lane);
@@ -281,39 +277,363 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs
     }
 }
 
-template <typename T, typename O, bool REFINE>
+template <typename T, typename O>
 static cudaError_t launch_solve(const SolveArgs& a, const SweepTables<O>& t, cudaStream_t s) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const size_t smem = warp_smem_bytes<T>(a.k) * SOLVE_WARPS;
-    cudaError_t e = cudaFuncSetAttribute(solve_kernel<T, O, REFINE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(solve_kernel<T, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_kernel<T, O, REFINE>, SOLVE_WARPS * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_kernel<T, O>, SOLVE_WARPS * 32, smem);
     if (per_sm < 1) per_sm = 1;
     int64_t want = a.list ? (int64_t)nsm * per_sm : (a.P + SOLVE_WARPS - 1) / SOLVE_WARPS;
     int blocks = (int)(want < (int64_t)nsm * per_sm ? want : (int64_t)nsm * per_sm);
     if (blocks < 1) blocks = 1;
-    solve_kernel<T, O, REFINE><<<blocks, SOLVE_WARPS * 32, smem, s>>>(a, t);
+    solve_kernel<T, O><<<blocks, SOLVE_WARPS * 32, smem, s>>>(a, t);
     return cudaGetLastError();
 }
 
 cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, cudaStream_t s) {
-    return launch_solve<double, double, false>(a, t, s);
-}
-
-cudaError_t launch_solve_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s) {
-    return launch_solve<float, float, true>(a, t, s);
-}
-
-cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s) {
-    return launch_solve<double, float, false>(a, t, s);
+    return launch_solve<double, double>(a, t, s);
 }
 
 // ---------------------------------------------------------------------------
-__global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut t, double* c64, float* c32,
+// FP32 path.  One warp per system, lane l owning rows l and l + 32 of the
+// system in registers.  The LHS is normalized by the sill (a correlation
+// matrix: pivots in (0, 1], weights unchanged) and kept in shared memory as
+// double-FP32 pairs (hi + lo, about 48 bits); grid-grid entries come from the
+// (hi, lo) lag table, entries involving a datum from one FP64 evaluation each,
+// packed 32 per pass.  Its FP32 copy is inverted in registers by the
+// Gauss-Jordan sweep operator (Goodnight 1979; no pivoting, which is stable
+// for symmetric positive definite matrices, and whose k-th pivot is the same
+// Schur complement a Cholesky factorization would test).  Every solve is then
+// a lane-parallel matrix-vector product instead of a sequential triangular
+// solve.  The weights are refined against the double-FP32 LHS: the residual
+// r = c - K w is accumulated with compensated (Dot2) FP32 arithmetic, which
+// carries the accuracy of an FP64 residual without GB300's narrow FP64 pipe.
+// Weights, sigma^2 = sill (1 - w'c) and b0 stay double-FP32 and are written as
+// (hi, lo) pairs for the compensated sweep.  A system with a pivot below
+// 1e-3 (near-singular: the canonical 1e-10 decision needs FP64) or whose
+// refinement does not contract is queued for the FP64 kernel.
+constexpr int SOLVE32_WARPS = 2;
+
+template <int NMAX>
+struct Smem32 {
+    static constexpr int LDK = NMAX + 1;  // odd row stride: conflict-free row reads
+    static constexpr size_t K = (size_t)NMAX * LDK * sizeof(DF);
+    static constexpr size_t C = (size_t)NMAX * sizeof(DF);
+    static constexpr size_t W = (size_t)NMAX * sizeof(DF);
+    static constexpr int CB = NMAX > 32 ? 64 : 32;  // one entry per owned row
+    static constexpr size_t V = (size_t)CB * sizeof(float);
+    static constexpr size_t COL = 2 * (size_t)CB * sizeof(float);
+    static constexpr size_t INFO = (size_t)NMAX * sizeof(NbInfo);
+    static constexpr size_t bytes = K + C + W + V + COL + INFO;
+    static_assert(K % 16 == 0 && bytes % 16 == 0, "16-byte aligned per-warp layout");
+};
+
+// normalized double-FP32 covariance between two points of the augmented set
+__device__ __forceinline__ DF kcov2n(const SolveArgs& a, const NbInfo& p, const NbInfo& q) {
+    if (p.did < 0 && q.did < 0) {
+        const CovLut& t = a.lut;
+        const int L0 = q.c0 - p.c0, L1 = q.c1 - p.c1, L2 = q.c2 - p.c2;
+        if (t.c2 != nullptr && L0 >= -t.e[0] && L0 <= t.e[0] && L1 >= -t.e[1] && L1 <= t.e[1] && L2 >= -t.e[2] &&
+            L2 <= t.e[2]) {
+            const float2 v = t.c2[(L0 + t.e[0]) + t.w[0] * ((L1 + t.e[1]) + t.w[1] * (L2 + t.e[2]))];
+            return {v.x, v.y};
+        }
+    }
+    return df_from_double(kcov(a, p, q) * a.inv_sill);
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return df_fast_two_sum(p, __fadd_rn(e, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
+}
+
+template <int NMAX>
+__global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const SolveArgs a, const SweepTables<float> tab) {
+    using S = Smem32<NMAX>;
+    constexpr int LDK = S::LDK;
+    constexpr bool TWO = NMAX > 32;  // lanes own a second row
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * S::bytes;
+    DF* K = reinterpret_cast<DF*>(base);
+    DF* c = reinterpret_cast<DF*>(base + S::K);
+    DF* w = reinterpret_cast<DF*>(base + S::K + S::C);
+    float* vec = reinterpret_cast<float*>(base + S::K + S::C + S::W);
+    float* colb = reinterpret_cast<float*>(base + S::K + S::C + S::W + S::V);
+    NbInfo* info = reinterpret_cast<NbInfo*>(base + S::K + S::C + S::W + S::V + S::COL);
+    const GridDev& G = a.grid;
+    const int k = a.k;
+    const DF sd_sill = df_sqrt(df_from_double(a.vario.sill));
+    const int64_t nwarps = (int64_t)gridDim.x * SOLVE32_WARPS;
+    const int i0 = lane, i1 = lane + 32;
+
+    for (int64_t pos = (int64_t)blockIdx.x * SOLVE32_WARPS + wib; pos < a.P; pos += nwarps) {
+        const int g = a.order[pos];
+        const int n = a.cnt[g];
+        int status = SGS_NODE_KRIGED_;
+        DF sigma = sd_sill;
+        if (n < a.nmin) {
+            status = SGS_NODE_PRIOR_NMIN_;
+        } else {
+            NbInfo self;
+            cell_of(G, g, self.c0, self.c1, self.c2);
+            self.did = -1;
+            for (int q = lane; q < n; q += 32) {
+                const int id = a.nbr[(int64_t)g * k + q];
+                NbInfo in;
+                if (id < G.N) {
+                    cell_of(G, id, in.c0, in.c1, in.c2);
+                    in.did = -1;
+                } else {
+                    in.c0 = in.c1 = in.c2 = 0;
+                    in.did = id - (int)G.N;
+                }
+                info[q] = in;
+            }
+            __syncwarp();
+            for (int q = lane; q < n; q += 32) c[q] = kcov2n(a, info[q], self);
+            for (int r = 0; r < n; ++r) {
+                const NbInfo ir = info[r];
+                if (ir.did >= 0) continue;
+                for (int q = lane; q <= r; q += 32) {
+                    const NbInfo iq = info[q];
+                    if (iq.did < 0) {
+                        const DF v = kcov2n(a, iq, ir);
+                        K[r * LDK + q] = v;
+                        K[q * LDK + r] = v;
+                    }
+                }
+            }
+            {
+                int* dl = reinterpret_cast<int*>(vec);
+                const int nd = collect_data(info, n, dl, lane);
+                for (int item = lane; item < nd * n; item += 32) {
+                    const int da = dl[item / n], q = item % n;
+                    const NbInfo iq = info[q];
+                    if (iq.did >= 0 && q > da) continue;  // data-data pair once
+                    const DF v = df_from_double(kcov(a, iq, info[da]) * a.inv_sill);
+                    K[da * LDK + q] = v;
+                    K[q * LDK + da] = v;
+                }
+            }
+            __syncwarp();
+            // ---- rows of the FP32 LHS into registers (identity padding) ----
+            float R0[NMAX], R1[TWO ? NMAX : 1];
+#pragma unroll
+            for (int j = 0; j < NMAX; ++j) {
+                R0[j] = (i0 < n && j < n) ? K[i0 * LDK + j].hi : (i0 == j ? 1.0f : 0.0f);
+                if (TWO) R1[j] = (i1 < n && j < n) ? K[i1 * LDK + j].hi : (i1 == j ? 1.0f : 0.0f);
+            }
+            // ---- Gauss-Jordan sweep with column rotation: R -> -K^-1 ----
+            // At step kk register j holds column (kk + j) mod NMAX, so the pivot
+            // column is always register 0 and every register index is static
+            // in a rolled loop (a fully unrolled sweep overflows the
+            // instruction cache).  The pivot column is broadcast through shared
+            // memory already rotated (slot j <- row (kk + j + 1) mod NMAX, which
+            // by symmetry is row kk's entry for register j + 1).  NMAX steps
+            // bring the columns back in place; padding pivots are exactly 1.
+            bool ok = true;
+            const bool own0 = i0 < NMAX, own1 = TWO && i1 < NMAX;
+#pragma unroll 1
+            for (int kk = 0; kk < NMAX; ++kk) {
+                const float d = __shfl_sync(FULL_MASK, kk < 32 ? R0[0] : R1[0], kk & 31);
+                if (!(d > 1e-3f)) {  // warp-uniform
+                    ok = false;
+                    break;
+                }
+                const float inv = __frcp_rn(d);
+                float* cb = colb + (kk & 1) * S::CB;
+                if (own0) {
+                    int p = i0 - kk - 1;
+                    cb[p < 0 ? p + NMAX : p] = R0[0];
+                }
+                if (own1) {
+                    int p = i1 - kk - 1;
+                    cb[p < 0 ? p + NMAX : p] = R1[0];
+                }
+                __syncwarp();
+                // owner row: A[k][j] / d == A[k][j] - (1 - 1/d) A[k][j]
+                const float a0 = i0 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R0[0], inv);
+                const float a1 = TWO ? (i1 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R1[0], inv)) : 0.0f;
+#pragma unroll
+                for (int j = 0; j < NMAX - 1; ++j) {
+                    const float akj = cb[j];
+                    R0[j] = __fmaf_rn(-a0, akj, R0[j + 1]);
+                    if (TWO) R1[TWO ? j : 0] = __fmaf_rn(-a1, akj, R1[TWO ? j + 1 : 0]);
+                }
+                R0[NMAX - 1] = i0 == kk ? -inv : a0;
+                if (TWO) R1[TWO ? NMAX - 1 : 0] = i1 == kk ? -inv : a1;
+            }
+            bool accept = ok;
+            if (accept) {
+                // w = K^-1 c = -R c
+                for (int q = lane; q < S::CB; q += 32) vec[q] = q < n ? c[q].hi : 0.0f;
+                __syncwarp();
+                float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                for (int j = 0; j < NMAX; ++j) {
+                    const float v = vec[j];
+                    s0 = __fmaf_rn(-R0[j], v, s0);
+                    if (TWO) s1 = __fmaf_rn(-R1[j], v, s1);
+                }
+                DF w0 = {s0, 0.0f}, w1 = {s1, 0.0f};
+                if (i0 < n) w[i0] = w0;
+                if (TWO && i1 < n) w[i1] = w1;
+                __syncwarp();
+                float prev = 0.0f, last = 0.0f;
+                float r0 = 0.0f, r1 = 0.0f;
+                for (int s = 0;; ++s) {
+                    // residual r = c - K w in double-FP32, own rows; the last
+                    // one (of the final weights) also feeds the variance
+                    r0 = 0.0f;
+                    r1 = 0.0f;
+                    if (i0 < n) {
+                        DFAcc acc;
+                        acc.init(c[i0]);
+                        for (int j = 0; j < n; ++j) acc.add_prod(df_neg(K[i0 * LDK + j]), w[j]);
+                        r0 = acc.value().hi;
+                    }
+                    if (TWO && i1 < n) {
+                        DFAcc acc;
+                        acc.init(c[i1]);
+                        for (int j = 0; j < n; ++j) acc.add_prod(df_neg(K[i1 * LDK + j]), w[j]);
+                        r1 = acc.value().hi;
+                    }
+                    if (s == a.refine_steps) break;
+                    __syncwarp();
+                    vec[i0] = r0;
+                    if (TWO) vec[i1] = r1;
+                    __syncwarp();
+                    float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < NMAX; ++j) {
+                        const float v = vec[j];
+                        d0 = __fmaf_rn(-R0[j], v, d0);
+                        if (TWO) d1 = __fmaf_rn(-R1[j], v, d1);
+                    }
+                    float dmax = 0.0f;
+                    if (i0 < n) {
+                        const DF t = df_two_sum(w0.hi, d0);
+                        w0 = df_fast_two_sum(t.hi, __fadd_rn(t.lo, w0.lo));
+                        w[i0] = w0;
+                        dmax = fabsf(d0);
+                    }
+                    if (TWO && i1 < n) {
+                        const DF t = df_two_sum(w1.hi, d1);
+                        w1 = df_fast_two_sum(t.hi, __fadd_rn(t.lo, w1.lo));
+                        w[i1] = w1;
+                        dmax = fmaxf(dmax, fabsf(d1));
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(FULL_MASK, dmax, o));
+                    prev = last;
+                    last = dmax;
+                    __syncwarp();
+                }
+                // the remaining error is about the contraction factor times the
+                // last correction
+                if (a.refine_steps >= 2) {
+                    const float rho = prev > 0.0f ? last / prev : 0.0f;
+                    accept = rho < 0.5f && rho * last <= 1e-9f && isfinite(last);
+                } else {
+                    accept = isfinite(last);
+                }
+                if (accept) {
+                    // sigma^2 = sill (1 - w'c - w'r) with r = c - K w: equal to
+                    // sill - w'c at the exact weights, but stationary there
+                    // (its error is second order in the weights' error), so
+                    // it stays accurate where the variance cancels to ~0 (a
+                    // node on a datum), where sqrt would magnify any error
+                    DFAcc acc;
+                    acc.init({0.0f, 0.0f});
+                    if (i0 < n) acc.add_prod(w0, df_add(c[i0], {r0, 0.0f}));
+                    if (TWO && i1 < n) acc.add_prod(w1, df_add(c[i1], {r1, 0.0f}));
+                    const DF wc = warp_sum_df(acc.value());
+                    sigma = df_mul(sd_sill, df_sqrt(df_add({1.0f, 0.0f}, df_neg(wc))));
+                }
+            }
+            if (!accept) {
+                if (lane == 0) a.fallback[atomicAdd(a.nfallback, 1)] = (int32_t)pos;
+                __syncwarp();
+                continue;
+            }
+        }
+        // ---- table row: grid neighbours with (hi, lo) weights, data folded into b0
+        int m = 0;
+        DFAcc b0acc;
+        b0acc.init({0.0f, 0.0f});
+        if (status == SGS_NODE_KRIGED_) {
+            for (int b = 0; b < n; b += 32) {
+                const int q = b + lane;
+                const bool isgrid = q < n && info[q].did < 0;
+                const unsigned bal = __ballot_sync(FULL_MASK, isgrid);
+                if (isgrid) {
+                    const int j = m + __popc(bal & lanemask_lt());
+                    tab.idx[pos * k + j] = a.nbr[(int64_t)g * k + q];
+                    reinterpret_cast<float2*>(tab.w)[pos * k + j] = make_float2(w[q].hi, w[q].lo);
+                } else if (q < n) {
+                    b0acc.add_prod(w[q], df_from_double(a.data_val[info[q].did] - a.mu));
+                }
+                m += __popc(bal);
+            }
+        }
+        const DF b0 = warp_sum_df(b0acc.value());
+        if (lane == 0) {
+            if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
+            tab.node[pos] = g;
+            tab.m[pos] = m;
+            reinterpret_cast<float2*>(tab.b0)[pos] = make_float2(b0.hi, b0.lo);
+            reinterpret_cast<float2*>(tab.sigma)[pos] = make_float2(sigma.hi, sigma.lo);
+            a.status[g] = (int8_t)status;
+        }
+        if (a.w_full) {
+            for (int q = lane; q < k; q += 32)
+                a.w_full[(int64_t)g * k + q] =
+                    (status == SGS_NODE_KRIGED_ && q < n) ? (double)w[q].hi + (double)w[q].lo : 0.0;
+            if (lane == 0) a.sigma_full[g] = (double)sigma.hi + (double)sigma.lo;
+        }
+        __syncwarp();
+    }
+}
+
+template <int NMAX>
+static cudaError_t launch_solve32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t smem = Smem32<NMAX>::bytes * SOLVE32_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(solve_fp32_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_fp32_kernel<NMAX>, SOLVE32_WARPS * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    int64_t want = (a.P + SOLVE32_WARPS - 1) / SOLVE32_WARPS;
+    int blocks = (int)(want < (int64_t)nsm * per_sm ? want : (int64_t)nsm * per_sm);
+    if (blocks < 1) blocks = 1;
+    solve_fp32_kernel<NMAX><<<blocks, SOLVE32_WARPS * 32, smem, s>>>(a, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s) {
+    if (a.k <= 16) return launch_solve32<16>(a, t, s);
+    if (a.k <= 32) return launch_solve32<32>(a, t, s);
+    if (a.k <= 48) return launch_solve32<48>(a, t, s);
+    return launch_solve32<64>(a, t, s);
+}
+
+cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s) {
+    return launch_solve<double, float>(a, t, s);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut t, double* c64, float2* c2,
                                 int64_t total) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
         const int L0 = (int)(i % t.w[0]) - t.e[0];
@@ -323,16 +643,20 @@ __global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut 
         const double c = cov_fp64(v, G.dim, dmul((double)L0, G.spacing[0]), dmul((double)L1, G.spacing[1]),
                                   G.dim == 3 ? dmul((double)L2, G.spacing[2]) : 0.0);
         c64[i] = c;
-        if (c32) c32[i] = (float)c;
+        if (c2) {  // normalized by the sill, as (hi, lo) for the FP32 path
+            const double cn = c / v.sill;
+            const float hi = (float)cn;
+            c2[i] = make_float2(hi, (float)(cn - (double)hi));
+        }
     }
 }
 
-cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float* c32,
+cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2,
                                 cudaStream_t s) {
     const int64_t total = (int64_t)lut.w[0] * lut.w[1] * lut.w[2];
     int blocks = (int)((total + 255) / 256);
     if (blocks > 65535) blocks = 65535;
-    fill_lut_kernel<<<blocks, 256, 0, s>>>(g, v, lut, c64, c32, total);
+    fill_lut_kernel<<<blocks, 256, 0, s>>>(g, v, lut, c64, c2, total);
     return cudaGetLastError();
 }
 

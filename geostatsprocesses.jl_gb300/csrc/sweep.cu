@@ -21,10 +21,6 @@ struct Vec4<float> {
     __device__ static void store(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 };
 
-__device__ __forceinline__ float4 fma4(float w, float4 v, float4 a) {
-    return make_float4(fmaf(w, v.x, a.x), fmaf(w, v.y, a.y), fmaf(w, v.z, a.z), fmaf(w, v.w, a.w));
-}
-
 struct D4 {
     double x, y, z, w;
 };
@@ -38,6 +34,30 @@ __device__ __forceinline__ void store_d4(double* p, D4 v) {
     reinterpret_cast<double2*>(p)[1] = make_double2(v.z, v.w);
 }
 
+// Compensated dot product in FP32 (Dot2: Ogita, Rump & Oishi 2005, "Accurate
+// sum and dot product"): the product w*x is split exactly into p + pe with an
+// FMA, p is added to the running sum s with TwoSum (Knuth), and every
+// rounding error, plus the low part of the weight, goes into the correction
+// c.  s + c carries the dot product to about twice FP32 precision; only the
+// final rounding to the stored FP32 value remains.
+struct Dot2 {
+    float s, c;
+    __device__ __forceinline__ void init(float hi, float lo) {
+        s = hi;
+        c = lo;
+    }
+    __device__ __forceinline__ void add(float wh, float wl, float x) {
+        const float p = __fmul_rn(wh, x);
+        const float pe = __fmaf_rn(wh, x, -p);
+        const float t = __fadd_rn(s, p);
+        const float bp = __fsub_rn(t, s);
+        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(e, __fmaf_rn(wl, x, pe)));
+    }
+    __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
+};
+
 // One thread per (node, chunk of 4 realizations).
 __global__ void __launch_bounds__(256) sweep_fp32_kernel(const SweepTables<float> t, int k, int64_t p0,
                                                          int64_t p1, int Rp, const float* __restrict__ z,
@@ -50,18 +70,30 @@ __global__ void __launch_bounds__(256) sweep_fp32_kernel(const SweepTables<float
         const int ch = (int)(i % cpn);
         const int g = t.node[pos];
         const int m = t.m[pos];
-        const float b0 = t.b0[pos];
-        float4 acc = make_float4(b0, b0, b0, b0);
+        const float2 b0 = reinterpret_cast<const float2*>(t.b0)[pos];
+        Dot2 a0, a1, a2, a3;
+        a0.init(b0.x, b0.y);
+        a1.init(b0.x, b0.y);
+        a2.init(b0.x, b0.y);
+        a3.init(b0.x, b0.y);
         const int32_t* idx = t.idx + pos * k;
-        const float* w = t.w + pos * k;
+        const float2* w = reinterpret_cast<const float2*>(t.w) + pos * k;
 #pragma unroll 4
         for (int j = 0; j < m; ++j) {
             const float4 v = Vec4<float>::load(V + (int64_t)idx[j] * Rp + 4 * ch);
-            acc = fma4(w[j], v, acc);
+            const float2 wj = w[j];
+            a0.add(wj.x, wj.y, v.x);
+            a1.add(wj.x, wj.y, v.y);
+            a2.add(wj.x, wj.y, v.z);
+            a3.add(wj.x, wj.y, v.w);
         }
         const float4 zz = z ? Vec4<float>::load(z + (int64_t)g * Rp + 4 * ch) : normals4(seed, g, ch);
-        acc = fma4(t.sigma[pos], zz, acc);
-        Vec4<float>::store(V + (int64_t)g * Rp + 4 * ch, acc);
+        const float2 sg = reinterpret_cast<const float2*>(t.sigma)[pos];
+        a0.add(sg.x, sg.y, zz.x);
+        a1.add(sg.x, sg.y, zz.y);
+        a2.add(sg.x, sg.y, zz.z);
+        a3.add(sg.x, sg.y, zz.w);
+        Vec4<float>::store(V + (int64_t)g * Rp + 4 * ch, make_float4(a0.value(), a1.value(), a2.value(), a3.value()));
     }
 }
 

@@ -1,0 +1,181 @@
+# ------------------------------------------------------------------
+# GeoStatsProcessesGPU — GPUSEQSIM, sequential Gaussian simulation on one
+# GB300, plugged into GeoStatsProcesses.jl's field-simulation method API
+# through libgeosgs.so (include/geosgs.h).
+#
+#   using GeoStatsProcesses, GeoStatsProcessesGPU
+#   ens = rand(rng, GaussianProcess(γ), grid, 256; data,
+#              method=GPUSEQSIM(path=RandomPath(), maxneighbors=48))
+#
+# GPUSEQSIM plugs in the way SEQSIM does (src/simulation/field/seqsim.jl:42-156):
+# a FieldSimulationMethod subtype (src/simulation/field.jl:135) with
+# `preprocess` and `randsingle` methods; `rand` (src/simulation/field.jl:73-124)
+# is not overridden.  The path is drawn once in `preprocess` and shared by all
+# realizations of the call; `randsingle` simulates realizations in blocks of
+# `batch` on the GPU and hands them out one by one.
+# ------------------------------------------------------------------
+module GeoStatsProcessesGPU
+
+using Random
+using Distributed: myid
+using Meshes
+using GeoTables
+using GeoStatsFunctions
+using Unitful: ustrip
+using GeoStatsProcesses
+import GeoStatsProcesses: preprocess, randsingle, FieldSimulationMethod
+
+export GPUSEQSIM
+
+const libgeosgs = get(ENV, "GEOSGS_LIB",
+  joinpath(@__DIR__, "..", "geosgs", "lib", "libgeosgs.so"))
+
+# ---- C structs (field order and types of include/geosgs.h) ----
+struct SgsVariogram
+  type::Int32
+  reserved::Int32
+  sill::Float64
+  nugget::Float64
+  ranges::NTuple{3,Float64}
+  rotation::NTuple{9,Float64}
+end
+
+struct SgsBall
+  radii::NTuple{3,Float64}
+  rotation::NTuple{9,Float64}
+end
+
+struct SgsProblem
+  dim::Int32
+  dims::NTuple{3,Int32}
+  origin::NTuple{3,Float64}
+  spacing::NTuple{3,Float64}
+  ndata::Int64
+  data_coords::Ptr{Float64}
+  data_values::Ptr{Float64}
+  variogram::SgsVariogram
+  mean::Float64
+  minneighbors::Int32
+  maxneighbors::Int32
+  search::Int32
+  precision::Int32
+  ball::SgsBall
+  path::Ptr{Int32}
+  refine_steps::Int32
+  warm_start::Int32
+  device::Int32
+  flags::Int32
+end
+
+const SGS_SEARCH_RANGE, SGS_SEARCH_BALL, SGS_SEARCH_NEAREST = Int32(0), Int32(1), Int32(2)
+
+"""
+    GPUSEQSIM(; path, minneighbors, maxneighbors, neighborhood, precision, refine_steps, batch, device)
+
+SEQSIM's options (`path`, `minneighbors`, `maxneighbors`, `neighborhood`)
+plus `precision` (`:fp32` = FP32 solves with FP64 refinement, `:fp64`),
+`refine_steps`, `batch` (realizations simulated per GPU call) and `device`.
+"""
+Base.@kwdef struct GPUSEQSIM{P,N} <: FieldSimulationMethod
+  path::P = LinearPath()
+  minneighbors::Int = 1
+  maxneighbors::Int = 26
+  neighborhood::N = :range
+  precision::Symbol = :fp32
+  refine_steps::Int = 2
+  batch::Int = 64
+  device::Int = 0
+end
+
+mutable struct GPUPlan
+  ptr::Ptr{Cvoid}
+  owner::Int
+  function GPUPlan(ptr)
+    p = new(ptr, myid())
+    finalizer(p) do q
+      q.ptr == C_NULL || ccall((:sgs_plan_destroy, libgeosgs), Cvoid, (Ptr{Cvoid},), q.ptr)
+      q.ptr = C_NULL
+    end
+  end
+end
+
+function check(rc, ptr)
+  rc == 0 && return
+  msg = unsafe_string(ccall((:sgs_last_error, libgeosgs), Cstring, (Ptr{Cvoid},), ptr))
+  rc == -1 ? throw(ArgumentError(msg)) : error("libgeosgs ($rc): $msg")
+end
+
+vtype(::SphericalVariogram) = Int32(1)
+vtype(::ExponentialVariogram) = Int32(2)
+vtype(::GaussianVariogram) = Int32(3)
+vtype(f) = throw(ArgumentError("GPUSEQSIM supports spherical, exponential and gaussian variograms"))
+
+pad3(t, fill) = ntuple(i -> i <= length(t) ? Float64(t[i]) : fill, 3)
+
+function rot9(R, dim)
+  M = Matrix{Float64}(I(3))
+  M[1:dim, 1:dim] .= Matrix(R)[1:dim, 1:dim]
+  ntuple(k -> M[(k - 1) % 3 + 1, (k - 1) ÷ 3 + 1], 9)  # column-major, leading dimension 3
+end
+
+function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, init, domain, data)
+  domain isa CartesianGrid || throw(ArgumentError("GPUSEQSIM simulates on a CartesianGrid"))
+  f = process.func
+  dim = embeddim(domain)
+  dims = size(domain)
+  orig = ustrip.(to(minimum(domain)))
+  spac = ustrip.(spacing(domain))
+  ball = f.ball
+  vg = SgsVariogram(vtype(f), 0, ustrip(sill(f)), ustrip(nugget(f)),
+                    pad3(ustrip.(radii(ball)), 1.0), rot9(rotation(ball), dim))
+  nb = method.neighborhood
+  search, sball = if nb === :range
+    SGS_SEARCH_RANGE, SgsBall((1.0, 1.0, 1.0), rot9(I(3), dim))
+  elseif nb isa MetricBall
+    SGS_SEARCH_BALL, SgsBall(pad3(ustrip.(radii(nb)), 1.0), rot9(rotation(nb), dim))
+  else
+    SGS_SEARCH_NEAREST, SgsBall((1.0, 1.0, 1.0), rot9(I(3), dim))
+  end
+  # data appended after the grid nodes, as SEQSIM's ExplicitInit (seqsim.jl:211-218,267-271)
+  xy = Float64[]
+  vals = Float64[]
+  var = :field
+  if !isnothing(data)
+    var = first(propertynames(values(data)))
+    for i in 1:nrow(data)
+      append!(xy, ustrip.(to(centroid(domain(data), i))))
+    end
+    vals = Float64.(ustrip.(getproperty(values(data), var)))
+  end
+  path = Int32.(collect(traverse(domain, method.path)) .- 1)  # one path for all realizations
+  planref = Ref{Ptr{Cvoid}}(C_NULL)
+  GC.@preserve xy vals path begin
+    prob = SgsProblem(Int32(dim), pad3(dims, 1.0) .|> Int32, pad3(orig, 0.0), pad3(spac, 1.0),
+                      length(vals), pointer(xy), pointer(vals), vg, Float64(ustrip(process.mean)),
+                      method.minneighbors, method.maxneighbors, search,
+                      method.precision === :fp64 ? Int32(0) : Int32(1), sball, pointer(path),
+                      method.refine_steps, 0, method.device, 0)
+    check(ccall((:sgs_plan_create, libgeosgs), Cint, (Ref{SgsProblem}, Ref{Ptr{Cvoid}}), prob, planref), C_NULL)
+  end
+  plan = GPUPlan(planref[])
+  check(ccall((:sgs_plan_prepare, libgeosgs), Cint, (Ptr{Cvoid},), plan.ptr), plan.ptr)
+  (; plan, var, nelm=nelements(domain), block=Ref(Matrix{Float64}(undef, 0, 0)), cursor=Ref(0))
+end
+
+function randsingle(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, domain, data, preproc)
+  (; plan, var, nelm, block, cursor) = preproc
+  # the plan lives on this process's GPU (src/simulation/field.jl:98-100 style check)
+  myid() == plan.owner || throw(ArgumentError("GPUSEQSIM realizations must run on the process that prepared them"))
+  if cursor[] == size(block[], 2)
+    B = Matrix{Float64}(undef, nelm, method.batch)  # N x batch, column = realization
+    check(ccall((:sgs_plan_simulate, libgeosgs), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Float64}, UInt64, Ptr{Float64}),
+                plan.ptr, method.batch, C_NULL, rand(rng, UInt64), B), plan.ptr)
+    block[] = B
+    cursor[] = 0
+  end
+  cursor[] += 1
+  (; var => block[][:, cursor[]])
+end
+
+end # module

@@ -30,8 +30,8 @@
 //    the ball by one factor and changes no distance order or covariance in
 //    exact arithmetic, so everything is evaluated in unscaled units.
 //  * isotropic ball: d2 = sum_j h_j^2, inside iff d2 <= r*r.  Ellipsoid:
-//    u_j = sum_i R(i,j) h_i, q_j = u_j / radius_j, d2 = sum_j q_j^2, inside
-//    iff d2 <= 1.  All sums in axis order, every operation rounded (built with
+//    u_j = sum_i R(i,j) h_i, q_j = u_j * (1 / radius_j) with the reciprocal
+//    rounded once, d2 = sum_j q_j^2, inside iff d2 <= 1.  All sums in axis order, every operation rounded (built with
 //    -ffp-contract=off; the GPU uses the _rn intrinsics).
 //  * neighbour order: ascending (d2, augmented index).
 //  * singular rule: the factorization fails when a pivot (before the square
@@ -65,6 +65,7 @@ struct Metric {
     int kind = 0;        // 0 iso, 1 ellipsoid, 2 unbounded (nearest)
     double rr = 0.0;     // r*r for iso
     double radii[3] = {1, 1, 1};
+    double inv[3] = {1, 1, 1};  // 1 / radii, rounded once
     double R[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     double ext[3] = {0, 0, 0};  // half extents of the bounding box (physical units)
 
@@ -80,7 +81,7 @@ struct Metric {
             double u = R[0 + 3 * j] * h[0];
             u = u + R[1 + 3 * j] * h[1];
             if (dim == 3) u = u + R[2 + 3 * j] * h[2];
-            double q = u / radii[j];
+            double q = u * inv[j];
             s = (j == 0) ? q * q : s + q * q;
         }
         return s;
@@ -186,7 +187,10 @@ struct oracle_plan {
 static void set_metric(Metric& m, int dim, int kind, const double* radii, const double* rot) {
     m.dim = dim;
     m.kind = kind;
-    for (int j = 0; j < 3; ++j) m.radii[j] = radii[j];
+    for (int j = 0; j < 3; ++j) {
+        m.radii[j] = radii[j];
+        m.inv[j] = 1.0 / radii[j];
+    }
     for (int j = 0; j < 9; ++j) m.R[j] = rot[j];
     if (kind == 0) {
         m.rr = radii[0] * radii[0];

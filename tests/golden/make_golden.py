@@ -53,7 +53,7 @@ def d2_metric(h, kind, radii, R, dim):
         u = u + R[1, j] * h[1]
         if dim == 3:
             u = u + R[2, j] * h[2]
-        q = u / radii[j]
+        q = u * (1.0 / radii[j])
         s = q * q if j == 0 else s + q * q
     return s
 

@@ -87,9 +87,13 @@ def test_c2_full_parity(precision, oracle_mod, geosgs_lib):
     io, co = O.neighbors()
     np.testing.assert_array_equal(cg, co)
     np.testing.assert_array_equal(ig, io)
-    _, _, stg = G.weights()
-    _, _, sto = O.weights()
+    wg, sg, stg = G.weights()
+    wo, so, sto = O.weights()
     np.testing.assert_array_equal(stg, sto)
+    kriged = sto == 0
+    np.testing.assert_allclose(wg[kriged], wo[kriged], rtol=0, atol=1e-10 if precision == "fp64" else 1e-8)
+    # at a node on a datum the variance cancels to ~0: compare variances
+    np.testing.assert_allclose(sg**2, so**2, rtol=0, atol=1e-10)
     z = np.random.default_rng(5).standard_normal((wl.nreals, O.N))
     err = rel_err(G.simulate(wl.nreals, z), O.simulate(wl.nreals, z))
     print(f"c2 {precision} max rel err {err:.3e}")
