@@ -462,11 +462,19 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                 // owner row: A[k][j] / d == A[k][j] - (1 - 1/d) A[k][j]
                 const float a0 = i0 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R0[0], inv);
                 const float a1 = TWO ? (i1 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R1[0], inv)) : 0.0f;
+                const float4* cb4 = reinterpret_cast<const float4*>(cb);  // 16-byte aligned
 #pragma unroll
-                for (int j = 0; j < NMAX - 1; ++j) {
-                    const float akj = cb[j];
-                    R0[j] = __fmaf_rn(-a0, akj, R0[j + 1]);
-                    if (TWO) R1[TWO ? j : 0] = __fmaf_rn(-a1, akj, R1[TWO ? j + 1 : 0]);
+                for (int j4 = 0; j4 < NMAX / 4; ++j4) {
+                    const float4 v = cb4[j4];
+                    const float akv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int j = 4 * j4 + t;
+                        if (j < NMAX - 1) {
+                            R0[j] = __fmaf_rn(-a0, akv[t], R0[j + 1]);
+                            if (TWO) R1[TWO ? j : 0] = __fmaf_rn(-a1, akv[t], R1[TWO ? j + 1 : 0]);
+                        }
+                    }
                 }
                 R0[NMAX - 1] = i0 == kk ? -inv : a0;
                 if (TWO) R1[TWO ? NMAX - 1 : 0] = i1 == kk ? -inv : a1;
@@ -488,12 +496,14 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                 if (TWO && i1 < n) w[i1] = w1;
                 __syncwarp();
                 float prev = 0.0f, last = 0.0f;
-                float r0 = 0.0f, r1 = 0.0f;
+                const int steps = a.refine_steps;
+                // weights and residual the variance is evaluated with: the last
+                // residual computed (it also drives the last correction)
+                DF sw0 = w0, sw1 = w1;
+                float sr0 = 0.0f, sr1 = 0.0f;
                 for (int s = 0;; ++s) {
-                    // residual r = c - K w in double-FP32, own rows; the last
-                    // one (of the final weights) also feeds the variance
-                    r0 = 0.0f;
-                    r1 = 0.0f;
+                    // residual r = c - K w in double-FP32, own rows
+                    float r0 = 0.0f, r1 = 0.0f;
                     if (i0 < n) {
                         DFAcc acc;
                         acc.init(c[i0]);
@@ -506,7 +516,13 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                         for (int j = 0; j < n; ++j) acc.add_prod(df_neg(K[i1 * LDK + j]), w[j]);
                         r1 = acc.value().hi;
                     }
-                    if (s == a.refine_steps) break;
+                    if (s + 1 >= steps) {
+                        sw0 = w0;
+                        sw1 = w1;
+                        sr0 = r0;
+                        sr1 = r1;
+                    }
+                    if (s == steps) break;  // steps == 0: no correction
                     __syncwarp();
                     vec[i0] = r0;
                     if (TWO) vec[i1] = r1;
@@ -536,6 +552,7 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                     prev = last;
                     last = dmax;
                     __syncwarp();
+                    if (s + 1 == steps) break;  // the final weights need no residual
                 }
                 // the remaining error is about the contraction factor times the
                 // last correction
@@ -553,8 +570,8 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                     // node on a datum), where sqrt would magnify any error
                     DFAcc acc;
                     acc.init({0.0f, 0.0f});
-                    if (i0 < n) acc.add_prod(w0, df_add(c[i0], {r0, 0.0f}));
-                    if (TWO && i1 < n) acc.add_prod(w1, df_add(c[i1], {r1, 0.0f}));
+                    if (i0 < n) acc.add_prod(sw0, df_add(c[i0], {sr0, 0.0f}));
+                    if (TWO && i1 < n) acc.add_prod(sw1, df_add(c[i1], {sr1, 0.0f}));
                     const DF wc = warp_sum_df(acc.value());
                     sigma = df_mul(sd_sill, df_sqrt(df_add({1.0f, 0.0f}, df_neg(wc))));
                 }
