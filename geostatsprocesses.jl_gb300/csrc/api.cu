@@ -201,6 +201,8 @@ int upload(sgs_plan* p, T** d, const T* h, size_t count) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+void sgs::set_thread_error(const char* msg) { g_create_err = msg; }
+
 extern "C" const char* sgs_version(void) { return "geosgs 0.1.0 (sm_103a)"; }
 
 extern "C" const char* sgs_last_error(const sgs_plan* plan) {

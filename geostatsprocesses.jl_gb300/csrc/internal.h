@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace sgs {
@@ -134,6 +135,10 @@ struct SolveArgs {
     const int32_t* list;         // FP64 re-solve: positions to solve (nullptr = all)
     unsigned long long* sum_m;   // accumulates the grid neighbours written to the tables
 };
+
+// Message returned by sgs_last_error(NULL) on this host thread.
+void set_thread_error(const char* msg);
+inline void set_thread_error(const std::string& msg) { set_thread_error(msg.c_str()); }
 
 // ---- launch wrappers (return cudaError_t of the launch) ----
 cudaError_t launch_search(const SearchArgs& a, cudaStream_t s);

@@ -113,6 +113,7 @@ EXPORTS = (
     "sgs_plan_destroy",
     "sgs_last_error",
     "sgs_version",
+    "sgs_schedule_noalloc",
 )
 
 _lib = None
@@ -152,6 +153,8 @@ def _declare(lib):
     lib.sgs_last_error.restype = C.c_char_p
     lib.sgs_version.argtypes = []
     lib.sgs_version.restype = C.c_char_p
+    lib.sgs_schedule_noalloc.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P, P, C.c_int32, ip, P]
+    lib.sgs_schedule_noalloc.restype = C.c_int
     return lib
 
 

@@ -189,6 +189,31 @@ const char* sgs_last_error(const sgs_plan* plan);
 /* Library version string. */
 const char* sgs_version(void);
 
+/* ---- allocation-free schedule ------------------------------------------ */
+#define SGS_NOALLOC_MAX_LEVELS 262144
+
+/* Dependency levels and the level-ordered node list of a neighbour table,
+ * without allocating memory.  No counterpart in the reference: it is the
+ * scheduling step of sgs_plan_prepare, offered on its own for callers that
+ * cannot let a library allocate device memory (an application whose memory
+ * pool already holds the device, or a loop where an allocation's implicit
+ * device synchronization is not acceptable).  All pointers except nlevels
+ * are device pointers owned by the caller: path (N), nbr (N x maxneighbors,
+ * node-major, -1 padded, ids >= N are data), count (N); outputs level (N),
+ * order (N, nodes grouped by level), offsets (nlevels + 1 entries, at most
+ * offsets_capacity), and *nlevels on the host.  stream is a cudaStream_t
+ * (NULL = default stream); the call returns when the results are complete.
+ * Working memory is one file-scope device array per device (about 2 MB)
+ * that stays until the process exits: schedules with more than
+ * SGS_NOALLOC_MAX_LEVELS levels are rejected with SGS_ERR_ARG.  The first
+ * call on a device looks up that array's address; make it before any stream
+ * capture.  Calls on one device share the array: calls that overlap on the
+ * GPU race and must be serialized by the caller.  Errors are reported by
+ * sgs_last_error(NULL). */
+int sgs_schedule_noalloc(const int32_t* path, const int32_t* nbr, const int32_t* count, int64_t nnodes,
+                         int32_t maxneighbors, int32_t* level, int32_t* order, int32_t* offsets,
+                         int32_t offsets_capacity, int32_t* nlevels, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
