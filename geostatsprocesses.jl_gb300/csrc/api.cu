@@ -42,6 +42,8 @@ struct sgs_plan {
     int precision = SGS_PREC_FP32_REFINE;
     int refine_steps = 2;
     int warm_start = 0;
+    int flags = 0;
+    int32_t* d_loff = nullptr;    // device level offsets (nlevels + 1)
     int64_t N = 0, D = 0;
     std::vector<int32_t> h_path;
     std::vector<TmplEntry> h_tmpl;
@@ -272,6 +274,8 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     if (pr->refine_steps < 0 || pr->refine_steps > 4) return set_err(P, SGS_ERR_ARG, "refine_steps must be in 0..4");
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
+    if (pr->flags & ~SGS_FLAG_ONE_LAUNCH_SWEEP) return set_err(P, SGS_ERR_ARG, "unknown flags");
+    P->flags = pr->flags;
 
     // neighbourhood: seqsim.jl:171-177,221-227
     static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -571,10 +575,12 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     P->info.d2h_bytes += sizeof(hs);
     if (hs[3]) return set_err(P, SGS_ERR_TIMEOUT, "dependency-level wait exceeded its bound");
     P->nlevels = hs[2] + 1;
-    int32_t *d_lcount = nullptr, *d_lfill = nullptr, *d_loff = nullptr;
+    int32_t *d_lcount = nullptr, *d_lfill = nullptr;
     if ((rc = dalloc(P, &d_lcount, P->nlevels))) return rc;
     if ((rc = dalloc(P, &d_lfill, P->nlevels))) return rc;
-    if ((rc = dalloc(P, &d_loff, P->nlevels + 1))) return rc;
+    dfree(P, P->d_loff);  // level offsets stay for the one-launch sweep
+    if ((rc = dalloc(P, &P->d_loff, P->nlevels + 1))) return rc;
+    int32_t* d_loff = P->d_loff;
     CK(P, cudaMemsetAsync(d_lcount, 0, P->nlevels * sizeof(int32_t), st));
     CK(P, cudaMemsetAsync(d_lfill, 0, P->nlevels * sizeof(int32_t), st));
     LAUNCH(P, 1, launch_level_order(N, P->d_level, P->nlevels, d_lcount, nullptr, nullptr, nullptr, st));
@@ -636,7 +642,6 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     CK(P, cudaStreamSynchronize(st));
     dfree(P, d_lcount);
     dfree(P, d_lfill);
-    dfree(P, d_loff);
     P->info.ms_search = elapsed(P->ev[0], P->ev[1]);
     P->info.ms_levels = elapsed(P->ev[1], P->ev[2]);
     P->info.ms_solve = elapsed(P->ev[3], P->ev[4]);
@@ -657,6 +662,22 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
 }
 
 static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, void* V, cudaStream_t st) {
+    if (P->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) {
+        // all levels in one cooperative launch (per-level launches if the
+        // device or the launch configuration does not allow it).  Measured on
+        // GB300 its grid barrier costs about a launch gap and its occupancy is
+        // lower, so per-level launches are the default.
+        cudaError_t e;
+        if (P->precision == SGS_PREC_FP64)
+            e = launch_sweep_all_fp64(P->t64, P->k, P->d_loff, P->nlevels, Rp, (const double*)z, seed, (double*)V, st);
+        else
+            e = launch_sweep_all_fp32(P->t32, P->k, P->d_loff, P->nlevels, Rp, (const float*)z, seed, (float*)V, st);
+        if (e == cudaSuccess) {
+            P->info.launches++;
+            return SGS_OK;
+        }
+        cudaGetLastError();
+    }
     for (int l = 0; l < P->nlevels; ++l) {
         const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
         cudaError_t e;

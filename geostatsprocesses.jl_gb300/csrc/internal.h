@@ -152,6 +152,11 @@ cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, in
                               const float* z, uint64_t seed, float* V, cudaStream_t s);
 cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
                               const double* z, uint64_t seed, double* V, cudaStream_t s);
+// all levels in one cooperative launch (loff: device level offsets, nlevels + 1)
+cudaError_t launch_sweep_all_fp32(const SweepTables<float>& t, int k, const int32_t* loff, int nlevels, int Rp,
+                                  const float* z, uint64_t seed, float* V, cudaStream_t s);
+cudaError_t launch_sweep_all_fp64(const SweepTables<double>& t, int k, const int32_t* loff, int nlevels, int Rp,
+                                  const double* z, uint64_t seed, double* V, cudaStream_t s);
 // host z (R x N, realization-major double) on device -> node-major [N][Rp] of T
 cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s);
 cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, double* z, cudaStream_t s);

@@ -329,7 +329,8 @@ struct Smem32 {
     static constexpr size_t V = (size_t)CB * sizeof(float);
     static constexpr size_t COL = 2 * (size_t)CB * sizeof(float);
     static constexpr size_t INFO = (size_t)NMAX * sizeof(NbInfo);
-    static constexpr size_t bytes = K + C + W + V + COL + INFO;
+    static constexpr size_t LIN = (size_t)NMAX * sizeof(int);
+    static constexpr size_t bytes = K + C + W + V + COL + INFO + LIN;
     static_assert(K % 16 == 0 && bytes % 16 == 0, "16-byte aligned per-warp layout");
 };
 
@@ -368,9 +369,14 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
     float* vec = reinterpret_cast<float*>(base + S::K + S::C + S::W);
     float* colb = reinterpret_cast<float*>(base + S::K + S::C + S::W + S::V);
     NbInfo* info = reinterpret_cast<NbInfo*>(base + S::K + S::C + S::W + S::V + S::COL);
+    int* lin = reinterpret_cast<int*>(base + S::K + S::C + S::W + S::V + S::COL + S::INFO);
     const GridDev& G = a.grid;
     const int k = a.k;
     const DF sd_sill = df_sqrt(df_from_double(a.vario.sill));
+    const float2* lut2 = a.lut.c2;
+    const int lw0 = a.lut.w[0], lw1 = a.lut.w[1];
+    const int lcentre = a.lut.e[0] + lw0 * (a.lut.e[1] + lw1 * a.lut.e[2]);
+    const int ltotal = lw0 * lw1 * a.lut.w[2];
     const int64_t nwarps = (int64_t)gridDim.x * SOLVE32_WARPS;
     const int i0 = lane, i1 = lane + 32;
 
@@ -396,18 +402,45 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                     in.did = id - (int)G.N;
                 }
                 info[q] = in;
+                // linear lag-table offset of the cell relative to the query: the
+                // table index of a grid pair (q, r) is centre + lin[r] - lin[q]
+                lin[q] = in.did < 0 ? (in.c0 - self.c0) + lw0 * ((in.c1 - self.c1) + lw1 * (in.c2 - self.c2)) : 0;
             }
             __syncwarp();
-            for (int q = lane; q < n; q += 32) c[q] = kcov2n(a, info[q], self);
-            for (int r = 0; r < n; ++r) {
-                const NbInfo ir = info[r];
-                if (ir.did >= 0) continue;
-                for (int q = lane; q <= r; q += 32) {
-                    const NbInfo iq = info[q];
-                    if (iq.did < 0) {
-                        const DF v = kcov2n(a, iq, ir);
-                        K[r * LDK + q] = v;
-                        K[q * LDK + r] = v;
+            if (lut2) {
+                // every neighbour is a template offset, so every pairwise lag is
+                // inside the table; the clamp only keeps reads in bounds
+                for (int q = lane; q < n; q += 32) {
+                    if (info[q].did < 0) {
+                        const float2 v = lut2[min(max(lcentre - lin[q], 0), ltotal - 1)];
+                        c[q] = {v.x, v.y};
+                    } else {
+                        c[q] = kcov2n(a, info[q], self);
+                    }
+                }
+                for (int r = 0; r < n; ++r) {
+                    if (info[r].did >= 0) continue;
+                    const int base = lcentre + lin[r];
+                    for (int q = lane; q <= r; q += 32) {
+                        if (info[q].did < 0) {
+                            const float2 v = lut2[min(max(base - lin[q], 0), ltotal - 1)];
+                            K[r * LDK + q] = {v.x, v.y};
+                            K[q * LDK + r] = {v.x, v.y};
+                        }
+                    }
+                }
+            } else {
+                for (int q = lane; q < n; q += 32) c[q] = kcov2n(a, info[q], self);
+                for (int r = 0; r < n; ++r) {
+                    const NbInfo ir = info[r];
+                    if (ir.did >= 0) continue;
+                    for (int q = lane; q <= r; q += 32) {
+                        const NbInfo iq = info[q];
+                        if (iq.did < 0) {
+                            const DF v = kcov2n(a, iq, ir);
+                            K[r * LDK + q] = v;
+                            K[q * LDK + r] = v;
+                        }
                     }
                 }
             }

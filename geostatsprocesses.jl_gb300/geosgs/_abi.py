@@ -30,6 +30,8 @@ SGS_SEARCH_NEAREST = 2
 SGS_PREC_FP64 = 0
 SGS_PREC_FP32_REFINE = 1
 
+SGS_FLAG_ONE_LAUNCH_SWEEP = 1
+
 SGS_NODE_KRIGED = 0
 SGS_NODE_PRIOR_NMIN = 1
 SGS_NODE_PRIOR_SINGULAR = 2

@@ -43,6 +43,7 @@ class GPUSEQSIM(FieldSimulationMethod):
     refine_steps: int = 2
     warm_start: bool = False
     device: int = 0
+    one_launch_sweep: bool = False  # all dependency levels in one cooperative launch
 
 
 class Ensemble:

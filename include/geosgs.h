@@ -61,6 +61,11 @@ extern "C" {
 #define SGS_PREC_FP32_REFINE 1  /* FP32 LHS + Cholesky, FP64 refinement residual and
                                    variance, FP32 weights and sweep                 */
 
+/* ---- sgs_problem.flags --------------------------------------------------- */
+#define SGS_FLAG_ONE_LAUNCH_SWEEP 1  /* sweep all dependency levels in one cooperative
+                                        launch with a grid barrier between levels,
+                                        instead of one launch per level */
+
 /* ---- per-node solve status (sgs_plan_weights) --------------------------- */
 #define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */
 #define SGS_NODE_PRIOR_NMIN   1  /* fewer than minneighbors neighbours: prior     */
@@ -107,7 +112,7 @@ typedef struct sgs_problem {
     int32_t refine_steps;     /* refinement steps for SGS_PREC_FP32_REFINE (0..4, default 2) */
     int32_t warm_start;       /* 1 = learned warm start of the kriging weights */
     int32_t device;           /* CUDA device ordinal */
-    int32_t flags;            /* reserved, 0 */
+    int32_t flags;            /* 0 or SGS_FLAG_* */
 } sgs_problem;
 
 typedef struct sgs_plan sgs_plan;

@@ -198,3 +198,22 @@ def test_error_codes(geosgs_lib):
     with pytest.raises(geosgs.GeoSGSError) as e:
         geosgs.Plan(p, (keep, bad))
     assert e.value.code == _abi.SGS_ERR_ARG
+
+
+@pytest.mark.parametrize("nreals", [4, 8, 12, 64, 256])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sweep_variants_agree_with_oracle(precision, nreals, oracle_mod, geosgs_lib):
+    """The sweep's launch forms (one cooperative launch over all levels; one
+    launch per level with a thread per chunk of 4 realizations, or with a
+    warp per node splitting the neighbour list for R <= 64) all match the
+    oracle."""
+    wl = workloads.small(n=48, k=16, ndata=25, vario="gau", nugget=0.02, precision=precision, nreals=nreals)
+    z = np.random.default_rng(nreals).standard_normal((nreals, 48 * 48))
+    ref = None
+    for one_launch in (False, True):
+        wl.method.one_launch_sweep = one_launch
+        G, O = both(wl, oracle_mod, precision)
+        if ref is None:
+            ref = O.simulate(nreals, z)
+        assert rel_err(G.simulate(nreals, z), ref) <= VALUE_TOL
+        G.close()
