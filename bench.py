@@ -332,7 +332,10 @@ def main():
     inf = fast["info"]
     sum_m = int(inf.sum_grid_neighbors)
     sv = 4
-    alg_bytes = (sum_m + N) * R * sv + sum_m * 8 + N * 16
+    # neighbour row reads + value writes, plus the sweep tables: per grid
+    # neighbour an int32 index and a (hi, lo) float2 weight, per node its id,
+    # neighbour count, (hi, lo) b0 and (hi, lo) sigma
+    alg_bytes = (sum_m + N) * R * sv + sum_m * 12 + N * 24
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -340,11 +343,13 @@ def main():
     except Exception:
         peak, peak_src = 6800.0, "fallback"
     achieved = alg_bytes / (fast["ms_sweep"] * 1e-3) / 1e9
+    # DRAM traffic of one sweep from the committed ncu capture (measured on a
+    # smaller grid of the same workload, scaled by the node-realizations)
     traffic = None
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
-        if tr.get("workload") == wl.name and tr.get("nreals") == R:
-            traffic = tr["dram_bytes_per_sweep"]
+        if args.workload == "c3" and R == 256:
+            traffic = tr["dram_bytes_per_node_real"] * N * R
     except Exception:
         pass
     roofline = {"kernel": "sweep_fp32_kernel (all level launches of one sweep)", "bound": "hbm",

@@ -74,6 +74,8 @@ struct sgs_plan {
     bool prepared = false;
     bool sweep_timed = false;     // ev[5]/ev[6] bracket the last sweep
     unsigned long long* d_sum_m = nullptr;
+    float* d_nn = nullptr;        // warm-start network parameters
+    float* d_winit = nullptr;     // warm-start predictions [N][k]
     sgs_info info{};
 };
 
@@ -495,15 +497,31 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     CK(P, cudaMemsetAsync(nfb, 0, sizeof(int32_t), P->stream));
     s.fallback = P->d_fallback;
     s.nfallback = nfb;
+    unsigned long long* nwarm = reinterpret_cast<unsigned long long*>(P->d_scratch + 8);  // scratch[8..9]
+    if (P->warm_start && P->d_nn) {
+        // learned warm start: predictions for every node, then the solve
+        // refines from them
+        int rc;
+        if (!P->d_winit && (rc = dalloc(P, &P->d_winit, (size_t)P->N * P->k))) return rc;
+        LAUNCH(P, 1, launch_nn_predict_plan(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn,
+                                            P->d_winit, P->stream));
+        CK(P, cudaMemsetAsync(nwarm, 0, sizeof(unsigned long long), P->stream));
+        s.w_init = P->d_winit;
+        s.n_warm = nwarm;
+    }
     LAUNCH(P, 1, launch_solve_fp32(s, P->t32, P->stream));
     // queued systems: re-solve in FP64 (the canonical decision and accuracy)
     s.list = P->d_fallback;
+    s.w_init = nullptr;
     LAUNCH(P, 1, launch_solve_fp64_into_fp32(s, P->t32, P->stream));
     int32_t h = 0;
+    unsigned long long hw = 0;
     CK(P, cudaMemcpyAsync(&h, nfb, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
+    if (s.n_warm) CK(P, cudaMemcpyAsync(&hw, nwarm, sizeof(hw), cudaMemcpyDeviceToHost, P->stream));
     CK(P, cudaStreamSynchronize(P->stream));
-    P->info.d2h_bytes += sizeof(int32_t);
+    P->info.d2h_bytes += sizeof(int32_t) + (s.n_warm ? sizeof(hw) : 0);
     P->info.n_fp64_fallback = h;
+    P->info.n_warm_accepted = (int64_t)hw;
     return SGS_OK;
 }
 
@@ -811,4 +829,56 @@ extern "C" int sgs_plan_info(const sgs_plan* P, sgs_info* info) {
         if (cudaEventSynchronize(P->ev[6]) == cudaSuccess) info->ms_sweep = elapsed(P->ev[5], P->ev[6]);
     }
     return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// learned warm start
+extern "C" int sgs_plan_features_device(sgs_plan* P, float* feat_dev, void* stream) {
+    if (!P || !feat_dev) return set_err(P, SGS_ERR_ARG, "null argument");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "features before prepare");
+    CK(P, cudaSetDevice(P->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->stream;
+    LAUNCH(P, 1, launch_nn_features(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, feat_dev, st));
+    CK(P, cudaStreamSynchronize(st));
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_set_network(sgs_plan* P, const float* params) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    CK(P, cudaSetDevice(P->device));
+    if (!params) {
+        dfree(P, P->d_nn);
+        P->d_nn = nullptr;
+        return SGS_OK;
+    }
+    int rc;
+    if (!P->d_nn && (rc = dalloc(P, &P->d_nn, SGS_NN_PARAMS))) return rc;
+    CK(P, cudaMemcpy(P->d_nn, params, SGS_NN_PARAMS * sizeof(float), cudaMemcpyHostToDevice));
+    P->info.h2d_bytes += SGS_NN_PARAMS * sizeof(float);
+    return SGS_OK;
+}
+
+extern "C" int sgs_nn_forward(const float* params, const float* feat, const int32_t* count, int64_t nsys, int32_t k,
+                              float* pred, void* stream) {
+    if (!params || !feat || !count || !pred || nsys < 0 || k < 1 || k > KMAX)
+        return set_err(nullptr, SGS_ERR_ARG, "invalid argument");
+    if (nsys == 0) return SGS_OK;
+    cudaError_t e = launch_nn_forward(params, feat, count, nsys, k, pred, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGS_OK : cuda_err(nullptr, e, "sgs_nn_forward");
+}
+
+extern "C" int sgs_nn_backward(const float* params, const float* feat, const int32_t* count, const float* target,
+                               int64_t nsys, int32_t k, float* grad, float* loss, void* stream) {
+    if (!params || !feat || !count || !target || !grad || !loss || nsys < 0 || k < 1 || k > KMAX)
+        return set_err(nullptr, SGS_ERR_ARG, "invalid argument");
+    if (nsys == 0) return SGS_OK;
+    cudaError_t e = launch_nn_backward(params, feat, count, target, nsys, k, grad, loss, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGS_OK : cuda_err(nullptr, e, "sgs_nn_backward");
+}
+
+extern "C" int sgs_nn_adam(float* params, const float* grad, float* m, float* v, int32_t step, float lr, float scale,
+                           void* stream) {
+    if (!params || !grad || !m || !v || step < 1) return set_err(nullptr, SGS_ERR_ARG, "invalid argument");
+    cudaError_t e = launch_nn_adam(params, grad, m, v, step, lr, scale, (cudaStream_t)stream);
+    return e == cudaSuccess ? SGS_OK : cuda_err(nullptr, e, "sgs_nn_adam");
 }

@@ -134,6 +134,8 @@ struct SolveArgs {
     int32_t* nfallback;
     const int32_t* list;         // FP64 re-solve: positions to solve (nullptr = all)
     unsigned long long* sum_m;   // accumulates the grid neighbours written to the tables
+    const float* w_init;         // optional node-indexed [N][k] warm-start weights (FP32 path)
+    unsigned long long* n_warm;  // counts systems accepted from the warm start
 };
 
 // Message returned by sgs_last_error(NULL) on this host thread.
@@ -164,5 +166,16 @@ cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, d
 cudaError_t launch_rows_to_out_fp32(const float* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
 cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
 cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2, cudaStream_t s);
+// learned warm start (learned.cu)
+cudaError_t launch_nn_features(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,
+                               const double* data_xyz, float* feat, cudaStream_t s);
+cudaError_t launch_nn_predict_plan(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,
+                                   const double* data_xyz, const float* params, float* out, cudaStream_t s);
+cudaError_t launch_nn_forward(const float* params, const float* feat, const int32_t* count, int64_t nsys, int k,
+                              float* pred, cudaStream_t s);
+cudaError_t launch_nn_backward(const float* params, const float* feat, const int32_t* count, const float* target,
+                               int64_t nsys, int k, float* grad, float* loss, cudaStream_t s);
+cudaError_t launch_nn_adam(float* p, const float* g, float* m, float* v, int step, float lr, float scale,
+                           cudaStream_t s);
 
 }  // namespace sgs

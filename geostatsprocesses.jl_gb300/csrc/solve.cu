@@ -514,15 +514,22 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
             }
             bool accept = ok;
             if (accept) {
-                // w = K^-1 c = -R c
-                for (int q = lane; q < S::CB; q += 32) vec[q] = q < n ? c[q].hi : 0.0f;
-                __syncwarp();
                 float s0 = 0.0f, s1 = 0.0f;
+                if (a.w_init) {
+                    // learned warm start: the refinement below starts from the
+                    // network's prediction and must meet the same tolerance
+                    if (i0 < n) s0 = a.w_init[(int64_t)g * k + i0];
+                    if (TWO && i1 < n) s1 = a.w_init[(int64_t)g * k + i1];
+                } else {
+                    // w = K^-1 c = -R c
+                    for (int q = lane; q < S::CB; q += 32) vec[q] = q < n ? c[q].hi : 0.0f;
+                    __syncwarp();
 #pragma unroll
-                for (int j = 0; j < NMAX; ++j) {
-                    const float v = vec[j];
-                    s0 = __fmaf_rn(-R0[j], v, s0);
-                    if (TWO) s1 = __fmaf_rn(-R1[j], v, s1);
+                    for (int j = 0; j < NMAX; ++j) {
+                        const float v = vec[j];
+                        s0 = __fmaf_rn(-R0[j], v, s0);
+                        if (TWO) s1 = __fmaf_rn(-R1[j], v, s1);
+                    }
                 }
                 DF w0 = {s0, 0.0f}, w1 = {s1, 0.0f};
                 if (i0 < n) w[i0] = w0;
@@ -614,6 +621,7 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                 __syncwarp();
                 continue;
             }
+            if (a.w_init && a.n_warm && lane == 0) atomicAdd(a.n_warm, 1ull);
         }
         // ---- table row: grid neighbours with (hi, lo) weights, data folded into b0
         int m = 0;

@@ -32,6 +32,9 @@ SGS_PREC_FP32_REFINE = 1
 
 SGS_FLAG_ONE_LAUNCH_SWEEP = 1
 
+SGS_NN_FEATURES = 8
+SGS_NN_PARAMS = 2401
+
 SGS_NODE_KRIGED = 0
 SGS_NODE_PRIOR_NMIN = 1
 SGS_NODE_PRIOR_SINGULAR = 2
@@ -115,6 +118,11 @@ EXPORTS = (
     "sgs_plan_destroy",
     "sgs_last_error",
     "sgs_version",
+    "sgs_plan_features_device",
+    "sgs_plan_set_network",
+    "sgs_nn_forward",
+    "sgs_nn_backward",
+    "sgs_nn_adam",
     "sgs_schedule_noalloc",
 )
 
@@ -155,6 +163,16 @@ def _declare(lib):
     lib.sgs_last_error.restype = C.c_char_p
     lib.sgs_version.argtypes = []
     lib.sgs_version.restype = C.c_char_p
+    lib.sgs_plan_features_device.argtypes = [P, P, P]
+    lib.sgs_plan_features_device.restype = C.c_int
+    lib.sgs_plan_set_network.argtypes = [P, C.POINTER(C.c_float)]
+    lib.sgs_plan_set_network.restype = C.c_int
+    lib.sgs_nn_forward.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P]
+    lib.sgs_nn_forward.restype = C.c_int
+    lib.sgs_nn_backward.argtypes = [P, P, P, P, C.c_int64, C.c_int32, P, P, P]
+    lib.sgs_nn_backward.restype = C.c_int
+    lib.sgs_nn_adam.argtypes = [P, P, P, P, C.c_int32, C.c_float, C.c_float, P]
+    lib.sgs_nn_adam.restype = C.c_int
     lib.sgs_schedule_noalloc.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P, P, C.c_int32, ip, P]
     lib.sgs_schedule_noalloc.restype = C.c_int
     return lib

@@ -86,6 +86,17 @@ class Plan:
         self._check(self.lib.sgs_plan_levels(self.h, _ip(lv), C.byref(n)))
         return lv, int(n.value)
 
+    def set_network(self, params):
+        """Warm-start network parameters (SGS_NN_PARAMS floats) or None."""
+        if params is None:
+            self._check(self.lib.sgs_plan_set_network(self.h, None))
+            return self
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32))
+        if p.shape != (_abi.SGS_NN_PARAMS,):
+            raise ValueError(f"expected {_abi.SGS_NN_PARAMS} parameters")
+        self._check(self.lib.sgs_plan_set_network(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return self
+
     def info(self) -> _abi.SgsInfo:
         inf = _abi.SgsInfo()
         self._check(self.lib.sgs_plan_info(self.h, C.byref(inf)))

@@ -194,6 +194,37 @@ const char* sgs_last_error(const sgs_plan* plan);
 /* Library version string. */
 const char* sgs_version(void);
 
+/* ---- learned warm start -------------------------------------------------
+ * A small permutation-invariant network predicts each system's kriging
+ * weights from per-neighbour features (normalized anisotropic lag to the
+ * node, its norm, covariance / sill, nugget / sill, variogram family).  With
+ * problem.warm_start = 1 and a network set on the plan, the FP32 solve starts
+ * its refinement from the prediction instead of the FP32 solution and
+ * accepts it only when the refined residual meets the usual tolerance; other
+ * systems take the FP64 path.  No counterpart in the reference (it is part
+ * of this method's GPU design); the training kernels run on device buffers
+ * owned by the caller. */
+#define SGS_NN_FEATURES 8
+#define SGS_NN_PARAMS   2401
+
+/* Features of every system (device out: N x maxneighbors x SGS_NN_FEATURES
+ * floats, node-indexed, zero for missing neighbours). */
+int sgs_plan_features_device(sgs_plan* plan, float* feat_dev, void* stream);
+/* Set (or clear with NULL) the network used by the warm start: host array of
+ * SGS_NN_PARAMS floats.  Takes effect at the next sgs_plan_prepare. */
+int sgs_plan_set_network(sgs_plan* plan, const float* params);
+/* Network forward pass: feat (nsys x k x F), count (nsys) -> pred (nsys x k). */
+int sgs_nn_forward(const float* params, const float* feat, const int32_t* count, int64_t nsys, int32_t k,
+                   float* pred, void* stream);
+/* Adds the batch's mean-squared-error loss to *loss and its gradient to grad
+ * (SGS_NN_PARAMS floats, zeroed by the caller), all device pointers. */
+int sgs_nn_backward(const float* params, const float* feat, const int32_t* count, const float* target,
+                    int64_t nsys, int32_t k, float* grad, float* loss, void* stream);
+/* One Adam step (beta 0.9 / 0.999) on device arrays of SGS_NN_PARAMS floats,
+ * with gradient scale `scale` (e.g. 1 / batch systems); step counts from 1. */
+int sgs_nn_adam(float* params, const float* grad, float* m, float* v, int32_t step, float lr, float scale,
+                void* stream);
+
 /* ---- allocation-free schedule ------------------------------------------ */
 #define SGS_NOALLOC_MAX_LEVELS 262144
 
