@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-nodes", type=int, default=60000, help="oracle sample size (nodes)")
+    ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned warm start")
+    ap.add_argument("--learned-systems", type=int, default=600000, help="training systems for the warm start")
+    ap.add_argument("--learned-epochs", type=int, default=8)
     ap.add_argument("--grid", default=None, help="override the 3D grid, e.g. 200,200,50 (profiling a smaller case)")
     ap.add_argument("--ndata", type=int, default=None, help="override the number of data (with --grid)")
     return ap.parse_args()
@@ -208,12 +211,14 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------- GPU legs
-def time_device(wl, args, torch, ws):
+def time_device(wl, args, torch, ws, network=None):
     """Device-resident steps: prepare (search, levels, solve) + sweep."""
     import geosgs
 
     p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
     plan = geosgs.Plan(p, keep)
+    if network is not None:
+        plan.set_network(network)
     R = wl.nreals
     Rp = (R + 3) // 4 * 4
     dt = torch.float64 if wl.method.precision == "fp64" else torch.float32
@@ -317,6 +322,32 @@ def main():
         a64.warmup = max(1, min(args.warmup, 2))
         fp64 = time_device(wl64, a64, torch, ws)
 
+    learned_res = None
+    if not args.no_learned:
+        # learned warm start: train on systems the method generates (random
+        # 3D variograms, same maxneighbors), then time the same steps with the
+        # network warm-starting every FP32 solve
+        from geosgs import learned
+
+        t0 = time.perf_counter()
+        feat, count, target = learned.generate(args.learned_systems, seed=11, torch=torch, dims=(48, 48, 32),
+                                               k=wl.method.maxneighbors)
+        t_gen = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        params, hist = learned.train(feat, count, target, torch, epochs=args.learned_epochs, batch=16384, lr=3e-3)
+        t_train = time.perf_counter() - t0
+        mean_sq = float((target ** 2).mean())
+        del feat, count, target
+        torch.cuda.empty_cache()
+        wll = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
+        wll.method.warm_start = True
+        al = argparse.Namespace(**vars(args))
+        al.steps = max(2, args.steps // 2)
+        al.warmup = max(1, min(args.warmup, 2))
+        learned_res = time_device(wll, al, torch, ws, network=params)
+        learned_res.update(dict(train_systems=args.learned_systems, epochs=args.learned_epochs,
+                                final_loss=hist[-1], mean_sq_weight=mean_sq, s_generate=t_gen, s_train=t_train))
+
     e2e = None
     if not args.no_e2e:
         e2e_s, e2e_inf, _ = time_e2e(wl, args, torch, ws, max(1, min(3, args.steps)))
@@ -388,6 +419,20 @@ def main():
                             "phases_ms": {"search": fp64["ms_search"], "levels": fp64["ms_levels"],
                                           "solve": fp64["ms_solve"], "sweep": fp64["ms_sweep"]}}
         out["speedup_vs_fp64_path"] = value / v64
+    if learned_res:
+        li = learned_res["info"]
+        vl = ws * N * R / (learned_res["ms"] * 1e-3)
+        out["learned_fp32_path"] = {
+            "value": vl, "ms_per_step": learned_res["ms"],
+            "phases_ms": {"search": learned_res["ms_search"], "levels": learned_res["ms_levels"],
+                          "solve_incl_prediction": learned_res["ms_solve"], "sweep": learned_res["ms_sweep"]},
+            "warm_start_accepted": int(li.n_warm_accepted), "fp64_fallback": int(li.n_fp64_fallback),
+            "kriged_systems": int(N - li.n_prior),
+            "training": {"systems": learned_res["train_systems"], "epochs": learned_res["epochs"],
+                         "final_mse": learned_res["final_loss"], "mean_sq_target": learned_res["mean_sq_weight"],
+                         "s_generate": round(learned_res["s_generate"], 2), "s_train": round(learned_res["s_train"], 2)},
+            "speedup_vs_fp64_path": (vl / (N * R / (fp64["ms"] * 1e-3) * ws)) if fp64 else None,
+        }
     print(json.dumps(out))
 
 

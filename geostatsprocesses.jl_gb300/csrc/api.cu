@@ -508,6 +508,9 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
         CK(P, cudaMemsetAsync(nwarm, 0, sizeof(unsigned long long), P->stream));
         s.w_init = P->d_winit;
         s.n_warm = nwarm;
+        // a prediction is far less accurate than the FP32 inverse's own
+        // solution, so warm-started systems take one more refinement step
+        s.refine_steps = std::min(P->refine_steps + 1, 4);
     }
     LAUNCH(P, 1, launch_solve_fp32(s, P->t32, P->stream));
     // queued systems: re-solve in FP64 (the canonical decision and accuracy)
