@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned warm start")
     ap.add_argument("--learned-systems", type=int, default=600000, help="training systems for the warm start")
     ap.add_argument("--learned-epochs", type=int, default=8)
+    ap.add_argument("--sweep-config", default=None,
+                    help='JSON sweep configuration (sgs_sweep_config fields) instead of the autotuner, e.g. '
+                         '\'{"mode": 0, "lanes_w": 32, "tight": 1}\' (profiling one form)')
     ap.add_argument("--grid", default=None, help="override the 3D grid, e.g. 200,200,50 (profiling a smaller case)")
     ap.add_argument("--ndata", type=int, default=None, help="override the number of data (with --grid)")
     return ap.parse_args()
@@ -229,6 +232,13 @@ def time_device(wl, args, torch, ws, network=None):
         plan.prepare()
         plan.simulate_device(R, None, 1000 + i, V.data_ptr(), stream)
 
+    # sweep autotuner: once per plan, outside the timed region
+    plan.prepare()
+    if args.sweep_config:
+        plan.set_sweep(**json.loads(args.sweep_config))
+        sweep_cfg, sweep_tried = dict(plan.sweep_config()), []
+    else:
+        sweep_cfg, sweep_tried = plan.tune_sweep(R)
     for i in range(args.warmup):
         step(i)
     torch.cuda.synchronize()
@@ -252,6 +262,7 @@ def time_device(wl, args, torch, ws, network=None):
     ms = e0.elapsed_time(e1) / args.steps
     inf = plan.info()
     res = dict(ms=max_over_ranks(ws, ms), launches=(inf.launches - launches0), info=inf,
+               sweep_config=sweep_cfg, sweep_tried=sweep_tried,
                ms_sweep=statistics.mean(sweeps), ms_solve=statistics.mean(solves),
                ms_search=statistics.mean(searches), ms_levels=statistics.mean(levels))
     plan.close()
@@ -259,7 +270,7 @@ def time_device(wl, args, torch, ws, network=None):
     return res
 
 
-def time_e2e(wl, args, torch, ws, steps):
+def time_e2e(wl, args, torch, ws, steps, sweep=None):
     """Through the public C ABI with host buffers: create (host -> device
     copies of the problem), prepare, simulate with the FP64 result copied to
     pinned host memory, destroy."""
@@ -271,6 +282,8 @@ def time_e2e(wl, args, torch, ws, steps):
 
     def step(i):
         plan = geosgs.Plan(p, keep)
+        if sweep:
+            plan.set_sweep(**sweep)
         plan.prepare()
         plan._check(plan.lib.sgs_plan_simulate(plan.h, R, None, 77 + i,
                                                out.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))))
@@ -350,7 +363,7 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        e2e_s, e2e_inf, _ = time_e2e(wl, args, torch, ws, max(1, min(3, args.steps)))
+        e2e_s, e2e_inf, _ = time_e2e(wl, args, torch, ws, max(1, min(3, args.steps)), sweep=fast["sweep_config"])
         e2e = {"value": ws * N * R / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(e2e_inf.h2d_bytes), "d2h_bytes_per_step": int(e2e_inf.d2h_bytes),
                "ms_per_step": 1e3 * e2e_s,
@@ -376,16 +389,24 @@ def main():
     achieved = alg_bytes / (fast["ms_sweep"] * 1e-3) / 1e9
     # DRAM traffic of one sweep from the committed ncu capture (measured on a
     # smaller grid of the same workload, scaled by the node-realizations)
-    traffic = None
+    traffic, tr = None, {}
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
         if args.workload == "c3" and R == 256:
             traffic = tr["dram_bytes_per_node_real"] * N * R
     except Exception:
         pass
-    roofline = {"kernel": "sweep_fp32_kernel (all level launches of one sweep)", "bound": "hbm",
+    sc = fast["sweep_config"]
+    form = {0: "sweep_flow_kernel (dataflow launches%s)" % (
+                ", levels %d-%d by per-level launches" % (sc["level_lo"], sc["level_hi"] - 1)
+                if sc["level_hi"] > sc["level_lo"] else ""),
+            1: "sweep_all_kernel (one cooperative launch)",
+            2: "sweep_level_kernel (one launch per level)"}[sc["mode"]]
+    roofline = {"kernel": form + ": all launches of one sweep", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_src, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                "peak_source": peak_src, "traffic": traffic,
+                "traffic_measured_on": (tr.get("kernel") if traffic is not None else None),
+                "algorithmic_bytes": alg_bytes,
                 "ms": fast["ms_sweep"]}
 
     cpu = None
@@ -412,6 +433,8 @@ def main():
         "e2e": e2e,
         "gpu_launches": int(fast["launches"]),
         "clocks": clk,
+        "sweep_config": {k: v for k, v in sc.items()},
+        "sweep_candidates_ms": [round(t["ms"], 3) for t in fast["sweep_tried"]],
     }
     if fp64:
         v64 = ws * N * R / (fp64["ms"] * 1e-3)

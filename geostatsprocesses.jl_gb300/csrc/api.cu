@@ -76,6 +76,12 @@ struct sgs_plan {
     unsigned long long* d_sum_m = nullptr;
     float* d_nn = nullptr;        // warm-start network parameters
     float* d_winit = nullptr;     // warm-start predictions [N][k]
+    int32_t* d_done = nullptr;    // dataflow sweep: per-node epoch flags
+    unsigned long long* d_flow = nullptr;  // dataflow sweep: ticket, error flag
+    int32_t flow_epoch = 0;
+    sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0.f};
+    int64_t done_cap = 0;         // flags allocated in d_done (pieces x N)
+    int last_sweep_mode = SGS_SWEEP_FLOW;  // mode of the last sweep launched
     sgs_info info{};
 };
 
@@ -276,8 +282,14 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     if (pr->refine_steps < 0 || pr->refine_steps > 4) return set_err(P, SGS_ERR_ARG, "refine_steps must be in 0..4");
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
-    if (pr->flags & ~SGS_FLAG_ONE_LAUNCH_SWEEP) return set_err(P, SGS_ERR_ARG, "unknown flags");
+    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP))
+        return set_err(P, SGS_ERR_ARG, "unknown flags");
+    if ((pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) && (pr->flags & SGS_FLAG_LEVEL_SWEEP))
+        return set_err(P, SGS_ERR_ARG, "SGS_FLAG_ONE_LAUNCH_SWEEP and SGS_FLAG_LEVEL_SWEEP exclude each other");
     P->flags = pr->flags;
+    P->sweep.mode = (pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) ? SGS_SWEEP_COOPERATIVE
+                    : (pr->flags & SGS_FLAG_LEVEL_SWEEP)   ? SGS_SWEEP_LEVELS
+                                                           : SGS_SWEEP_FLOW;
 
     // neighbourhood: seqsim.jl:171-177,221-227
     static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -657,6 +669,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
             if ((rc = dalloc(P, &P->d_fallback, N))) return rc;
         }
     }
+    if (!P->d_flow && (rc = dalloc(P, &P->d_flow, 2))) return rc;
     CK(P, cudaEventRecord(P->ev[3], st));
     if ((rc = run_solve(P, nullptr, nullptr))) return rc;
     CK(P, cudaEventRecord(P->ev[4], st));
@@ -682,12 +695,22 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     return SGS_OK;
 }
 
+// error flag of the last dataflow sweep (the caller has synchronized)
+static int check_flow_error(sgs_plan* P) {
+    if (!P->d_flow || P->last_sweep_mode != SGS_SWEEP_FLOW) return SGS_OK;
+    int32_t err = 0;
+    CK(P, cudaMemcpy(&err, P->d_flow + 1, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) return set_err(P, SGS_ERR_TIMEOUT, "dataflow sweep: a dependency wait exceeded its bound");
+    return SGS_OK;
+}
+
 static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, void* V, cudaStream_t st) {
-    if (P->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) {
+    (void)R;
+    const sgs_sweep_config& c = P->sweep;
+    P->last_sweep_mode = c.mode;
+    if (c.mode == SGS_SWEEP_COOPERATIVE) {
         // all levels in one cooperative launch (per-level launches if the
-        // device or the launch configuration does not allow it).  Measured on
-        // GB300 its grid barrier costs about a launch gap and its occupancy is
-        // lower, so per-level launches are the default.
+        // device or the launch configuration does not allow it)
         cudaError_t e;
         if (P->precision == SGS_PREC_FP64)
             e = launch_sweep_all_fp64(P->t64, P->k, P->d_loff, P->nlevels, Rp, (const double*)z, seed, (double*)V, st);
@@ -698,6 +721,75 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
             return SGS_OK;
         }
         cudaGetLastError();
+        P->last_sweep_mode = SGS_SWEEP_LEVELS;
+    } else if (c.mode == SGS_SWEEP_FLOW) {
+        // leading levels by per-level launches, the rest in one dataflow launch
+        int W = c.lanes_w, G = c.lanes_g;
+        const int H = flow_layout(Rp, W, G);
+        const int64_t nflags = P->N * H;
+        if (nflags > P->done_cap) {
+            CK(P, cudaStreamSynchronize(st));
+            dfree(P, P->d_done);
+            P->d_done = nullptr;
+            P->done_cap = 0;
+            int rc;
+            if ((rc = dalloc(P, &P->d_done, nflags))) return rc;
+            P->done_cap = nflags;
+            CK(P, cudaMemsetAsync(P->d_done, 0, nflags * sizeof(int32_t), st));
+            P->flow_epoch = 0;
+        }
+        if (P->flow_epoch >= 0x7ffffff0) {
+            CK(P, cudaMemsetAsync(P->d_done, 0, P->done_cap * sizeof(int32_t), st));
+            P->flow_epoch = 0;
+        }
+        // levels [lo, hi) by per-level launches, the rest by dataflow launches
+        const int lo = std::max(0, std::min(c.level_lo, P->nlevels));
+        const int hi = std::max(lo, std::min(c.level_hi, P->nlevels));
+        const int64_t plo = P->h_loff[lo], phi = P->h_loff[hi];
+        const int32_t epoch = ++P->flow_epoch;
+        CK(P, cudaMemsetAsync(P->d_flow, 0, 2 * sizeof(unsigned long long), st));
+        auto flow = [&](int64_t p0, int64_t p1) -> int {
+            FlowArgs f{};
+            f.item0 = p0 * H;
+            f.item1 = p1 * H;
+            f.N = P->N;
+            f.H = H;
+            f.done = P->d_done;
+            f.epoch = epoch;
+            f.ticket = P->d_flow;
+            f.err = reinterpret_cast<int32_t*>(P->d_flow + 1);
+            f.chunk = std::max(1, c.chunk);
+            f.blocks_per_sm = c.blocks_per_sm;
+            f.tight = c.tight;
+            f.wait_ns = 10000000000ull;  // 10 s: far beyond any dependency chain
+            cudaError_t e;
+            if (P->precision == SGS_PREC_FP64)
+                e = launch_sweep_flow_fp64(P->t64, P->k, Rp, W, G, (const double*)z, seed, (double*)V, f, P->nsm, st);
+            else
+                e = launch_sweep_flow_fp32(P->t32, P->k, Rp, W, G, (const float*)z, seed, (float*)V, f, P->nsm, st);
+            if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
+            P->info.launches++;
+            return SGS_OK;
+        };
+        int rc;
+        if (plo > 0 && (rc = flow(0, plo))) return rc;
+        for (int l = lo; l < hi; ++l) {
+            const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
+            cudaError_t e;
+            if (P->precision == SGS_PREC_FP64)
+                e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
+            else
+                e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st);
+            if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
+            if (p1 > p0) P->info.launches++;
+        }
+        if (phi < P->N) {
+            const int32_t* node = P->precision == SGS_PREC_FP64 ? P->t64.node : P->t32.node;
+            if (phi > plo) LAUNCH(P, 1, launch_flow_mark(node, plo, phi, H, P->N, P->d_done, epoch, st));
+            if (plo > 0) CK(P, cudaMemsetAsync(P->d_flow, 0, sizeof(unsigned long long), st));  // ticket only
+            if ((rc = flow(phi, P->N))) return rc;
+        }
+        return SGS_OK;
     }
     for (int l = 0; l < P->nlevels; ++l) {
         const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
@@ -709,7 +801,6 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
         if (p1 > p0) P->info.launches++;
     }
-    (void)R;
     return SGS_OK;
 }
 
@@ -771,6 +862,7 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
         P->info.d2h_bytes += (int64_t)N * rn * sizeof(double);
     }
     CK(P, cudaStreamSynchronize(st));
+    if ((rc = check_flow_error(P))) return rc;
     P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
     P->sweep_timed = false;
     dfree(P, ob);
@@ -830,6 +922,8 @@ extern "C" int sgs_plan_info(const sgs_plan* P, sgs_info* info) {
     if (P->sweep_timed) {  // a device-resident sweep: time it once it has finished
         cudaSetDevice(P->device);
         if (cudaEventSynchronize(P->ev[6]) == cudaSuccess) info->ms_sweep = elapsed(P->ev[5], P->ev[6]);
+        // a device-resident dataflow sweep reports a failed wait here
+        return check_flow_error(const_cast<sgs_plan*>(P));
     }
     return SGS_OK;
 }
@@ -884,4 +978,110 @@ extern "C" int sgs_nn_adam(float* params, const float* grad, float* m, float* v,
     if (!params || !grad || !m || !v || step < 1) return set_err(nullptr, SGS_ERR_ARG, "invalid argument");
     cudaError_t e = launch_nn_adam(params, grad, m, v, step, lr, scale, (cudaStream_t)stream);
     return e == cudaSuccess ? SGS_OK : cuda_err(nullptr, e, "sgs_nn_adam");
+}
+
+// ---------------------------------------------------------------------------
+// Sweep configuration and its autotuner.
+extern "C" int sgs_plan_set_sweep(sgs_plan* P, const sgs_sweep_config* c) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!c) return set_err(P, SGS_ERR_ARG, "null sweep configuration");
+    if (c->mode < SGS_SWEEP_FLOW || c->mode > SGS_SWEEP_LEVELS) return set_err(P, SGS_ERR_ARG, "unknown sweep mode");
+    if (c->mode == SGS_SWEEP_FLOW &&
+        (c->chunk < 0 || c->chunk > 64 || c->blocks_per_sm < 0 || c->blocks_per_sm > 32 || c->lanes_g < 0 ||
+         c->lanes_g > 2 || c->lanes_w < 0 || c->lanes_w > 32 || (c->lanes_w & (c->lanes_w - 1)) ||
+         c->level_lo < 0 || c->level_hi < 0 || c->tight < 0 || c->tight > 1))
+        return set_err(P, SGS_ERR_ARG, "invalid dataflow sweep parameters");
+    P->sweep = *c;
+    if (P->sweep.chunk < 1) P->sweep.chunk = 1;
+    return SGS_OK;
+}
+
+// time one sweep configuration (after a warm-up run); < 0 on failure
+static int time_sweep(sgs_plan* P, const sgs_sweep_config& c, int R, int Rp, void* V, float* ms) {
+    P->sweep = c;
+    cudaStream_t st = P->stream;
+    int rc;
+    if ((rc = run_sweep(P, R, Rp, nullptr, 7, V, st))) return rc;
+    CK(P, cudaEventRecord(P->ev[5], st));
+    if ((rc = run_sweep(P, R, Rp, nullptr, 7, V, st))) return rc;
+    CK(P, cudaEventRecord(P->ev[6], st));
+    CK(P, cudaStreamSynchronize(st));
+    if ((rc = check_flow_error(P))) return rc;
+    *ms = elapsed(P->ev[5], P->ev[6]);
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* chosen, sgs_sweep_config* tried,
+                                   int32_t max_tried, int32_t* ntried) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "tune before prepare");
+    if (R < 1) return set_err(P, SGS_ERR_ARG, "invalid nreals");
+    CK(P, cudaSetDevice(P->device));
+    const int Rp = (R + 3) / 4 * 4;
+    const int cpn = Rp / 4;
+    const bool fp64 = P->precision == SGS_PREC_FP64;
+    const size_t es = fp64 ? sizeof(double) : sizeof(float);
+    void* V = nullptr;
+    int rc;
+    if ((rc = dalloc(P, (unsigned char**)&V, (size_t)P->N * Rp * es))) return rc;
+    const sgs_sweep_config saved = P->sweep;
+    std::vector<sgs_sweep_config> done;
+    int best = -1;
+    auto run = [&](sgs_sweep_config c) -> int {
+        float ms = 0.f;
+        int r = time_sweep(P, c, R, Rp, V, &ms);
+        if (r) return r;
+        c.ms = ms;
+        done.push_back(c);
+        if (best < 0 || ms < done[best].ms) best = (int)done.size() - 1;
+        return SGS_OK;
+    };
+    // stage 1: per-level launches and whole-sweep dataflow mappings
+    int p2 = 1;
+    while (p2 < cpn && p2 < 32) p2 <<= 1;
+    rc = run({SGS_SWEEP_LEVELS, 1, 0, 1, 0, 0, 0, 0, 0.f});
+    for (int W = p2; !rc && W >= std::max(1, p2 / 4); W >>= 1)
+        for (int G = 1; !rc && G <= (cpn >= 2 * W ? 2 : 1); ++G)
+            for (int tight = 0; !rc && tight <= 1; ++tight)
+                for (int chunk : {1, 2}) {
+                    if (rc) break;
+                    rc = run({SGS_SWEEP_FLOW, chunk, 0, G, W, 0, 0, tight, 0.f});
+                }
+    // stage 2: the best dataflow mapping, with the span of large levels
+    // (from the first to the last level holding at least `thr` nodes) swept
+    // by per-level launches instead
+    if (!rc) {
+        int bf = -1;
+        for (int i = 0; i < (int)done.size(); ++i)
+            if (done[i].mode == SGS_SWEEP_FLOW && (bf < 0 || done[i].ms < done[bf].ms)) bf = i;
+        int last_lo = -1, last_hi = -1;
+        for (int64_t thr : {(int64_t)P->nsm * 64, (int64_t)P->nsm * 16, (int64_t)P->nsm * 4}) {
+            int lo = -1, hi = -1;
+            for (int l = 0; l < P->nlevels; ++l)
+                if (P->h_loff[l + 1] - P->h_loff[l] >= thr) {
+                    if (lo < 0) lo = l;
+                    hi = l + 1;
+                }
+            if (bf < 0 || lo < 0 || (lo == last_lo && hi == last_hi)) continue;
+            last_lo = lo;
+            last_hi = hi;
+            sgs_sweep_config c = done[bf];
+            c.level_lo = lo;
+            c.level_hi = hi;
+            if ((rc = run(c))) break;
+        }
+    }
+    dfree(P, V);
+    if (rc || best < 0) {
+        P->sweep = saved;
+        return rc ? rc : set_err(P, SGS_ERR_CUDA, "no sweep configuration could be timed");
+    }
+    P->sweep = done[best];
+    P->sweep_timed = false;
+    if (chosen) *chosen = done[best];
+    const int n = (int)done.size();
+    if (tried)
+        for (int i = 0; i < std::min(n, (int)max_tried); ++i) tried[i] = done[i];
+    if (ntried) *ntried = n;
+    return SGS_OK;
 }

@@ -110,6 +110,25 @@ struct SweepTables {
     T* sigma;                    // P x S: conditional std (sqrt(sill) for the prior)
 };
 
+// Dataflow sweep state: warps take items (position in level order x piece of
+// the row) from `ticket` and wait, per neighbour, until the neighbour's flag
+// of the same piece equals epoch (set once that piece of this sweep is
+// stored).
+struct FlowArgs {
+    int64_t item0;               // first item of this launch (earlier ones are done)
+    int64_t item1;               // one past the last item of this launch
+    int64_t N;                   // nodes (flag stride between pieces)
+    int H;                       // pieces per row
+    int32_t* done;               // H x N flags, piece-major
+    int32_t epoch;               // > 0, new for every sweep over the same flags
+    unsigned long long* ticket;  // 1 counter, zero at launch
+    int32_t* err;                // 1 flag, zero at launch
+    int chunk;                   // consecutive items taken per ticket
+    int blocks_per_sm;           // resident blocks per SM to launch (<= occupancy)
+    int tight;                   // 1: kernel compiled for higher residency (register cap)
+    uint64_t wait_ns;            // longest wait for one flag before giving up
+};
+
 struct SolveArgs {
     GridDev grid;
     VarioDev vario;
@@ -159,6 +178,17 @@ cudaError_t launch_sweep_all_fp32(const SweepTables<float>& t, int k, const int3
                                   const float* z, uint64_t seed, float* V, cudaStream_t s);
 cudaError_t launch_sweep_all_fp64(const SweepTables<double>& t, int k, const int32_t* loff, int nlevels, int Rp,
                                   const double* z, uint64_t seed, double* V, cudaStream_t s);
+// all levels in one persistent dataflow launch (no level barriers); W lanes
+// per slice of the neighbour list and G chunks of 4 realizations per lane,
+// as returned by flow_layout, which also gives the pieces per row
+int flow_layout(int Rp, int& W, int& G);
+cudaError_t launch_sweep_flow_fp32(const SweepTables<float>& t, int k, int Rp, int W, int G, const float* z,
+                                   uint64_t seed, float* V, const FlowArgs& f, int nsm, cudaStream_t s);
+cudaError_t launch_sweep_flow_fp64(const SweepTables<double>& t, int k, int Rp, int W, int G, const double* z,
+                                   uint64_t seed, double* V, const FlowArgs& f, int nsm, cudaStream_t s);
+cudaError_t launch_flow_mark(const int32_t* node, int64_t p0, int64_t p1, int H, int64_t N, int32_t* done,
+                             int32_t epoch, cudaStream_t s);
+int sweep_flow_max_blocks_per_sm(bool fp64, int G, bool tight);
 // host z (R x N, realization-major double) on device -> node-major [N][Rp] of T
 cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s);
 cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, double* z, cudaStream_t s);

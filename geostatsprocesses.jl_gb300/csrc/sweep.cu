@@ -7,8 +7,13 @@
 // V[node][Rp] with realizations contiguous, so one node's update reads each
 // grid neighbour's row of realizations with coalesced vector loads:
 //   V[g][r] = b0 + sum_j w_j V[nb_j][r] + sigma * z[g][r]
-// All nodes of one dependency level are independent; levels run in order.
-// The data's fixed values enter through b0 (computed by the solve).
+// All nodes of one dependency level are independent.  The default sweep is
+// one persistent dataflow launch (sweep_flow_kernel) in which each node waits
+// only for its own neighbours; per-level launches and a cooperative launch
+// with grid barriers between levels are the alternatives.  The data's fixed
+// values enter through b0 (computed by the solve).
+#include <algorithm>
+
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -321,6 +326,307 @@ cudaError_t launch_sweep_all_fp32(const SweepTables<float>& t, int k, const int3
 cudaError_t launch_sweep_all_fp64(const SweepTables<double>& t, int k, const int32_t* loff, int nlevels, int Rp,
                                   const double* z, uint64_t seed, double* V, cudaStream_t s) {
     return sweep_all<double>(t, k, loff, nlevels, Rp, z, seed, V, s);
+}
+
+// ---------------------------------------------------------------------------
+// Dataflow sweep: the dependency levels in one persistent launch, with no
+// barrier between levels.  Realizations are independent, so a node's row is
+// cut into H pieces of P4 chunks of 4 realizations, and every (node, piece)
+// is a work item with its own flag: piece q of a node waits only for piece q
+// of its grid neighbours.  Items are numbered position-major (item = pos * H
+// + q, positions in level order) and warps take `chunk` consecutive items per
+// ticket.  A dependency always has a smaller item number (strictly lower
+// level, same piece), and item numbers are taken in increasing order by
+// warps that are running, so every wait ends: the smallest unfinished item
+// can always proceed.  Waits are bounded anyway (wait_ns of wall-clock time);
+// a warp that gives up sets err, skips the update but still raises its flag,
+// and no warp takes new tickets once err is set.
+//
+// Memory ordering: the item's lanes store the piece, each fences (gpu
+// scope), the warp synchronizes, lane 0 stores the flag; a reader's lanes
+// load flags, fence, synchronize, then read rows with L2-only loads
+// (ld.global.cg), so no stale L1 line of a row written by another SM is used.
+//
+// Lane layout inside a warp: W lanes per slice of the neighbour list (a
+// power of two), S = 32 / W slices, each lane G chunks of the piece
+// (P4 = W * G); the S partial sums are combined across lanes at the end.
+__device__ __forceinline__ int ld_flag(const int32_t* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_flag(int32_t* p, int v) {
+    asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait until piece q of every grid neighbour is stored in this sweep (flags
+// of piece q: done_q); false when a wait gave up.  A legitimate wait can last
+// as long as the longest dependency chain, so the bound is wall-clock time.
+__device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m, const int32_t* done_q,
+                                          const FlowArgs& f, int lane) {
+    bool ok = true;
+    for (int j = lane; j < m; j += 32) {
+        const int32_t* flag = done_q + idx[j];
+        uint64_t t0 = 0;
+        while (ld_flag(flag) != f.epoch) {
+            const uint64_t now = global_ns();
+            if (t0 == 0) t0 = now;
+            if (now - t0 > f.wait_ns) {
+                ok = false;
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    ok = __all_sync(FULL_MASK, ok);
+    __threadfence();
+    __syncwarp();
+    return ok;
+}
+
+// One piece (chunks [c0, c0 + W*G) of the row, clipped to the row) of one
+// node, FP32 values with compensated sums.
+template <int G>
+__device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int k, int64_t pos, int g, int m, int Rp,
+                                                int c0, int W, int lane, const float* __restrict__ z, uint64_t seed,
+                                                float* __restrict__ V) {
+    const int cpn = Rp >> 2;
+    const int S = 32 / W, s = lane / W, cl = lane % W;
+    const int32_t* idx = t.idx + pos * k;
+    const float2* w = reinterpret_cast<const float2*>(t.w) + pos * k;
+    Dot2 a[G][4];
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[gi][q].init(0.f, 0.f);
+#pragma unroll 4
+    for (int j = s; j < m; j += S) {
+        const float4* row = reinterpret_cast<const float4*>(V + (int64_t)idx[j] * Rp);
+        const float2 wj = w[j];
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi) {
+            const int ch = c0 + cl + gi * W;
+            if (ch < cpn) {
+                const float4 v = __ldcg(row + ch);
+                a[gi][0].add(wj.x, wj.y, v.x);
+                a[gi][1].add(wj.x, wj.y, v.y);
+                a[gi][2].add(wj.x, wj.y, v.z);
+                a[gi][3].add(wj.x, wj.y, v.w);
+            }
+        }
+    }
+    for (int o = W; o < 32; o <<= 1)
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                dot2_merge(a[gi][q], __shfl_xor_sync(FULL_MASK, a[gi][q].s, o),
+                           __shfl_xor_sync(FULL_MASK, a[gi][q].c, o));
+    if (s == 0) {
+        const float2 b0 = reinterpret_cast<const float2*>(t.b0)[pos];
+        const float2 sg = reinterpret_cast<const float2*>(t.sigma)[pos];
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi) {
+            const int ch = c0 + cl + gi * W;
+            if (ch < cpn) {
+                const float4 zz =
+                    z ? *reinterpret_cast<const float4*>(z + (int64_t)g * Rp + 4 * ch) : normals4(seed, g, ch);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) dot2_merge(a[gi][q], b0.x, b0.y);
+                a[gi][0].add(sg.x, sg.y, zz.x);
+                a[gi][1].add(sg.x, sg.y, zz.y);
+                a[gi][2].add(sg.x, sg.y, zz.z);
+                a[gi][3].add(sg.x, sg.y, zz.w);
+                Vec4<float>::store(V + (int64_t)g * Rp + 4 * ch, make_float4(a[gi][0].value(), a[gi][1].value(),
+                                                                             a[gi][2].value(), a[gi][3].value()));
+            }
+        }
+    }
+}
+
+// The same for FP64 values (plain FMA sums).
+template <int G>
+__device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, int k, int64_t pos, int g, int m, int Rp,
+                                                int c0, int W, int lane, const double* __restrict__ z, uint64_t seed,
+                                                double* __restrict__ V) {
+    const int cpn = Rp >> 2;
+    const int S = 32 / W, s = lane / W, cl = lane % W;
+    const int32_t* idx = t.idx + pos * k;
+    const double* w = t.w + pos * k;
+    D4 a[G];
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) a[gi] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 4
+    for (int j = s; j < m; j += S) {
+        const double2* row = reinterpret_cast<const double2*>(V + (int64_t)idx[j] * Rp);
+        const double wj = w[j];
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi) {
+            const int ch = c0 + cl + gi * W;
+            if (ch < cpn) {
+                const double2 v0 = __ldcg(row + 2 * ch);
+                const double2 v1 = __ldcg(row + 2 * ch + 1);
+                a[gi].x = fma(wj, v0.x, a[gi].x);
+                a[gi].y = fma(wj, v0.y, a[gi].y);
+                a[gi].z = fma(wj, v1.x, a[gi].z);
+                a[gi].w = fma(wj, v1.y, a[gi].w);
+            }
+        }
+    }
+    for (int o = W; o < 32; o <<= 1)
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi) {
+            a[gi].x += __shfl_xor_sync(FULL_MASK, a[gi].x, o);
+            a[gi].y += __shfl_xor_sync(FULL_MASK, a[gi].y, o);
+            a[gi].z += __shfl_xor_sync(FULL_MASK, a[gi].z, o);
+            a[gi].w += __shfl_xor_sync(FULL_MASK, a[gi].w, o);
+        }
+    if (s == 0) {
+        const double b0 = t.b0[pos], sg = t.sigma[pos];
+#pragma unroll
+        for (int gi = 0; gi < G; ++gi) {
+            const int ch = c0 + cl + gi * W;
+            if (ch < cpn) {
+                D4 zz;
+                if (z) {
+                    zz = load_d4(z + (int64_t)g * Rp + 4 * ch);
+                } else {
+                    const float4 f = normals4(seed, g, ch);
+                    zz = {(double)f.x, (double)f.y, (double)f.z, (double)f.w};
+                }
+                D4 r;
+                r.x = fma(sg, zz.x, a[gi].x + b0);
+                r.y = fma(sg, zz.y, a[gi].y + b0);
+                r.z = fma(sg, zz.z, a[gi].z + b0);
+                r.w = fma(sg, zz.w, a[gi].w + b0);
+                store_d4(V + (int64_t)g * Rp + 4 * ch, r);
+            }
+        }
+    }
+}
+
+template <typename T, int G, int MINB>
+__global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables<T> t, int k, int Rp, int W,
+                                                               const T* __restrict__ z, uint64_t seed,
+                                                               T* __restrict__ V, const FlowArgs f) {
+    const int lane = threadIdx.x & 31;
+    const int64_t items = f.item1;
+    const int P4 = W * G;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0)
+            base = (*(volatile int32_t*)f.err) ? (unsigned long long)items
+                                                 : f.item0 + atomicAdd(f.ticket, (unsigned long long)f.chunk);
+        base = __shfl_sync(FULL_MASK, base, 0);
+        if ((int64_t)base >= items) break;
+        const int64_t end = min((int64_t)base + f.chunk, items);
+        for (int64_t it = (int64_t)base; it < end; ++it) {
+            const int64_t pos = it / f.H;
+            const int q = (int)(it - pos * f.H);
+            const int g = t.node[pos];
+            const int m = t.m[pos];
+            int32_t* done_q = f.done + (int64_t)q * f.N;
+            const bool ok = flow_wait(t.idx + pos * k, m, done_q, f, lane);
+            if (ok) {
+                if constexpr (sizeof(T) == 4) flow_piece_fp32<G>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
+                else flow_piece_fp64<G>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
+            } else if (lane == 0) {
+                atomicExch(f.err, 1);
+            }
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_flag(done_q + g, f.epoch);
+        }
+    }
+}
+
+// Flags of the positions [p0, p1) swept by per-level launches before a
+// dataflow launch takes over (every piece).
+__global__ void flow_mark_kernel(const int32_t* __restrict__ node, int64_t p0, int64_t p1, int H, int64_t N,
+                                 int32_t* __restrict__ done, int32_t epoch) {
+    const int64_t n = (p1 - p0) * H;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = p0 + i / H;
+        const int q = (int)(i % H);
+        done[(int64_t)q * N + node[pos]] = epoch;
+    }
+}
+
+// Lane layout for a row of cpn chunks: W lanes per slice (0 = automatic),
+// G chunks per lane; returns the pieces per row.
+int flow_layout(int Rp, int& W, int& G) {
+    const int cpn = Rp / 4;
+    int p2 = 1;
+    while (p2 < cpn && p2 < 32) p2 <<= 1;
+    if (W <= 0 || W > p2) W = p2;
+    if (G != 2) G = 1;
+    if (W * G > cpn && G == 2) G = 1;
+    return (cpn + W * G - 1) / (W * G);
+}
+
+template <typename T, int G, int MINB>
+static cudaError_t flow_launch(const SweepTables<T>& t, int k, int Rp, int W, const T* z, uint64_t seed, T* V,
+                               const FlowArgs& f, int nsm, cudaStream_t s) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_flow_kernel<T, G, MINB>, 256, 0);
+    if (e != cudaSuccess) return e;
+    if (f.blocks_per_sm > 0 && f.blocks_per_sm < per_sm) per_sm = f.blocks_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    const int64_t items = (f.item1 - f.item0 + f.chunk - 1) / f.chunk;
+    int64_t blocks = std::min<int64_t>((int64_t)nsm * per_sm, (items + 7) / 8);
+    if (blocks < 1) blocks = 1;
+    sweep_flow_kernel<T, G, MINB><<<(int)blocks, 256, 0, s>>>(t, k, Rp, W, z, seed, V, f);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t sweep_flow(const SweepTables<T>& t, int k, int Rp, int W, int G, const T* z, uint64_t seed, T* V,
+                              const FlowArgs& f, int nsm, cudaStream_t s) {
+    if (f.item1 <= f.item0) return cudaSuccess;
+    if (G == 2) return f.tight ? flow_launch<T, 2, 4>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                               : flow_launch<T, 2, 1>(t, k, Rp, W, z, seed, V, f, nsm, s);
+    return f.tight ? flow_launch<T, 1, 6>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                   : flow_launch<T, 1, 1>(t, k, Rp, W, z, seed, V, f, nsm, s);
+}
+
+cudaError_t launch_sweep_flow_fp32(const SweepTables<float>& t, int k, int Rp, int W, int G, const float* z,
+                                   uint64_t seed, float* V, const FlowArgs& f, int nsm, cudaStream_t s) {
+    return sweep_flow<float>(t, k, Rp, W, G, z, seed, V, f, nsm, s);
+}
+
+cudaError_t launch_sweep_flow_fp64(const SweepTables<double>& t, int k, int Rp, int W, int G, const double* z,
+                                   uint64_t seed, double* V, const FlowArgs& f, int nsm, cudaStream_t s) {
+    return sweep_flow<double>(t, k, Rp, W, G, z, seed, V, f, nsm, s);
+}
+
+cudaError_t launch_flow_mark(const int32_t* node, int64_t p0, int64_t p1, int H, int64_t N, int32_t* done,
+                             int32_t epoch, cudaStream_t s) {
+    if (p1 <= p0) return cudaSuccess;
+    const int64_t n = (p1 - p0) * H;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1 << 16);
+    flow_mark_kernel<<<blocks, 256, 0, s>>>(node, p0, p1, H, N, done, epoch);
+    return cudaGetLastError();
+}
+
+int sweep_flow_max_blocks_per_sm(bool fp64, int G, bool tight) {
+    int per_sm = 0;
+    if (fp64) {
+        if (G == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, tight ? sweep_flow_kernel<double, 2, 4> : sweep_flow_kernel<double, 2, 1>, 256, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, tight ? sweep_flow_kernel<double, 1, 6> : sweep_flow_kernel<double, 1, 1>, 256, 0);
+    } else {
+        if (G == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, tight ? sweep_flow_kernel<float, 2, 4> : sweep_flow_kernel<float, 2, 1>, 256, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, tight ? sweep_flow_kernel<float, 1, 6> : sweep_flow_kernel<float, 1, 1>, 256, 0);
+    }
+    return per_sm;
 }
 
 // ---------------------------------------------------------------------------

@@ -31,6 +31,7 @@ SGS_PREC_FP64 = 0
 SGS_PREC_FP32_REFINE = 1
 
 SGS_FLAG_ONE_LAUNCH_SWEEP = 1
+SGS_FLAG_LEVEL_SWEEP = 2
 
 SGS_NN_FEATURES = 8
 SGS_NN_PARAMS = 2401
@@ -79,6 +80,28 @@ class SgsProblem(C.Structure):
     ]
 
 
+SGS_SWEEP_FLOW = 0
+SGS_SWEEP_COOPERATIVE = 1
+SGS_SWEEP_LEVELS = 2
+
+
+class SgsSweepConfig(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32),
+        ("chunk", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("lanes_g", C.c_int32),
+        ("lanes_w", C.c_int32),
+        ("level_lo", C.c_int32),
+        ("level_hi", C.c_int32),
+        ("tight", C.c_int32),
+        ("ms", C.c_float),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class SgsInfo(C.Structure):
     _fields_ = [
         ("nnodes", C.c_int64),
@@ -124,6 +147,8 @@ EXPORTS = (
     "sgs_nn_backward",
     "sgs_nn_adam",
     "sgs_schedule_noalloc",
+    "sgs_plan_set_sweep",
+    "sgs_plan_tune_sweep",
 )
 
 _lib = None
@@ -167,6 +192,11 @@ def _declare(lib):
     lib.sgs_plan_features_device.restype = C.c_int
     lib.sgs_plan_set_network.argtypes = [P, C.POINTER(C.c_float)]
     lib.sgs_plan_set_network.restype = C.c_int
+    lib.sgs_plan_set_sweep.argtypes = [P, C.POINTER(SgsSweepConfig)]
+    lib.sgs_plan_set_sweep.restype = C.c_int
+    lib.sgs_plan_tune_sweep.argtypes = [P, C.c_int32, C.POINTER(SgsSweepConfig), C.POINTER(SgsSweepConfig),
+                                        C.c_int32, C.POINTER(C.c_int32)]
+    lib.sgs_plan_tune_sweep.restype = C.c_int
     lib.sgs_nn_forward.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P]
     lib.sgs_nn_forward.restype = C.c_int
     lib.sgs_nn_backward.argtypes = [P, P, P, P, C.c_int64, C.c_int32, P, P, P]

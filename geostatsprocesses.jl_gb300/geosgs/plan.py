@@ -32,6 +32,9 @@ class Plan:
         info = self.info()
         self.k = int(info.maxneighbors)
         self.prepared = False
+        self._sweep = _abi.SgsSweepConfig(2 if problem.flags & _abi.SGS_FLAG_LEVEL_SWEEP else
+                                          1 if problem.flags & _abi.SGS_FLAG_ONE_LAUNCH_SWEEP else 0,
+                                          1, 0, 1, 0, 0, 0, 0, 0.0).as_dict()
 
     def close(self):
         if getattr(self, "h", None):
@@ -96,6 +99,30 @@ class Plan:
             raise ValueError(f"expected {_abi.SGS_NN_PARAMS} parameters")
         self._check(self.lib.sgs_plan_set_network(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
         return self
+
+    def set_sweep(self, mode=_abi.SGS_SWEEP_FLOW, chunk=1, blocks_per_sm=0, lanes_g=1, lanes_w=0, level_lo=0,
+                  level_hi=0, tight=0, **_ignored):
+        """How simulate() runs the sweep (SGS_SWEEP_* mode and dataflow
+        mapping; see sgs_sweep_config).  Accepts a dict returned by
+        tune_sweep() as keyword arguments."""
+        c = _abi.SgsSweepConfig(mode, chunk, blocks_per_sm, lanes_g, lanes_w, level_lo, level_hi, tight, 0.0)
+        self._check(self.lib.sgs_plan_set_sweep(self.h, C.byref(c)))
+        self._sweep = c.as_dict()
+        return self
+
+    def sweep_config(self) -> dict:
+        """The sweep configuration set last (set_sweep / tune_sweep)."""
+        return dict(self._sweep)
+
+    def tune_sweep(self, nreals: int):
+        """Times the candidate sweep configurations for nreals realizations,
+        keeps the fastest; returns (chosen, [all timed]) as dicts."""
+        chosen = _abi.SgsSweepConfig()
+        tried = (_abi.SgsSweepConfig * 64)()
+        n = C.c_int32()
+        self._check(self.lib.sgs_plan_tune_sweep(self.h, nreals, C.byref(chosen), tried, 64, C.byref(n)))
+        self._sweep = chosen.as_dict()
+        return chosen.as_dict(), [tried[i].as_dict() for i in range(min(n.value, 64))]
 
     def info(self) -> _abi.SgsInfo:
         inf = _abi.SgsInfo()

@@ -72,7 +72,8 @@ def build_problem(process: GaussianProcess, domain: CartesianGrid, data: GeoTabl
     p.refine_steps = int(getattr(method, "refine_steps", 2))
     p.warm_start = 1 if getattr(method, "warm_start", False) else 0
     p.device = int(getattr(method, "device", 0))
-    p.flags = _abi.SGS_FLAG_ONE_LAUNCH_SWEEP if getattr(method, "one_launch_sweep", False) else 0
+    p.flags = ((_abi.SGS_FLAG_ONE_LAUNCH_SWEEP if getattr(method, "one_launch_sweep", False) else 0)
+               | (_abi.SGS_FLAG_LEVEL_SWEEP if getattr(method, "level_sweep", False) else 0))
     perm = method.path.permutation(domain.nelements())
     if perm is not None:
         perm = np.ascontiguousarray(perm, dtype=np.int32)

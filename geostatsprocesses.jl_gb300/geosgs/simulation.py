@@ -44,6 +44,7 @@ class GPUSEQSIM(FieldSimulationMethod):
     warm_start: bool = False
     device: int = 0
     one_launch_sweep: bool = False  # all dependency levels in one cooperative launch
+    level_sweep: bool = False       # one launch per dependency level (default: dataflow)
 
 
 class Ensemble:

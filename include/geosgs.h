@@ -62,9 +62,12 @@ extern "C" {
                                    variance, FP32 weights and sweep                 */
 
 /* ---- sgs_problem.flags --------------------------------------------------- */
-#define SGS_FLAG_ONE_LAUNCH_SWEEP 1  /* sweep all dependency levels in one cooperative
-                                        launch with a grid barrier between levels,
-                                        instead of one launch per level */
+/* The default sweep is one persistent dataflow launch: warps take nodes in
+   level order and wait (bounded) on per-node flags of their neighbours, with
+   no barrier between levels.  These flags select the alternatives: */
+#define SGS_FLAG_ONE_LAUNCH_SWEEP 1  /* one cooperative launch with a grid barrier
+                                        between dependency levels */
+#define SGS_FLAG_LEVEL_SWEEP      2  /* one launch per dependency level */
 
 /* ---- per-node solve status (sgs_plan_weights) --------------------------- */
 #define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */
@@ -224,6 +227,41 @@ int sgs_nn_backward(const float* params, const float* feat, const int32_t* count
  * with gradient scale `scale` (e.g. 1 / batch systems); step counts from 1. */
 int sgs_nn_adam(float* params, const float* grad, float* m, float* v, int32_t step, float lr, float scale,
                 void* stream);
+
+/* ---- sweep configuration and autotuning --------------------------------- */
+#define SGS_SWEEP_FLOW        0  /* one persistent dataflow launch (default)      */
+#define SGS_SWEEP_COOPERATIVE 1  /* one cooperative launch, grid barrier per level */
+#define SGS_SWEEP_LEVELS      2  /* one launch per dependency level                */
+
+typedef struct sgs_sweep_config {
+    int32_t mode;             /* SGS_SWEEP_*                                         */
+    int32_t chunk;            /* flow: work items a warp takes per ticket            */
+    int32_t blocks_per_sm;    /* flow: resident 256-thread blocks per SM (0 = max)   */
+    int32_t lanes_g;          /* flow: chunks of 4 realizations per lane, 1 or 2     */
+    int32_t lanes_w;          /* flow: lanes per slice of the neighbour list, a power
+                                 of two <= 32 (0 = the row's chunks, at most 32);
+                                 32 / lanes_w slices split the neighbour list and a
+                                 row is cut into pieces of lanes_w * lanes_g chunks,
+                                 each a separate work item                          */
+    int32_t level_lo;         /* flow: dependency levels [level_lo, level_hi) are   */
+    int32_t level_hi;         /* swept by per-level launches, the levels before and
+                                 after them by one dataflow launch each             */
+    int32_t tight;            /* flow: 1 = the kernel variant compiled for higher
+                                 residency (register cap)                           */
+    float   ms;               /* sgs_plan_tune_sweep: measured time of this config   */
+} sgs_sweep_config;
+
+/* Sets how sgs_plan_simulate* run the sweep.  No counterpart in the reference
+ * (its draw loop is serial, seqsim.jl:98-138); results are the same for every
+ * configuration up to the order of FP32 roundings. */
+int sgs_plan_set_sweep(sgs_plan* plan, const sgs_sweep_config* config);
+/* Times the candidate sweep configurations for `nreals` realizations on the
+ * prepared plan (each on a scratch value array, after one warm-up run), keeps
+ * the fastest for later sgs_plan_simulate* calls and returns it in *chosen
+ * (may be NULL).  tried (may be NULL) receives up to max_tried of the
+ * configurations timed, and *ntried (may be NULL) their count. */
+int sgs_plan_tune_sweep(sgs_plan* plan, int32_t nreals, sgs_sweep_config* chosen, sgs_sweep_config* tried,
+                        int32_t max_tried, int32_t* ntried);
 
 /* ---- allocation-free schedule ------------------------------------------ */
 #define SGS_NOALLOC_MAX_LEVELS 262144

@@ -10,7 +10,7 @@ import pytest
 
 import geosgs
 from conftest import golden_cases, golden_problem, load_golden
-from geosgs import workloads
+from geosgs import _abi, workloads
 
 pytestmark = pytest.mark.gpu
 
@@ -200,20 +200,49 @@ def test_error_codes(geosgs_lib):
     assert e.value.code == _abi.SGS_ERR_ARG
 
 
-@pytest.mark.parametrize("nreals", [4, 8, 12, 64, 256])
+SWEEP_FORMS = [
+    dict(mode=_abi.SGS_SWEEP_FLOW),                                   # default dataflow mapping
+    dict(mode=_abi.SGS_SWEEP_FLOW, chunk=2, lanes_w=8),                # rows cut into pieces
+    dict(mode=_abi.SGS_SWEEP_FLOW, chunk=4, lanes_g=2, tight=1, blocks_per_sm=1),
+    dict(mode=_abi.SGS_SWEEP_FLOW, lanes_w=4, tight=1, level_lo=0, level_hi=3),  # per-level launches first
+    dict(mode=_abi.SGS_SWEEP_FLOW, level_lo=5, level_hi=12),           # dataflow, per-level, dataflow
+    dict(mode=_abi.SGS_SWEEP_FLOW, level_lo=0, level_hi=10 ** 6),      # every level by per-level launches
+    dict(mode=_abi.SGS_SWEEP_LEVELS),
+    dict(mode=_abi.SGS_SWEEP_COOPERATIVE),
+]
+
+
+@pytest.mark.parametrize("nreals", [4, 8, 12, 64, 200, 256, 520])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_sweep_variants_agree_with_oracle(precision, nreals, oracle_mod, geosgs_lib):
-    """The sweep's launch forms (one cooperative launch over all levels; one
-    launch per level with a thread per chunk of 4 realizations, or with a
-    warp per node splitting the neighbour list for R <= 64) all match the
-    oracle."""
+    """Every form of the sweep matches the oracle: the persistent dataflow
+    launch (rows cut into independent pieces, 1 or 2 chunks of 4
+    realizations per lane, neighbour lists split over lane slices, 1-4 items
+    per ticket, register-capped variants, reduced residency, leading levels
+    by per-level launches), one launch per level (thread per chunk, or warp
+    per node for R <= 64), and one cooperative launch with grid barriers
+    between levels."""
     wl = workloads.small(n=48, k=16, ndata=25, vario="gau", nugget=0.02, precision=precision, nreals=nreals)
     z = np.random.default_rng(nreals).standard_normal((nreals, 48 * 48))
-    ref = None
-    for one_launch in (False, True):
-        wl.method.one_launch_sweep = one_launch
-        G, O = both(wl, oracle_mod, precision)
-        if ref is None:
-            ref = O.simulate(nreals, z)
-        assert rel_err(G.simulate(nreals, z), ref) <= VALUE_TOL
-        G.close()
+    G, O = both(wl, oracle_mod, precision)
+    ref = O.simulate(nreals, z)
+    for form in SWEEP_FORMS:
+        G.set_sweep(**form)
+        assert rel_err(G.simulate(nreals, z), ref) <= VALUE_TOL, form
+        # seeded draws: the same values whatever the form
+        if form is SWEEP_FORMS[0]:
+            seeded = G.simulate(nreals, seed=5)
+        else:
+            assert rel_err(G.simulate(nreals, seed=5), seeded) <= VALUE_TOL, form
+    G.close()
+
+
+def test_sweep_autotuner_keeps_the_fastest_form(oracle_mod, geosgs_lib):
+    wl = workloads.small(n=64, k=24, ndata=40, vario="exp", nugget=0.05, precision="fp32", nreals=64)
+    z = np.random.default_rng(3).standard_normal((64, 64 * 64))
+    G, O = both(wl, oracle_mod, "fp32")
+    chosen, tried = G.tune_sweep(64)
+    assert len(tried) >= 4 and all(t["ms"] > 0 for t in tried)
+    assert chosen["ms"] == min(t["ms"] for t in tried)
+    assert rel_err(G.simulate(64, z), O.simulate(64, z)) <= VALUE_TOL
+    G.close()

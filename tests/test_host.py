@@ -58,9 +58,10 @@ def test_struct_layout_matches_header():
 #include <stdio.h>
 #include "geosgs.h"
 int main(void){
- printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sgs_problem), offsetof(sgs_problem, variogram),
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sgs_problem), offsetof(sgs_problem, variogram),
    offsetof(sgs_problem, mean), offsetof(sgs_problem, ball), offsetof(sgs_problem, path),
-   offsetof(sgs_problem, flags), sizeof(sgs_info), offsetof(sgs_info, ms_sweep));
+   offsetof(sgs_problem, flags), sizeof(sgs_info), offsetof(sgs_info, ms_sweep),
+   sizeof(sgs_sweep_config), offsetof(sgs_sweep_config, ms));
  return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -69,9 +70,9 @@ int main(void){
         exe = os.path.join(d, "p")
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
-    P, I = _abi.SgsProblem, _abi.SgsInfo
+    P, I, W = _abi.SgsProblem, _abi.SgsInfo, _abi.SgsSweepConfig
     want = [C.sizeof(P), P.variogram.offset, P.mean.offset, P.ball.offset, P.path.offset, P.flags.offset,
-            C.sizeof(I), I.ms_sweep.offset]
+            C.sizeof(I), I.ms_sweep.offset, C.sizeof(W), W.ms.offset]
     assert got == want
 
 
