@@ -40,14 +40,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--nreals", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 path measurement")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-nodes", type=int, default=60000, help="oracle sample size (nodes)")
     ap.add_argument("--no-learned", action="store_true", help="skip training and timing the learned warm start")
-    ap.add_argument("--learned-systems", type=int, default=600000, help="training systems for the warm start")
+    ap.add_argument("--learned-systems", type=int, default=None,
+                    help="training systems for the warm start (default 600,000; 10,000,000 for c4)")
     ap.add_argument("--learned-epochs", type=int, default=8)
     ap.add_argument("--sweep-config", default=None,
                     help='JSON sweep configuration (sgs_sweep_config fields) instead of the autotuner, e.g. '
@@ -64,6 +65,8 @@ def workload(name, precision, nreals, grid=None, ndata=None):
         wl = workloads.c1(precision)
     elif name == "c2":
         wl = workloads.c2(precision)
+    elif name == "c4":
+        wl = workloads.c4(precision, dims=tuple(int(x) for x in grid.split(",")) if grid else (256, 256, 256))
     elif grid:
         dims = tuple(int(x) for x in grid.split(","))
         wl = workloads.c3(precision, dims=dims, ndata=ndata if ndata is not None else 5000)
@@ -342,6 +345,8 @@ def main():
         # network warm-starting every FP32 solve
         from geosgs import learned
 
+        if args.learned_systems is None:
+            args.learned_systems = 10_000_000 if args.workload == "c4" else 600_000
         t0 = time.perf_counter()
         feat, count, target = learned.generate(args.learned_systems, seed=11, torch=torch, dims=(48, 48, 32),
                                                k=wl.method.maxneighbors)

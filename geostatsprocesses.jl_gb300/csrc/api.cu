@@ -282,7 +282,7 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     if (pr->refine_steps < 0 || pr->refine_steps > 4) return set_err(P, SGS_ERR_ARG, "refine_steps must be in 0..4");
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
-    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP))
+    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32))
         return set_err(P, SGS_ERR_ARG, "unknown flags");
     if ((pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) && (pr->flags & SGS_FLAG_LEVEL_SWEEP))
         return set_err(P, SGS_ERR_ARG, "SGS_FLAG_ONE_LAUNCH_SWEEP and SGS_FLAG_LEVEL_SWEEP exclude each other");
@@ -477,6 +477,21 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+// Warm-start predictions [N][k] of the plan's network for every system: BF16
+// on the tensor cores (tcgen05) or FP32 on the CUDA cores.  The tensor-core
+// kernel's error flag is scratch[12] (read by the caller after a sync).
+static int run_predict(sgs_plan* P, float* out, bool tensor_cores, cudaStream_t st) {
+    if (tensor_cores) {
+        CK(P, cudaMemsetAsync(P->d_scratch + 12, 0, sizeof(int32_t), st));
+        LAUNCH(P, 1, launch_nn_predict_tc(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn, out,
+                                          P->d_scratch + 12, P->nsm, st));
+    } else {
+        LAUNCH(P, 1, launch_nn_predict_plan(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn, out,
+                                            st));
+    }
+    return SGS_OK;
+}
+
 static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     SolveArgs s{};
     s.grid = P->grid;
@@ -515,8 +530,7 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
         // refines from them
         int rc;
         if (!P->d_winit && (rc = dalloc(P, &P->d_winit, (size_t)P->N * P->k))) return rc;
-        LAUNCH(P, 1, launch_nn_predict_plan(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn,
-                                            P->d_winit, P->stream));
+        if ((rc = run_predict(P, P->d_winit, !(P->flags & SGS_FLAG_NN_FP32), P->stream))) return rc;
         CK(P, cudaMemsetAsync(nwarm, 0, sizeof(unsigned long long), P->stream));
         s.w_init = P->d_winit;
         s.n_warm = nwarm;
@@ -533,8 +547,11 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     unsigned long long hw = 0;
     CK(P, cudaMemcpyAsync(&h, nfb, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
     if (s.n_warm) CK(P, cudaMemcpyAsync(&hw, nwarm, sizeof(hw), cudaMemcpyDeviceToHost, P->stream));
+    int32_t htc = 0;
+    if (s.n_warm) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + 12, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
     CK(P, cudaStreamSynchronize(P->stream));
-    P->info.d2h_bytes += sizeof(int32_t) + (s.n_warm ? sizeof(hw) : 0);
+    P->info.d2h_bytes += sizeof(int32_t) + (s.n_warm ? sizeof(hw) + sizeof(htc) : 0);
+    if (htc) return set_err(P, SGS_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait exceeded its bound");
     P->info.n_fp64_fallback = h;
     P->info.n_warm_accepted = (int64_t)hw;
     return SGS_OK;
@@ -1083,5 +1100,21 @@ extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* cho
     if (tried)
         for (int i = 0; i < std::min(n, (int)max_tried); ++i) tried[i] = done[i];
     if (ntried) *ntried = n;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_predict_device(sgs_plan* P, float* out, int32_t tensor_cores, void* stream) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "predict before prepare");
+    if (!P->d_nn) return set_err(P, SGS_ERR_STATE, "no network set (sgs_plan_set_network)");
+    if (!out) return set_err(P, SGS_ERR_ARG, "null output");
+    CK(P, cudaSetDevice(P->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->stream;
+    int rc;
+    if ((rc = run_predict(P, out, tensor_cores != 0, st))) return rc;
+    int32_t htc = 0;
+    if (tensor_cores) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + 12, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CK(P, cudaStreamSynchronize(st));
+    if (htc) return set_err(P, SGS_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait exceeded its bound");
     return SGS_OK;
 }

@@ -201,6 +201,11 @@ cudaError_t launch_nn_features(const GridDev& G, const VarioDev& v, const int32_
                                const double* data_xyz, float* feat, cudaStream_t s);
 cudaError_t launch_nn_predict_plan(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,
                                    const double* data_xyz, const float* params, float* out, cudaStream_t s);
+// BF16 tensor-core inference (learned_tc.cu); err: device flag set when an
+// MMA completion wait gave up
+cudaError_t launch_nn_predict_tc(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,
+                                 const double* data_xyz, const float* params, float* out, int32_t* err, int nsm,
+                                 cudaStream_t s);
 cudaError_t launch_nn_forward(const float* params, const float* feat, const int32_t* count, int64_t nsys, int k,
                               float* pred, cudaStream_t s);
 cudaError_t launch_nn_backward(const float* params, const float* feat, const int32_t* count, const float* target,

@@ -32,6 +32,7 @@ SGS_PREC_FP32_REFINE = 1
 
 SGS_FLAG_ONE_LAUNCH_SWEEP = 1
 SGS_FLAG_LEVEL_SWEEP = 2
+SGS_FLAG_NN_FP32 = 4
 
 SGS_NN_FEATURES = 8
 SGS_NN_PARAMS = 2401
@@ -149,6 +150,7 @@ EXPORTS = (
     "sgs_schedule_noalloc",
     "sgs_plan_set_sweep",
     "sgs_plan_tune_sweep",
+    "sgs_plan_predict_device",
 )
 
 _lib = None
@@ -197,6 +199,8 @@ def _declare(lib):
     lib.sgs_plan_tune_sweep.argtypes = [P, C.c_int32, C.POINTER(SgsSweepConfig), C.POINTER(SgsSweepConfig),
                                         C.c_int32, C.POINTER(C.c_int32)]
     lib.sgs_plan_tune_sweep.restype = C.c_int
+    lib.sgs_plan_predict_device.argtypes = [P, P, C.c_int32, P]
+    lib.sgs_plan_predict_device.restype = C.c_int
     lib.sgs_nn_forward.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P]
     lib.sgs_nn_forward.restype = C.c_int
     lib.sgs_nn_backward.argtypes = [P, P, P, P, C.c_int64, C.c_int32, P, P, P]

@@ -124,6 +124,11 @@ class Plan:
         self._sweep = chosen.as_dict()
         return chosen.as_dict(), [tried[i].as_dict() for i in range(min(n.value, 64))]
 
+    def predict_device(self, out_ptr: int, tensor_cores: bool = True, stream: int | None = None):
+        """Warm-start predictions [N][k] (float32) into a device buffer."""
+        self._check(self.lib.sgs_plan_predict_device(self.h, C.c_void_p(out_ptr), 1 if tensor_cores else 0,
+                                                     C.c_void_p(stream) if stream else None))
+
     def info(self) -> _abi.SgsInfo:
         inf = _abi.SgsInfo()
         self._check(self.lib.sgs_plan_info(self.h, C.byref(inf)))

@@ -11,6 +11,11 @@ the stated seed.  Coordinates are cell units with origin 0 and unit spacing.
   c3  3D 200x200x100, 5,000 data uniform in the box (seed 3, values N(0,1)),
       exponential (sill 1, ranges 50/25/5, 30 deg RotZ, nugget 0.05), search
       ellipsoid = the variogram's, k=48, RandomPath seed 4, 256 realizations
+  c4  3D 256x256x256 (16.8M nodes), unconditional, spherical (sill 1, ranges
+      40/20/8, 30 deg RotZ, nugget 0.1: one draw inside the warm-start
+      network's training distribution), search ellipsoid = the variogram's,
+      k=32, RandomPath seed 5, 64 realizations (the learned warm start's
+      evaluation run)
 """
 from __future__ import annotations
 
@@ -65,6 +70,15 @@ def c3(precision: str = "fp32", nreals: int = 256, dims=(200, 200, 100), ndata: 
     m = GPUSEQSIM(path=RandomPath(4), maxneighbors=48, neighborhood=ball, precision=precision)
     name = "c3_3d_%dx%dx%d_exp_aniso_d%d_k48" % (*dims, ndata)
     return Workload(name, proc, grid, data, m, nreals)
+
+
+def c4(precision: str = "fp32", nreals: int = 64, dims=(256, 256, 256)) -> Workload:
+    grid = CartesianGrid(tuple(dims))
+    ball = MetricBall((40.0, 20.0, 8.0), RotZ(30.0))
+    proc = GaussianProcess(SphericalVariogram(ball, sill=1.0, nugget=0.1), 0.0)
+    m = GPUSEQSIM(path=RandomPath(5), maxneighbors=32, neighborhood=ball, precision=precision)
+    name = "c4_3d_%dx%dx%d_sph_aniso_uncond_k32" % tuple(dims)
+    return Workload(name, proc, grid, None, m, nreals)
 
 
 def small(dim=2, n=24, k=8, ndata=0, vario="sph", seed=0, nugget=0.0, ranges=(6.0, 6.0, 6.0),

@@ -68,6 +68,8 @@ extern "C" {
 #define SGS_FLAG_ONE_LAUNCH_SWEEP 1  /* one cooperative launch with a grid barrier
                                         between dependency levels */
 #define SGS_FLAG_LEVEL_SWEEP      2  /* one launch per dependency level */
+#define SGS_FLAG_NN_FP32          4  /* warm-start inference in FP32 on the CUDA cores
+                                        instead of BF16 on the tensor cores */
 
 /* ---- per-node solve status (sgs_plan_weights) --------------------------- */
 #define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */
@@ -227,6 +229,13 @@ int sgs_nn_backward(const float* params, const float* feat, const int32_t* count
  * with gradient scale `scale` (e.g. 1 / batch systems); step counts from 1. */
 int sgs_nn_adam(float* params, const float* grad, float* m, float* v, int32_t step, float lr, float scale,
                 void* stream);
+
+/* Writes the warm-start network's predicted weights of every system of a
+ * prepared plan (device array of nnodes x maxneighbors floats, zero past each
+ * node's neighbour count): BF16 inference with FP32 accumulation on the
+ * tensor cores (tensor_cores = 1) or FP32 on the CUDA cores (0).  No
+ * counterpart in the reference.  Returns when the predictions are complete. */
+int sgs_plan_predict_device(sgs_plan* plan, float* out_dev, int32_t tensor_cores, void* stream);
 
 /* ---- sweep configuration and autotuning --------------------------------- */
 #define SGS_SWEEP_FLOW        0  /* one persistent dataflow launch (default)      */

@@ -63,3 +63,41 @@ def test_training_and_warm_started_solve(oracle_mod, geosgs_lib):
     z = np.random.default_rng(4).standard_normal((8, O.N))
     vg, vo = G.simulate(8, z), O.simulate(8, z)
     assert float(np.max(np.abs(vg - vo) / np.maximum(np.abs(vo), 1.0))) <= 1e-6
+
+
+@pytest.mark.parametrize("k", [32, 48])
+def test_tensor_core_inference_matches_fp32(k, geosgs_lib):
+    """BF16 tensor-core inference (tcgen05, FP32 accumulation) agrees with
+    the FP32 CUDA-core forward pass of the same network on a plan's systems
+    within BF16 rounding, and writes zeros past each node's neighbour count."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(7)
+    params = learned.init_params(5) + rng.standard_normal(nn_oracle.NPARAMS).astype(np.float32) * 0.05
+    wl = workloads.small(dim=3, n=40, nz=12, k=k, ndata=30, vario="exp", ranges=(12.0, 6.0, 4.0),
+                         rotation=geosgs.RotZ(25.0), nugget=0.05,
+                         ball=geosgs.MetricBall((12.0, 6.0, 4.0), geosgs.RotZ(25.0)), precision="fp32", nreals=4)
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = geosgs.Plan(p, keep).set_network(params).prepare()
+    N = G.N
+    tc = torch.full((N, G.k), 7.0, dtype=torch.float32, device="cuda")
+    f32 = torch.full((N, G.k), 7.0, dtype=torch.float32, device="cuda")
+    G.predict_device(tc.data_ptr(), tensor_cores=True)
+    G.predict_device(f32.data_ptr(), tensor_cores=False)
+    a, b = tc.cpu().numpy(), f32.cpu().numpy()
+    _, cnt = G.neighbors()
+    pad = np.arange(G.k)[None, :] >= cnt[:, None]
+    assert np.all(a[pad] == 0.0) and np.all(b[pad] == 0.0)
+    scale = float(np.abs(b).max())
+    err = np.abs(a - b)
+    print(f"k={k}: max |tc - fp32| {err.max():.3e}, mean {err.mean():.3e}, scale {scale:.3e}")
+    assert err.max() <= 0.05 * scale
+    assert err.mean() <= 0.01 * float(np.abs(b).mean()) + 1e-4
+    # the FP32 path itself is the numpy restatement's forward
+    feat = torch.empty((N, G.k, nn_oracle.F), dtype=torch.float32, device="cuda")
+    G._check(G.lib.sgs_plan_features_device(G.h, __import__("ctypes").c_void_p(feat.data_ptr()), None))
+    fh = feat.cpu().numpy()
+    for g in rng.choice(N, 20, replace=False):
+        n = int(cnt[g])
+        if n:
+            np.testing.assert_allclose(b[g, :n], nn_oracle.forward(params, fh[g], n), rtol=1e-4, atol=1e-5)
+    G.close()
