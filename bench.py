@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--ndomains", type=int, default=1000, help="c5: domains in the batch")
     ap.add_argument("--nreals", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 path measurement")
     ap.add_argument("--no-e2e", action="store_true")
@@ -304,6 +305,182 @@ def time_e2e(wl, args, torch, ws, steps, sweep=None):
     return dt, infs[-1], float(out[0, :8].sum())
 
 
+# ------------------------------------------------------- batch of domains
+def time_batch(bw, args, torch, ws, precision):
+    """Device-resident steps of a batch: prepare (graph: search, levels,
+    order, bins, solves) + seeded sweep (graph) into a device array."""
+    import geosgs
+
+    probs = []
+    for w in bw.items:
+        w.method.precision = precision
+        probs.append(geosgs.build_problem(w.process, w.domain, w.data, w.method))
+    t0 = time.perf_counter()
+    B = geosgs.Batch(probs)
+    t_create = time.perf_counter() - t0
+    R = bw.nreals
+    Rp = (R + 3) // 4 * 4
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    B.prepare()
+    V = torch.empty(B.nnodes * Rp, dtype=dt, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    if args.sweep_config:
+        B.set_sweep(**json.loads(args.sweep_config))
+        cfg, tried = json.loads(args.sweep_config), []
+    else:
+        cfg, tried = B.tune_sweep(R)
+
+    def step(i):
+        B.prepare()
+        B.simulate_device(R, 1000 + i, V.data_ptr(), stream)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    launches0, graphs0 = B.info().launches, B.info().graph_launches
+    ph = {"search": [], "levels": [], "solve": [], "sweep": []}
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.steps):
+        step(args.warmup + i)
+        inf = B.info()
+        ph["search"].append(inf.ms_search)
+        ph["levels"].append(inf.ms_levels)
+        ph["solve"].append(inf.ms_solve)
+        ph["sweep"].append(inf.ms_sweep)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1) / args.steps
+    inf = B.info()
+    res = dict(ms=max_over_ranks(ws, ms), launches=inf.launches - launches0, graphs=inf.graph_launches - graphs0,
+               info=inf, sweep_config=cfg, sweep_tried=tried, s_create=t_create,
+               phases={k: statistics.mean(v) for k, v in ph.items()})
+    B.close()
+    del V
+    torch.cuda.empty_cache()
+    return res, probs
+
+
+def cpu_sample_batch(bw, budget_nodes: int):
+    """FP64 oracle on the first domains of the batch (whole domains, up to
+    about budget_nodes nodes): nodes*reals/s over the sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import geosgs
+    import oracle
+
+    oracle.build()
+    nodes, secs, used = 0, 0.0, 0
+    for w in bw.items:
+        n = w.domain.nelements()
+        if used and nodes + n > budget_nodes:
+            continue
+        w.method.precision = "fp64"
+        p, keep = geosgs.build_problem(w.process, w.domain, w.data, w.method)
+        O = oracle.OraclePlan(p, keep)
+        t0 = time.perf_counter()
+        O.prepare()
+        O.simulate(bw.nreals, None, seed=1)
+        secs += time.perf_counter() - t0
+        nodes += n
+        used += 1
+        if nodes >= budget_nodes:
+            break
+    cores = os.cpu_count()
+    sample = (f"oracle FP64 on {used} whole domains of {bw.name} ({nodes} nodes x {bw.nreals} realizations: "
+              f"search, solve and draw loop); {cores} threads")
+    return nodes * bw.nreals / secs, cores, sample
+
+
+def main_batch(args, torch, ws, rank, uuid):
+    from geosgs import workloads
+
+    bw = workloads.c5("fp32", nreals=args.nreals or 8, ndomains=args.ndomains)
+    N, R = bw.nodes(), bw.nreals
+    clocks = ClockSampler(uuid).start()
+    fast, probs = time_batch(bw, args, torch, ws, "fp32")
+    clk = clocks.stop()
+    fp64 = None
+    if not args.no_fp64:
+        a64 = argparse.Namespace(**vars(args))
+        a64.steps = max(2, args.steps // 2)
+        a64.warmup = max(1, min(args.warmup, 2))
+        fp64, _ = time_batch(workloads.c5("fp64", nreals=R, ndomains=args.ndomains), a64, torch, ws, "fp64")
+    e2e = None
+    if not args.no_e2e and N * R * 8 <= (8 << 30):
+        import geosgs
+
+        out = torch.empty(N * R, dtype=torch.float64, pin_memory=True).numpy()
+        import ctypes as C
+
+        def e2e_step(i):
+            B = geosgs.Batch(probs)
+            B.prepare()
+            B._check(B.lib.sgs_batch_simulate(B.h, R, None, 77 + i, out.ctypes.data_as(C.POINTER(C.c_double))))
+            inf = B.info()
+            B.close()
+            return inf
+
+        e2e_step(0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        k = max(1, min(3, args.steps))
+        infs = [e2e_step(1 + i) for i in range(k)]
+        dt = (time.perf_counter() - t0) / k
+        e2e = {"value": ws * N * R / dt, "unit": UNIT, "h2d_bytes_per_step": int(infs[-1].h2d_bytes),
+               "d2h_bytes_per_step": int(infs[-1].d2h_bytes), "ms_per_step": 1e3 * dt,
+               "path": "sgs_batch_create + sgs_batch_prepare + sgs_batch_simulate (FP64 out to pinned host) + "
+                       "sgs_batch_destroy"}
+    if rank != 0:
+        return
+    inf = fast["info"]
+    sum_m = int(inf.sum_grid_neighbors)
+    Rp = (R + 3) // 4 * 4
+    # neighbour row reads + value writes (rows of Rp values), and per grid
+    # neighbour an int32 index and a (hi, lo) weight, per node its id, count,
+    # CSR row start, (hi, lo) b0 and sigma
+    alg_bytes = (sum_m + N) * Rp * 4 + sum_m * 12 + N * 32
+    try:
+        peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except Exception:
+        peak, peak_src = 6800.0, "fallback"
+    ms_sweep = fast["phases"]["sweep"]
+    achieved = alg_bytes / (ms_sweep * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        v, cores, sample = cpu_sample_batch(bw, args.cpu_nodes * 4)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    value = ws * N * R / (fast["ms"] * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG64 domains, variograms, data and paths; on-device Philox normals)",
+        "config": {"workload": bw.name, "ndomains": len(bw.items), "nodes": N, "nreals": R,
+                   "ndata": int(inf.ndata), "precision": "FP32 LHS+Cholesky, FP64 refinement residual and variance",
+                   "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (sweep tables %.1f GB)" % ((sum_m * 12 + N * 32) / 1e9)},
+        "phases_ms": fast["phases"], "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior),
+        "n_fp64_fallback": int(inf.n_fp64_fallback), "bin_systems": [int(x) for x in inf.bin_systems],
+        "device_gb": inf.device_bytes / 1e9, "s_create": round(fast["s_create"], 2),
+        "roofline": {"kernel": "sweep_flow_kernel<float, CSR> (one persistent dataflow launch)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None, "algorithmic_bytes": alg_bytes, "ms": ms_sweep},
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(fast["launches"]) // max(1, args.steps),
+        "graph_launches_per_step": fast["graphs"] / max(1, args.steps), "clocks": clk,
+        "sweep_config": fast["sweep_config"],
+        "sweep_candidates_ms": [round(t["ms"], 3) for t in fast["sweep_tried"]],
+    }
+    if fp64:
+        v64 = ws * N * R / (fp64["ms"] * 1e-3)
+        out["fp64_path"] = {"value": v64, "ms_per_step": fp64["ms"], "phases_ms": fp64["phases"]}
+        out["speedup_vs_fp64_path"] = value / v64
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -323,6 +500,9 @@ def main():
     except Exception:
         uuid = None
 
+    if args.workload == "c5":
+        main_batch(args, torch, ws, rank, uuid)
+        return
     wl = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
     N, R = wl.domain.nelements(), wl.nreals
 

@@ -230,56 +230,231 @@ extern "C" void sgs_plan_destroy(sgs_plan* p) {
     delete p;
 }
 
-static int plan_init(sgs_plan* P, const sgs_problem* pr) {
+// Host-side set-up of one problem: validation (argument errors as the
+// reference's ArgumentError / @assert), the neighbourhood metric, the path
+// and its ranks, the sorted offset template and the data buckets.  Shared by
+// plans and batches of domains.
+int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
+#define HERR(msg)              \
+    do {                       \
+        err = (msg);           \
+        return SGS_ERR_ARG;    \
+    } while (0)
     const int dim = pr->dim;
-    if (dim != 2 && dim != 3) return set_err(P, SGS_ERR_ARG, "dim must be 2 or 3");
-    GridDev& G = P->grid;
+    if (dim != 2 && dim != 3) HERR("dim must be 2 or 3");
+    GridDev& G = H.grid;
     G.dim = dim;
     G.N = 1;
     for (int j = 0; j < 3; ++j) {
         G.n[j] = j < dim ? pr->dims[j] : 1;
         G.origin[j] = j < dim ? pr->origin[j] : 0.0;
         G.spacing[j] = j < dim ? pr->spacing[j] : 1.0;
-        if (G.n[j] < 1) return set_err(P, SGS_ERR_ARG, "grid dims must be >= 1");
+        if (G.n[j] < 1) HERR("grid dims must be >= 1");
         if (!(G.spacing[j] > 0.0) || !std::isfinite(G.spacing[j]) || !std::isfinite(G.origin[j]))
-            return set_err(P, SGS_ERR_ARG, "spacing must be finite and > 0");
+            HERR("spacing must be finite and > 0");
         G.N *= G.n[j];
     }
-    if (G.N > (int64_t)INT32_MAX / 2) return set_err(P, SGS_ERR_ARG, "grid too large (N must be < 2^30)");
-    P->N = G.N;
-    P->D = pr->ndata;
-    if (P->D < 0 || (P->D > 0 && (!pr->data_coords || !pr->data_values)))
-        return set_err(P, SGS_ERR_ARG, "invalid data arrays");
-    if (P->N + P->D > (int64_t)INT32_MAX) return set_err(P, SGS_ERR_ARG, "too many points");
-    for (int64_t i = 0; i < P->D * dim; ++i)
-        if (!std::isfinite(pr->data_coords[i])) return set_err(P, SGS_ERR_ARG, "data coordinates must be finite");
-    for (int64_t i = 0; i < P->D; ++i)
-        if (!std::isfinite(pr->data_values[i])) return set_err(P, SGS_ERR_ARG, "data values must be finite");
+    if (G.N > (int64_t)INT32_MAX / 2) HERR("grid too large (N must be < 2^30)");
+    H.N = G.N;
+    H.D = pr->ndata;
+    if (H.D < 0 || (H.D > 0 && (!pr->data_coords || !pr->data_values))) HERR("invalid data arrays");
+    if (H.N + H.D > (int64_t)INT32_MAX) HERR("too many points");
+    for (int64_t i = 0; i < H.D * dim; ++i)
+        if (!std::isfinite(pr->data_coords[i])) HERR("data coordinates must be finite");
+    for (int64_t i = 0; i < H.D; ++i)
+        if (!std::isfinite(pr->data_values[i])) HERR("data values must be finite");
     const sgs_variogram& v = pr->variogram;
-    if (v.type < SGS_SPHERICAL || v.type > SGS_GAUSSIAN) return set_err(P, SGS_ERR_ARG, "unknown variogram type");
+    if (v.type < SGS_SPHERICAL || v.type > SGS_GAUSSIAN) HERR("unknown variogram type");
     if (!(v.sill > 0.0) || !(v.nugget >= 0.0) || v.nugget > v.sill || !std::isfinite(v.sill))
-        return set_err(P, SGS_ERR_ARG, "invalid sill/nugget");
+        HERR("invalid sill/nugget");
     for (int j = 0; j < dim; ++j)
-        if (!(v.ranges[j] > 0.0) || !std::isfinite(v.ranges[j])) return set_err(P, SGS_ERR_ARG, "ranges must be finite and > 0");
-    if (!std::isfinite(pr->mean)) return set_err(P, SGS_ERR_ARG, "mean must be finite");
-    P->vario.type = v.type;
-    P->vario.sill = v.sill;
-    P->vario.nugget = v.nugget;
-    for (int j = 0; j < 3; ++j) P->vario.inv_range[j] = j < dim ? 1.0 / v.ranges[j] : 1.0;
-    for (int j = 0; j < 9; ++j) P->vario.R[j] = v.rotation[j];
-    P->mean = pr->mean;
+        if (!(v.ranges[j] > 0.0) || !std::isfinite(v.ranges[j])) HERR("ranges must be finite and > 0");
+    if (!std::isfinite(pr->mean)) HERR("mean must be finite");
+    H.vario.type = v.type;
+    H.vario.sill = v.sill;
+    H.vario.nugget = v.nugget;
+    for (int j = 0; j < 3; ++j) H.vario.inv_range[j] = j < dim ? 1.0 / v.ranges[j] : 1.0;
+    for (int j = 0; j < 9; ++j) H.vario.R[j] = v.rotation[j];
+    H.mean = pr->mean;
 
     // seqsim.jl:202-208
     int64_t nmax = pr->maxneighbors, nmin = pr->minneighbors;
-    if (nmax > P->N || nmax < 1) nmax = P->N;
+    if (nmax > H.N || nmax < 1) nmax = H.N;
     if (nmin > nmax || nmin < 1) nmin = 1;
-    if (nmax > KMAX) return set_err(P, SGS_ERR_ARG, "maxneighbors above 64 is not supported on the GPU");
-    P->k = (int)nmax;
-    P->nmin = (int)nmin;
-    if (pr->precision != SGS_PREC_FP64 && pr->precision != SGS_PREC_FP32_REFINE)
-        return set_err(P, SGS_ERR_ARG, "unknown precision");
+    if (nmax > KMAX) HERR("maxneighbors above 64 is not supported on the GPU");
+    H.k = (int)nmax;
+    H.nmin = (int)nmin;
+    if (pr->precision != SGS_PREC_FP64 && pr->precision != SGS_PREC_FP32_REFINE) HERR("unknown precision");
+    if (pr->refine_steps < 0 || pr->refine_steps > 4) HERR("refine_steps must be in 0..4");
+
+    // neighbourhood: seqsim.jl:171-177,221-227
+    static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (pr->search == SGS_SEARCH_RANGE) {
+        double rmax = v.ranges[0];
+        for (int j = 1; j < dim; ++j) rmax = std::max(rmax, v.ranges[j]);
+        double r[3] = {rmax, rmax, rmax};
+        set_metric(H.metric, dim, METRIC_ISO, r, I9);
+    } else if (pr->search == SGS_SEARCH_BALL) {
+        for (int j = 0; j < dim; ++j)
+            if (!(pr->ball.radii[j] > 0.0) || !std::isfinite(pr->ball.radii[j]))
+                HERR("ball radii must be finite and > 0");
+        bool iso = is_identity(pr->ball.rotation, dim);
+        for (int j = 1; j < dim; ++j) iso = iso && pr->ball.radii[j] == pr->ball.radii[0];
+        set_metric(H.metric, dim, iso ? METRIC_ISO : METRIC_ELLIPSOID, pr->ball.radii, pr->ball.rotation);
+    } else if (pr->search == SGS_SEARCH_NEAREST) {
+        double r[3] = {1, 1, 1};
+        set_metric(H.metric, dim, METRIC_NEAREST, r, I9);
+    } else {
+        HERR("unknown search kind");
+    }
+
+    // path and ranks
+    H.path.resize(H.N);
+    H.rank.assign(H.N, -1);
+    for (int64_t t = 0; t < H.N; ++t) {
+        const int64_t g = pr->path ? pr->path[t] : t;
+        if (g < 0 || g >= H.N || H.rank[g] != -1) HERR("path is not a permutation of the grid nodes");
+        H.path[t] = (int32_t)g;
+        H.rank[g] = (int32_t)t;
+    }
+
+    // template: cell offsets inside the neighbourhood in canonical order
+    int64_t e[3] = {0, 0, 0};
+    int64_t cells = 1;
+    for (int j = 0; j < dim; ++j) {
+        if (H.metric.kind == METRIC_NEAREST) e[j] = G.n[j] - 1;
+        else e[j] = std::min<int64_t>(G.n[j] - 1, (int64_t)std::floor(H.metric.ext[j] / G.spacing[j]) + 1);
+        cells *= 2 * e[j] + 1;
+    }
+    if (cells > (int64_t)1 << 28) HERR("search neighbourhood spans too many cells");
+    struct Ent { double d2; int64_t lin; TmplEntry e; };
+    std::vector<Ent> ents;
+    for (int64_t c = -e[2]; c <= e[2]; ++c)
+        for (int64_t b = -e[1]; b <= e[1]; ++b)
+            for (int64_t a = -e[0]; a <= e[0]; ++a) {
+                if (a == 0 && b == 0 && c == 0) continue;
+                double h[3] = {(double)a * G.spacing[0], (double)b * G.spacing[1], dim == 3 ? (double)c * G.spacing[2] : 0.0};
+                double d = host_d2(H.metric, dim, h);
+                if (!host_inside(H.metric, d)) continue;
+                int64_t lin = a + (int64_t)G.n[0] * (b + (int64_t)G.n[1] * c);
+                ents.push_back({d, lin, TmplEntry{(int)a, (int)b, (int)c, (int)lin}});
+            }
+    std::sort(ents.begin(), ents.end(), [](const Ent& x, const Ent& y) {
+        return x.d2 < y.d2 || (x.d2 == y.d2 && x.lin < y.lin);
+    });
+    H.tmpl.resize(ents.size());
+    H.tmpl_d2.resize(ents.size());
+    for (size_t i = 0; i < ents.size(); ++i) {
+        H.tmpl[i] = ents[i].e;
+        H.tmpl_d2[i] = ents[i].d2;
+        H.tmpl_ext[0] = std::max(H.tmpl_ext[0], std::abs(ents[i].e.dx));
+        H.tmpl_ext[1] = std::max(H.tmpl_ext[1], std::abs(ents[i].e.dy));
+        H.tmpl_ext[2] = std::max(H.tmpl_ext[2], std::abs(ents[i].e.dz));
+    }
+
+    // data: id order (solve) and bucket order (search)
+    H.xyz.assign((size_t)H.D * 3, 0.0);
+    H.val.resize(H.D);
+    for (int64_t i = 0; i < H.D; ++i) {
+        for (int j = 0; j < dim; ++j) H.xyz[i * 3 + j] = pr->data_coords[i * dim + j];
+        H.val[i] = pr->data_values[i];
+    }
+    const int B = 8;
+    int64_t nbk = 1;
+    for (int j = 0; j < 3; ++j) {
+        H.nb[j] = (G.n[j] + B - 1) / B;
+        H.bw[j] = G.spacing[j] * (double)B;
+        nbk *= H.nb[j];
+    }
+    std::vector<int64_t> bid(H.D);
+    H.bstart.assign(nbk + 1, 0);
+    for (int64_t i = 0; i < H.D; ++i) {
+        int64_t bc[3] = {0, 0, 0};
+        for (int j = 0; j < dim; ++j) {
+            double f = std::floor((H.xyz[i * 3 + j] - G.origin[j]) / H.bw[j]);
+            f = std::max(0.0, std::min(f, (double)(H.nb[j] - 1)));
+            bc[j] = (int64_t)f;
+        }
+        bid[i] = bc[0] + H.nb[0] * (bc[1] + H.nb[1] * bc[2]);
+        H.bstart[bid[i] + 1]++;
+    }
+    for (int64_t b = 0; b < nbk; ++b) H.bstart[b + 1] += H.bstart[b];
+    H.xyz_b.resize((size_t)H.D * 3);
+    H.did.resize(H.D);
+    {
+        std::vector<int32_t> cur(H.bstart.begin(), H.bstart.end() - 1);
+        for (int64_t i = 0; i < H.D; ++i) {
+            const int32_t q = cur[bid[i]]++;
+            H.did[q] = (int32_t)i;
+            for (int j = 0; j < 3; ++j) H.xyz_b[(size_t)q * 3 + j] = H.xyz[i * 3 + j];
+        }
+    }
+    // FP32 copies relative to the grid origin for the search's screen, and a
+    // bound that covers their rounding: lags are off by at most dh per axis
+    {
+        H.xf.resize(H.D);
+        double amax = 0.0;
+        for (int j = 0; j < dim; ++j) amax = std::max(amax, (double)G.n[j] * G.spacing[j]);
+        for (int64_t i = 0; i < H.D; ++i) {
+            double r[3] = {0, 0, 0};
+            for (int j = 0; j < dim; ++j) {
+                r[j] = H.xyz_b[(size_t)i * 3 + j] - G.origin[j];
+                amax = std::max(amax, std::fabs(r[j]));
+            }
+            H.xf[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
+        }
+        const double dh = 4.0 * amax * std::ldexp(1.0, -24) + 1e-30;
+        MetricDev& m = H.metric;
+        double slack = 0.0;
+        if (m.kind == METRIC_ISO) {
+            const double r = std::sqrt(m.rr);
+            slack = 2.0 * r * dh * std::sqrt((double)dim) + dim * dh * dh;
+        } else if (m.kind == METRIC_ELLIPSOID) {
+            for (int j = 0; j < dim; ++j) {
+                double dq = 0.0;
+                for (int i = 0; i < dim; ++i) dq += std::fabs(m.R[i + 3 * j]);
+                dq *= dh * m.inv[j];
+                slack += 2.02 * dq + dq * dq;
+            }
+        }
+        m.bound_f = (float)((m.kind == METRIC_ISO ? m.rr : 1.0) * (1.0 + 1e-3) + slack);
+    }
+    return SGS_OK;
+#undef HERR
+}
+
+// Search arguments of a domain whose device arrays are set by the caller.
+void sgs::search_args_of(const HostDomain& H, SearchArgs& sa) {
+    sa.grid = H.grid;
+    sa.metric = H.metric;
+    sa.k = H.k;
+    sa.T = (int)H.tmpl.size();
+    sa.D = H.D;
+    for (int j = 0; j < 3; ++j) {
+        sa.nb[j] = H.nb[j];
+        sa.bw[j] = H.bw[j];
+        sa.inv_bw_f[j] = (float)(1.0 / H.bw[j]);
+        sa.ext_f[j] = (float)H.metric.ext[j];
+        sa.spacing_f[j] = (float)H.grid.spacing[j];
+    }
+}
+
+static int plan_init(sgs_plan* P, const sgs_problem* pr) {
+    HostDomain H;
+    {
+        std::string err;
+        const int rc = host_domain(pr, H, err);
+        if (rc != SGS_OK) return set_err(P, rc, err);
+    }
+    P->grid = H.grid;
+    P->metric = H.metric;
+    P->vario = H.vario;
+    P->mean = H.mean;
+    P->N = H.N;
+    P->D = H.D;
+    P->k = H.k;
+    P->nmin = H.nmin;
     P->precision = pr->precision;
-    if (pr->refine_steps < 0 || pr->refine_steps > 4) return set_err(P, SGS_ERR_ARG, "refine_steps must be in 0..4");
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
     if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32))
@@ -290,70 +465,13 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     P->sweep.mode = (pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) ? SGS_SWEEP_COOPERATIVE
                     : (pr->flags & SGS_FLAG_LEVEL_SWEEP)   ? SGS_SWEEP_LEVELS
                                                            : SGS_SWEEP_FLOW;
-
-    // neighbourhood: seqsim.jl:171-177,221-227
-    static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    if (pr->search == SGS_SEARCH_RANGE) {
-        double rmax = v.ranges[0];
-        for (int j = 1; j < dim; ++j) rmax = std::max(rmax, v.ranges[j]);
-        double r[3] = {rmax, rmax, rmax};
-        set_metric(P->metric, dim, METRIC_ISO, r, I9);
-    } else if (pr->search == SGS_SEARCH_BALL) {
-        for (int j = 0; j < dim; ++j)
-            if (!(pr->ball.radii[j] > 0.0) || !std::isfinite(pr->ball.radii[j]))
-                return set_err(P, SGS_ERR_ARG, "ball radii must be finite and > 0");
-        bool iso = is_identity(pr->ball.rotation, dim);
-        for (int j = 1; j < dim; ++j) iso = iso && pr->ball.radii[j] == pr->ball.radii[0];
-        set_metric(P->metric, dim, iso ? METRIC_ISO : METRIC_ELLIPSOID, pr->ball.radii, pr->ball.rotation);
-    } else if (pr->search == SGS_SEARCH_NEAREST) {
-        double r[3] = {1, 1, 1};
-        set_metric(P->metric, dim, METRIC_NEAREST, r, I9);
-    } else {
-        return set_err(P, SGS_ERR_ARG, "unknown search kind");
-    }
-
-    // path and ranks
-    P->h_path.resize(P->N);
-    std::vector<int32_t> rank(P->N, -1);
-    for (int64_t t = 0; t < P->N; ++t) {
-        const int64_t g = pr->path ? pr->path[t] : t;
-        if (g < 0 || g >= P->N || rank[g] != -1) return set_err(P, SGS_ERR_ARG, "path is not a permutation of the grid nodes");
-        P->h_path[t] = (int32_t)g;
-        rank[g] = (int32_t)t;
-    }
-
-    // template: cell offsets inside the neighbourhood in canonical order
-    int64_t e[3] = {0, 0, 0};
-    int64_t cells = 1;
-    for (int j = 0; j < dim; ++j) {
-        if (P->metric.kind == METRIC_NEAREST) e[j] = G.n[j] - 1;
-        else e[j] = std::min<int64_t>(G.n[j] - 1, (int64_t)std::floor(P->metric.ext[j] / G.spacing[j]) + 1);
-        cells *= 2 * e[j] + 1;
-    }
-    if (cells > (int64_t)1 << 28) return set_err(P, SGS_ERR_ARG, "search neighbourhood spans too many cells");
-    struct Ent { double d2; int64_t lin; TmplEntry e; };
-    std::vector<Ent> ents;
-    for (int64_t c = -e[2]; c <= e[2]; ++c)
-        for (int64_t b = -e[1]; b <= e[1]; ++b)
-            for (int64_t a = -e[0]; a <= e[0]; ++a) {
-                if (a == 0 && b == 0 && c == 0) continue;
-                double h[3] = {(double)a * G.spacing[0], (double)b * G.spacing[1], dim == 3 ? (double)c * G.spacing[2] : 0.0};
-                double d = host_d2(P->metric, dim, h);
-                if (!host_inside(P->metric, d)) continue;
-                int64_t lin = a + (int64_t)G.n[0] * (b + (int64_t)G.n[1] * c);
-                ents.push_back({d, lin, TmplEntry{(int)a, (int)b, (int)c, (int)lin}});
-            }
-    std::sort(ents.begin(), ents.end(), [](const Ent& x, const Ent& y) {
-        return x.d2 < y.d2 || (x.d2 == y.d2 && x.lin < y.lin);
-    });
-    P->h_tmpl.resize(ents.size());
-    P->h_tmpl_d2.resize(ents.size());
-    for (size_t i = 0; i < ents.size(); ++i) {
-        P->h_tmpl[i] = ents[i].e;
-        P->h_tmpl_d2[i] = ents[i].d2;
-        P->tmpl_ext[0] = std::max(P->tmpl_ext[0], std::abs(ents[i].e.dx));
-        P->tmpl_ext[1] = std::max(P->tmpl_ext[1], std::abs(ents[i].e.dy));
-        P->tmpl_ext[2] = std::max(P->tmpl_ext[2], std::abs(ents[i].e.dz));
+    P->h_path = H.path;
+    P->h_tmpl = H.tmpl;
+    P->h_tmpl_d2 = H.tmpl_d2;
+    for (int j = 0; j < 3; ++j) {
+        P->tmpl_ext[j] = H.tmpl_ext[j];
+        P->nb[j] = H.nb[j];
+        P->bw[j] = H.bw[j];
     }
 
     // device
@@ -371,82 +489,15 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
 
     int rc;
     if ((rc = upload(P, &P->d_path, P->h_path.data(), P->N))) return rc;
-    if ((rc = upload(P, &P->d_rank, rank.data(), P->N))) return rc;
+    if ((rc = upload(P, &P->d_rank, H.rank.data(), P->N))) return rc;
     if ((rc = upload(P, &P->d_tmpl, P->h_tmpl.data(), P->h_tmpl.size()))) return rc;
     if ((rc = upload(P, &P->d_tmpl_d2, P->h_tmpl_d2.data(), P->h_tmpl_d2.size()))) return rc;
-
-    // data: id order (solve) and bucket order (search)
-    std::vector<double> xyz((size_t)P->D * 3, 0.0), val(P->D);
-    for (int64_t i = 0; i < P->D; ++i) {
-        for (int j = 0; j < dim; ++j) xyz[i * 3 + j] = pr->data_coords[i * dim + j];
-        val[i] = pr->data_values[i];
-    }
-    const int B = 8;
-    int64_t nbk = 1;
-    for (int j = 0; j < 3; ++j) {
-        P->nb[j] = (G.n[j] + B - 1) / B;
-        P->bw[j] = G.spacing[j] * (double)B;
-        nbk *= P->nb[j];
-    }
-    std::vector<int64_t> bid(P->D);
-    std::vector<int32_t> bstart(nbk + 1, 0);
-    for (int64_t i = 0; i < P->D; ++i) {
-        int64_t bc[3] = {0, 0, 0};
-        for (int j = 0; j < dim; ++j) {
-            double f = std::floor((xyz[i * 3 + j] - G.origin[j]) / P->bw[j]);
-            f = std::max(0.0, std::min(f, (double)(P->nb[j] - 1)));
-            bc[j] = (int64_t)f;
-        }
-        bid[i] = bc[0] + P->nb[0] * (bc[1] + P->nb[1] * bc[2]);
-        bstart[bid[i] + 1]++;
-    }
-    for (int64_t b = 0; b < nbk; ++b) bstart[b + 1] += bstart[b];
-    std::vector<double> xyz_b((size_t)P->D * 3);
-    std::vector<int32_t> did(P->D);
-    {
-        std::vector<int32_t> cur(bstart.begin(), bstart.end() - 1);
-        for (int64_t i = 0; i < P->D; ++i) {
-            const int32_t q = cur[bid[i]]++;
-            did[q] = (int32_t)i;
-            for (int j = 0; j < 3; ++j) xyz_b[(size_t)q * 3 + j] = xyz[i * 3 + j];
-        }
-    }
-    if ((rc = upload(P, &P->d_dxyz, xyz.data(), xyz.size()))) return rc;
-    if ((rc = upload(P, &P->d_dval, val.data(), val.size()))) return rc;
-    if ((rc = upload(P, &P->d_dxyz_b, xyz_b.data(), xyz_b.size()))) return rc;
-    if ((rc = upload(P, &P->d_did, did.data(), did.size()))) return rc;
-    if ((rc = upload(P, &P->d_bstart, bstart.data(), bstart.size()))) return rc;
-    // FP32 copies relative to the grid origin for the search's screen, and a
-    // bound that covers their rounding: lags are off by at most dh per axis
-    {
-        std::vector<float4> xf(P->D);
-        double amax = 0.0;
-        for (int j = 0; j < dim; ++j) amax = std::max(amax, (double)G.n[j] * G.spacing[j]);
-        for (int64_t i = 0; i < P->D; ++i) {
-            double r[3] = {0, 0, 0};
-            for (int j = 0; j < dim; ++j) {
-                r[j] = xyz_b[(size_t)i * 3 + j] - G.origin[j];
-                amax = std::max(amax, std::fabs(r[j]));
-            }
-            xf[i] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.0f);
-        }
-        if ((rc = upload(P, &P->d_dxyz_f, xf.data(), xf.size()))) return rc;
-        const double dh = 4.0 * amax * std::ldexp(1.0, -24) + 1e-30;
-        MetricDev& m = P->metric;
-        double slack = 0.0;
-        if (m.kind == METRIC_ISO) {
-            const double r = std::sqrt(m.rr);
-            slack = 2.0 * r * dh * std::sqrt((double)dim) + dim * dh * dh;
-        } else if (m.kind == METRIC_ELLIPSOID) {
-            for (int j = 0; j < dim; ++j) {
-                double dq = 0.0;
-                for (int i = 0; i < dim; ++i) dq += std::fabs(m.R[i + 3 * j]);
-                dq *= dh * m.inv[j];
-                slack += 2.02 * dq + dq * dq;
-            }
-        }
-        m.bound_f = (float)((m.kind == METRIC_ISO ? m.rr : 1.0) * (1.0 + 1e-3) + slack);
-    }
+    if ((rc = upload(P, &P->d_dxyz, H.xyz.data(), H.xyz.size()))) return rc;
+    if ((rc = upload(P, &P->d_dval, H.val.data(), H.val.size()))) return rc;
+    if ((rc = upload(P, &P->d_dxyz_b, H.xyz_b.data(), H.xyz_b.size()))) return rc;
+    if ((rc = upload(P, &P->d_did, H.did.data(), H.did.size()))) return rc;
+    if ((rc = upload(P, &P->d_bstart, H.bstart.data(), H.bstart.size()))) return rc;
+    if ((rc = upload(P, &P->d_dxyz_f, H.xf.data(), H.xf.size()))) return rc;
     CK(P, cudaStreamSynchronize(P->stream));
 
     P->info.nnodes = P->N;

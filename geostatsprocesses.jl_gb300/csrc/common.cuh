@@ -225,4 +225,34 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+// ---- batches of domains: global numbering and per-domain descriptors ----
+// Domain d owns the global ids [off[d], off[d+1]); returns d for id x
+// (0 <= x < off[nd]) by binary search over the nd + 1 offsets.
+__device__ __forceinline__ int find_domain(const int64_t* __restrict__ off, int nd, int64_t x) {
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Copy a descriptor (a plain struct, 4-byte multiple) from global into this
+// warp's shared-memory slot, all lanes cooperating; the caller __syncwarp()s.
+template <typename T>
+__device__ __forceinline__ void warp_copy_struct(T* dst, const T* src, int lane) {
+    static_assert(sizeof(T) % 4 == 0, "descriptor size");
+    int* d = reinterpret_cast<int*>(dst);
+    const int* s = reinterpret_cast<const int*>(src);
+    for (int i = lane; i < (int)(sizeof(T) / 4); i += 32) d[i] = __ldg(s + i);
+}
+
+// First table entry of sweep-table row `pos`: rows of k entries, or CSR
+// offsets when the tables are packed (batches of domains with different k).
+template <typename T>
+__device__ __forceinline__ int64_t table_row(const SweepTables<T>& t, int64_t pos, int k) {
+    return t.off ? t.off[pos] : pos * (int64_t)k;
+}
+
 }  // namespace sgs

@@ -5,7 +5,10 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
+
+#include "../../include/geosgs.h"
 
 namespace sgs {
 
@@ -108,6 +111,8 @@ struct SweepTables {
     T* w;                        // P x k x S weights of those
     T* b0;                       // P x S: data term sum_i w_i (d_i - mu)
     T* sigma;                    // P x S: conditional std (sqrt(sill) for the prior)
+    const int64_t* off;          // nullptr: row p starts at p * k; else CSR row starts
+                                 // (P + 1), used by batches of domains
 };
 
 // Dataflow sweep state: warps take items (position in level order x piece of
@@ -127,6 +132,8 @@ struct FlowArgs {
     int blocks_per_sm;           // resident blocks per SM to launch (<= occupancy)
     int tight;                   // 1: kernel compiled for higher residency (register cap)
     uint64_t wait_ns;            // longest wait for one flag before giving up
+    const uint64_t* seed_dev;    // nullptr, or the draw seed in device memory (read at
+                                 // launch; lets a captured graph take a new seed)
 };
 
 struct SolveArgs {
@@ -155,7 +162,34 @@ struct SolveArgs {
     unsigned long long* sum_m;   // accumulates the grid neighbours written to the tables
     const float* w_init;         // optional node-indexed [N][k] warm-start weights (FP32 path)
     unsigned long long* n_warm;  // counts systems accepted from the warm start
+    int64_t node0;               // added to node ids written to the sweep tables (the
+                                 // domain's first global id in a batch; 0 for a plan)
 };
+
+// Host-side description of one problem (api.cu: host_domain): everything
+// sgs_plan_create derives on the host before uploading.
+struct HostDomain {
+    GridDev grid{};
+    MetricDev metric{};
+    VarioDev vario{};
+    double mean = 0.0;
+    int k = 0, nmin = 1;
+    int64_t N = 0, D = 0;
+    std::vector<int32_t> path, rank;      // path rank -> node, node -> path rank
+    std::vector<TmplEntry> tmpl;          // offsets sorted by (d2, linear offset)
+    std::vector<double> tmpl_d2;
+    int tmpl_ext[3] = {0, 0, 0};          // largest |offset| per axis
+    std::vector<double> xyz, val;         // data, id order (xyz: D x 3)
+    std::vector<double> xyz_b;            // data, bucket order
+    std::vector<int32_t> did, bstart;     // data id per bucket entry; bucket starts
+    std::vector<float4> xf;               // FP32 origin-relative coordinates, bucket order
+    int nb[3] = {1, 1, 1};
+    double bw[3] = {1, 1, 1};
+};
+// Validates *pr and fills H; SGS_OK or SGS_ERR_ARG with err set.
+int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err);
+// The geometry fields of a domain's SearchArgs (device pointers left as they are).
+void search_args_of(const HostDomain& H, SearchArgs& sa);
 
 // Message returned by sgs_last_error(NULL) on this host thread.
 void set_thread_error(const char* msg);
@@ -169,6 +203,20 @@ cudaError_t launch_level_order(int64_t N, const int32_t* level, int nlevels, int
 cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, cudaStream_t s);
 cudaError_t launch_solve_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s);
 cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<float>& t, cudaStream_t s);
+// batches of domains (doms: device descriptors, noff: ndom + 1 global node
+// offsets, order: level-ordered global node ids; the positions to solve are
+// list[desc[1] .. desc[1] + desc[0]), desc on the device)
+cudaError_t launch_search_batch(const SearchArgs* doms, const int64_t* noff, int ndom, int64_t total, int nsm,
+                                cudaStream_t s);
+cudaError_t launch_solve_fp32_batch(int nmax, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                    const int32_t* order, const int32_t* list, const int32_t* desc,
+                                    const SweepTables<float>& t, int nsm, cudaStream_t s);
+cudaError_t launch_solve_fp64_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                    const int32_t* order, const int32_t* list, const int32_t* desc,
+                                    const SweepTables<double>& t, int nsm, cudaStream_t s);
+cudaError_t launch_solve_fp64_into_fp32_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                              const int32_t* order, const int32_t* list, const int32_t* desc,
+                                              const SweepTables<float>& t, int nsm, cudaStream_t s);
 cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp,
                               const float* z, uint64_t seed, float* V, cudaStream_t s);
 cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,

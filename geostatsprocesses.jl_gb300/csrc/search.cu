@@ -57,32 +57,27 @@ __device__ void warp_sort_pairs(long long* key, int32_t* idx, int n, int lane) {
     }
 }
 
-__global__ void __launch_bounds__(SEARCH_WARPS * 32)
-search_kernel(const SearchArgs a) {
-    __shared__ long long s_gd2[SEARCH_WARPS][KMAX];
-    __shared__ int32_t s_gidx[SEARCH_WARPS][KMAX];
-    __shared__ long long s_dd2[SEARCH_WARPS][DCAP];
-    __shared__ int32_t s_didx[SEARCH_WARPS][DCAP];
-    __shared__ int32_t s_squ[SEARCH_WARPS][64];  // screened data candidates
+// Per-warp shared-memory buffers of the search.
+struct SearchSmem {
+    long long* gd2;   // [KMAX] grid candidates' d2 keys
+    int32_t* gidx;    // [KMAX] their node ids
+    long long* dd2;   // [DCAP] data candidates' d2 keys
+    int32_t* didx;    // [DCAP] their augmented ids
+    int32_t* squ;     // [64] screened data candidates
+};
 
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    long long* gd2 = s_gd2[wib];
-    int32_t* gidx = s_gidx[wib];
-    long long* dd2 = s_dd2[wib];
+// The neighbour row of node g of the problem described by `a`.
+__device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane, const SearchSmem& sm) {
+    long long* gd2 = sm.gd2;
+    int32_t* gidx = sm.gidx;
+    long long* dd2 = sm.dd2;
     const long long* tkey = reinterpret_cast<const long long*>(a.tmpl_d2);
-    int32_t* didx = s_didx[wib];
-    int32_t* squ = s_squ[wib];
+    int32_t* didx = sm.didx;
+    int32_t* squ = sm.squ;
     const GridDev& G = a.grid;
     const int k = a.k;
     const unsigned lt = lanemask_lt();
-    const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
-
-    // Nodes go in id order, so the warps of a block take neighbouring cells
-    // and share the rank and data cache lines they scan; the result of a
-    // node depends only on its path rank, not on when it is processed.
-    for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < G.N; gg += nwarps) {
-        const int g = (int)gg;
+    {
         const int64_t t = a.rank[g];
         int i0, i1, i2;
         cell_of(G, g, i0, i1, i2);
@@ -248,6 +243,59 @@ search_kernel(const SearchArgs a) {
         }
         __syncwarp();
     }
+}
+
+#define SEARCH_SMEM_DECL                                                  \
+    __shared__ long long s_gd2[SEARCH_WARPS][KMAX];                       \
+    __shared__ int32_t s_gidx[SEARCH_WARPS][KMAX];                        \
+    __shared__ long long s_dd2[SEARCH_WARPS][DCAP];                       \
+    __shared__ int32_t s_didx[SEARCH_WARPS][DCAP];                        \
+    __shared__ int32_t s_squ[SEARCH_WARPS][64];                           \
+    const int lane = threadIdx.x & 31;                                    \
+    const int wib = threadIdx.x >> 5;                                     \
+    const SearchSmem sm{s_gd2[wib], s_gidx[wib], s_dd2[wib], s_didx[wib], s_squ[wib]}
+
+__global__ void __launch_bounds__(SEARCH_WARPS * 32) search_kernel(const SearchArgs a) {
+    SEARCH_SMEM_DECL;
+    const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
+    // Nodes go in id order, so the warps of a block take neighbouring cells
+    // and share the rank and data cache lines they scan; the result of a
+    // node depends only on its path rank, not on when it is processed.
+    for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < a.grid.N; gg += nwarps)
+        search_node(a, (int)gg, lane, sm);
+}
+
+// Every node of a batch of domains: global node ids [noff[d], noff[d+1])
+// belong to domain d, described by doms[d] (its own grid, metric, template,
+// data, path ranks and neighbour rows).  A warp copies its current domain's
+// descriptor to shared memory when it moves into another domain.
+__global__ void __launch_bounds__(SEARCH_WARPS * 32)
+search_batch_kernel(const SearchArgs* __restrict__ doms, const int64_t* __restrict__ noff, int ndom) {
+    SEARCH_SMEM_DECL;
+    __shared__ SearchArgs s_dom[SEARCH_WARPS];
+    const int64_t total = noff[ndom];
+    const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
+    int64_t lo = 0, hi = 0;
+    for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < total; gg += nwarps) {
+        if (gg < lo || gg >= hi) {
+            const int d = find_domain(noff, ndom, gg);
+            lo = noff[d];
+            hi = noff[d + 1];
+            __syncwarp();
+            warp_copy_struct(&s_dom[wib], &doms[d], lane);
+            __syncwarp();
+        }
+        search_node(s_dom[wib], (int)(gg - lo), lane, sm);
+    }
+}
+
+cudaError_t launch_search_batch(const SearchArgs* doms, const int64_t* noff, int ndom, int64_t total, int nsm,
+                                cudaStream_t s) {
+    int64_t want = (total + SEARCH_WARPS - 1) / SEARCH_WARPS;
+    int blocks = (int)(want < (int64_t)nsm * 8 ? want : (int64_t)nsm * 8);
+    if (blocks < 1) blocks = 1;
+    search_batch_kernel<<<blocks, SEARCH_WARPS * 32, 0, s>>>(doms, noff, ndom);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_search(const SearchArgs& a, cudaStream_t s) {

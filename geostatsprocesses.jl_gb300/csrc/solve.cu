@@ -155,6 +155,7 @@ template <typename O>
 __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t pos, int g, int n,
                           const NbInfo* info, const double* w, double sigma, int status, int lane) {
     const int k = a.k;
+    const int64_t row = table_row(tab, pos, k);
     int m = 0;
     double b0 = 0.0;
     if (status == SGS_NODE_KRIGED_) {
@@ -164,8 +165,8 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
             const unsigned b = __ballot_sync(FULL_MASK, isgrid);
             if (isgrid) {
                 const int j = m + __popc(b & lanemask_lt());
-                tab.idx[pos * k + j] = a.nbr[(int64_t)g * k + q];
-                put(tab.w, pos * k + j, w[q]);
+                tab.idx[row + j] = a.nbr[(int64_t)g * k + q] + (int32_t)a.node0;
+                put(tab.w, row + j, w[q]);
             } else if (q < n) {
                 b0 += w[q] * (a.data_val[info[q].did] - a.mu);
             }
@@ -175,7 +176,7 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
     }
     if (lane == 0) {
         if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
-        tab.node[pos] = g;
+        tab.node[pos] = g + (int32_t)a.node0;
         tab.m[pos] = m;
         put(tab.b0, pos, b0);
         put(tab.sigma, pos, sigma);
@@ -188,36 +189,27 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
     }
 }
 
-// The plain FP64 path (T = double): FP64 LHS, Cholesky and weights.  O is the
-// table type: double for the FP64 path, float (hi, lo pairs) when it re-solves
-// the systems the FP32 path queued.  With a.list set, solves only the queued
-// positions.
+// One system (node g, sweep-table row pos) of the problem `a`, in this warp's
+// shared-memory slot `base` laid out for up to kl neighbours (kl >= a.k, or
+// >= the node's neighbour count).
 template <typename T, typename O>
-__global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs a, const SweepTables<O> tab) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
+__device__ __forceinline__ void solve_system(const SolveArgs& a, const SweepTables<O>& tab, int64_t pos, int g,
+                                             unsigned char* base, int kl, int lane) {
     const int k = a.k;
-    const int ld = k + 1;
-    unsigned char* base = smem + (size_t)wib * warp_smem_bytes<T>(k);
+    const int ld = kl + 1;
     T* A = reinterpret_cast<T*>(base);
-    double* c = reinterpret_cast<double*>(base + ((size_t)k * ld * sizeof(T) + 15) / 16 * 16);
-    double* w = c + k;
-    T* rhs = reinterpret_cast<T*>(w + k);
-    NbInfo* info = reinterpret_cast<NbInfo*>(reinterpret_cast<unsigned char*>(rhs) + ((size_t)k * sizeof(T) + 15) / 16 * 16);
+    double* c = reinterpret_cast<double*>(base + ((size_t)kl * ld * sizeof(T) + 15) / 16 * 16);
+    double* w = c + kl;
+    T* rhs = reinterpret_cast<T*>(w + kl);
+    NbInfo* info = reinterpret_cast<NbInfo*>(reinterpret_cast<unsigned char*>(rhs) + ((size_t)kl * sizeof(T) + 15) / 16 * 16);
     const GridDev& G = a.grid;
     const double sill = a.vario.sill;
     const double prior_sd = sqrt(sill);
-
-    const int64_t count = a.list ? (int64_t)*a.nfallback : a.P;
-    const int64_t nwarps = (int64_t)gridDim.x * SOLVE_WARPS;
-    for (int64_t it = (int64_t)blockIdx.x * SOLVE_WARPS + wib; it < count; it += nwarps) {
-        const int64_t pos = a.list ? (int64_t)a.list[it] : it;
-        const int g = a.order[pos];
+    {
         const int n = a.cnt[g];
         if (n < a.nmin) {
             write_row<O>(a, tab, pos, g, n, info, w, prior_sd, SGS_NODE_PRIOR_NMIN_, lane);
-            continue;
+            return;
         }
         NbInfo self;
         cell_of(G, g, self.c0, self.c1, self.c2);
@@ -266,7 +258,7 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs
         }
         if (!ok) {
             write_row<O>(a, tab, pos, g, n, info, w, prior_sd, SGS_NODE_PRIOR_SINGULAR_, lane);
-            continue;
+            return;
         }
         double wc = 0.0;
         for (int q = lane; q < n; q += 32) wc += w[q] * c[q];
@@ -274,6 +266,57 @@ __global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs
         const double var = sill - wc;
         write_row<O>(a, tab, pos, g, n, info, w, sqrt(var > 0.0 ? var : 0.0), SGS_NODE_KRIGED_, lane);
         __syncwarp();
+    }
+}
+
+// The plain FP64 path (T = double): FP64 LHS, Cholesky and weights.  O is the
+// table type: double for the FP64 path, float (hi, lo pairs) when it re-solves
+// the systems the FP32 path queued.  With a.list set, solves only the queued
+// positions.
+template <typename T, typename O>
+__global__ void __launch_bounds__(SOLVE_WARPS * 32) solve_kernel(const SolveArgs a, const SweepTables<O> tab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * warp_smem_bytes<T>(a.k);
+    const int64_t count = a.list ? (int64_t)*a.nfallback : a.P;
+    const int64_t nwarps = (int64_t)gridDim.x * SOLVE_WARPS;
+    for (int64_t it = (int64_t)blockIdx.x * SOLVE_WARPS + wib; it < count; it += nwarps) {
+        const int64_t pos = a.list ? (int64_t)a.list[it] : it;
+        solve_system<T, O>(a, tab, pos, a.order[pos], base, a.k, lane);
+    }
+}
+
+// Batch form: desc[0] positions list[desc[1] ...] of the level-ordered
+// global node list `order`, each solved with its domain's descriptor (domain
+// d owns global node ids [noff[d], noff[d+1])); shared memory laid out for kl
+// neighbours.
+template <typename T, typename O>
+__global__ void __launch_bounds__(SOLVE_WARPS * 32)
+solve_batch_kernel(const SolveArgs* __restrict__ doms, const int64_t* __restrict__ noff, int ndom,
+                   const int32_t* __restrict__ order, const int32_t* __restrict__ list,
+                   const int32_t* __restrict__ desc, int kl, const SweepTables<O> tab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ SolveArgs s_dom[SOLVE_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * warp_smem_bytes<T>(kl);
+    const int64_t n = desc[0];
+    const int32_t* lst = list + desc[1];
+    const int64_t nwarps = (int64_t)gridDim.x * SOLVE_WARPS;
+    int64_t lo = 0, hi = 0;
+    for (int64_t it = (int64_t)blockIdx.x * SOLVE_WARPS + wib; it < n; it += nwarps) {
+        const int64_t pos = lst[it];
+        const int64_t gg = order[pos];
+        if (gg < lo || gg >= hi) {
+            const int d = find_domain(noff, ndom, gg);
+            lo = noff[d];
+            hi = noff[d + 1];
+            __syncwarp();
+            warp_copy_struct(&s_dom[wib], &doms[d], lane);
+            __syncwarp();
+        }
+        solve_system<T, O>(s_dom[wib], tab, pos, (int)(gg - lo), base, kl, lane);
     }
 }
 
@@ -354,15 +397,14 @@ __device__ __forceinline__ DF df_mul(DF a, DF b) {
     return df_fast_two_sum(p, __fadd_rn(e, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
 }
 
+// One system (node g, sweep-table row pos) of the problem `a` with at most
+// NMAX neighbours, in this warp's shared-memory slot `base`.
 template <int NMAX>
-__global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const SolveArgs a, const SweepTables<float> tab) {
+__device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTables<float>& tab, int64_t pos, int g,
+                                               unsigned char* base, int lane) {
     using S = Smem32<NMAX>;
     constexpr int LDK = S::LDK;
     constexpr bool TWO = NMAX > 32;  // lanes own a second row
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    unsigned char* base = smem + (size_t)wib * S::bytes;
     DF* K = reinterpret_cast<DF*>(base);
     DF* c = reinterpret_cast<DF*>(base + S::K);
     DF* w = reinterpret_cast<DF*>(base + S::K + S::C);
@@ -377,11 +419,8 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
     const int lw0 = a.lut.w[0], lw1 = a.lut.w[1];
     const int lcentre = a.lut.e[0] + lw0 * (a.lut.e[1] + lw1 * a.lut.e[2]);
     const int ltotal = lw0 * lw1 * a.lut.w[2];
-    const int64_t nwarps = (int64_t)gridDim.x * SOLVE32_WARPS;
     const int i0 = lane, i1 = lane + 32;
-
-    for (int64_t pos = (int64_t)blockIdx.x * SOLVE32_WARPS + wib; pos < a.P; pos += nwarps) {
-        const int g = a.order[pos];
+    {
         const int n = a.cnt[g];
         int status = SGS_NODE_KRIGED_;
         DF sigma = sd_sill;
@@ -391,12 +430,15 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
             NbInfo self;
             cell_of(G, g, self.c0, self.c1, self.c2);
             self.did = -1;
+            bool fits = true;  // every grid neighbour within half the table's extents
             for (int q = lane; q < n; q += 32) {
                 const int id = a.nbr[(int64_t)g * k + q];
                 NbInfo in;
                 if (id < G.N) {
                     cell_of(G, id, in.c0, in.c1, in.c2);
                     in.did = -1;
+                    fits = fits && 2 * abs(in.c0 - self.c0) <= a.lut.e[0] && 2 * abs(in.c1 - self.c1) <= a.lut.e[1] &&
+                           2 * abs(in.c2 - self.c2) <= a.lut.e[2];
                 } else {
                     in.c0 = in.c1 = in.c2 = 0;
                     in.did = id - (int)G.N;
@@ -406,10 +448,12 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                 // table index of a grid pair (q, r) is centre + lin[r] - lin[q]
                 lin[q] = in.did < 0 ? (in.c0 - self.c0) + lw0 * ((in.c1 - self.c1) + lw1 * (in.c2 - self.c2)) : 0;
             }
+            fits = __all_sync(FULL_MASK, fits);
             __syncwarp();
-            if (lut2) {
-                // every neighbour is a template offset, so every pairwise lag is
-                // inside the table; the clamp only keeps reads in bounds
+            if (lut2 && fits) {
+                // every pairwise lag of grid neighbours is inside the table (a
+                // plan's table spans twice the search template, so this always
+                // holds there); the clamp only keeps reads in bounds
                 for (int q = lane; q < n; q += 32) {
                     if (info[q].did < 0) {
                         const float2 v = lut2[min(max(lcentre - lin[q], 0), ltotal - 1)];
@@ -619,12 +663,13 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
             if (!accept) {
                 if (lane == 0) a.fallback[atomicAdd(a.nfallback, 1)] = (int32_t)pos;
                 __syncwarp();
-                continue;
+                return;
             }
             if (a.w_init && a.n_warm && lane == 0) atomicAdd(a.n_warm, 1ull);
         }
         // ---- table row: grid neighbours with (hi, lo) weights, data folded into b0
         int m = 0;
+        const int64_t row = table_row(tab, pos, k);
         DFAcc b0acc;
         b0acc.init({0.0f, 0.0f});
         if (status == SGS_NODE_KRIGED_) {
@@ -634,8 +679,8 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
                 const unsigned bal = __ballot_sync(FULL_MASK, isgrid);
                 if (isgrid) {
                     const int j = m + __popc(bal & lanemask_lt());
-                    tab.idx[pos * k + j] = a.nbr[(int64_t)g * k + q];
-                    reinterpret_cast<float2*>(tab.w)[pos * k + j] = make_float2(w[q].hi, w[q].lo);
+                    tab.idx[row + j] = a.nbr[(int64_t)g * k + q] + (int32_t)a.node0;
+                    reinterpret_cast<float2*>(tab.w)[row + j] = make_float2(w[q].hi, w[q].lo);
                 } else if (q < n) {
                     b0acc.add_prod(w[q], df_from_double(a.data_val[info[q].did] - a.mu));
                 }
@@ -645,7 +690,7 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
         const DF b0 = warp_sum_df(b0acc.value());
         if (lane == 0) {
             if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
-            tab.node[pos] = g;
+            tab.node[pos] = g + (int32_t)a.node0;
             tab.m[pos] = m;
             reinterpret_cast<float2*>(tab.b0)[pos] = make_float2(b0.hi, b0.lo);
             reinterpret_cast<float2*>(tab.sigma)[pos] = make_float2(sigma.hi, sigma.lo);
@@ -658,6 +703,49 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
             if (lane == 0) a.sigma_full[g] = (double)sigma.hi + (double)sigma.lo;
         }
         __syncwarp();
+    }
+}
+
+template <int NMAX>
+__global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const SolveArgs a, const SweepTables<float> tab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * Smem32<NMAX>::bytes;
+    const int64_t nwarps = (int64_t)gridDim.x * SOLVE32_WARPS;
+    for (int64_t pos = (int64_t)blockIdx.x * SOLVE32_WARPS + wib; pos < a.P; pos += nwarps)
+        solve32_system<NMAX>(a, tab, pos, a.order[pos], base, lane);
+}
+
+// Batch form of solve_fp32_kernel: desc[0] positions list[desc[1] ...]
+// (systems with at most NMAX neighbours, from any domain), each solved with
+// its domain's descriptor.
+template <int NMAX>
+__global__ void __launch_bounds__(SOLVE32_WARPS * 32)
+solve_fp32_batch_kernel(const SolveArgs* __restrict__ doms, const int64_t* __restrict__ noff, int ndom,
+                        const int32_t* __restrict__ order, const int32_t* __restrict__ list,
+                        const int32_t* __restrict__ desc, const SweepTables<float> tab) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ SolveArgs s_dom[SOLVE32_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * Smem32<NMAX>::bytes;
+    const int64_t n = desc[0];
+    const int32_t* lst = list + desc[1];
+    const int64_t nwarps = (int64_t)gridDim.x * SOLVE32_WARPS;
+    int64_t lo = 0, hi = 0;
+    for (int64_t it = (int64_t)blockIdx.x * SOLVE32_WARPS + wib; it < n; it += nwarps) {
+        const int64_t pos = lst[it];
+        const int64_t gg = order[pos];
+        if (gg < lo || gg >= hi) {
+            const int d = find_domain(noff, ndom, gg);
+            lo = noff[d];
+            hi = noff[d + 1];
+            __syncwarp();
+            warp_copy_struct(&s_dom[wib], &doms[d], lane);
+            __syncwarp();
+        }
+        solve32_system<NMAX>(s_dom[wib], tab, pos, (int)(gg - lo), base, lane);
     }
 }
 
@@ -691,6 +779,66 @@ cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<fl
 }
 
 // ---------------------------------------------------------------------------
+// Batches of domains.  Persistent grids (as many blocks as fit on the SMs)
+// walk a device-resident list whose length is read on the device, so the
+// launches need nothing from the host and can be captured in a graph.
+template <int NMAX>
+static cudaError_t launch_solve32_batch(const SolveArgs* doms, const int64_t* noff, int ndom, const int32_t* order,
+                                        const int32_t* list, const int32_t* desc, const SweepTables<float>& t,
+                                        int nsm, cudaStream_t s) {
+    const size_t smem = Smem32<NMAX>::bytes * SOLVE32_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(solve_fp32_batch_kernel<NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_fp32_batch_kernel<NMAX>, SOLVE32_WARPS * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    solve_fp32_batch_kernel<NMAX><<<nsm * per_sm, SOLVE32_WARPS * 32, smem, s>>>(doms, noff, ndom, order, list, desc, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_fp32_batch(int nmax, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                    const int32_t* order, const int32_t* list, const int32_t* desc,
+                                    const SweepTables<float>& t, int nsm, cudaStream_t s) {
+    switch (nmax) {
+        case 8: return launch_solve32_batch<8>(doms, noff, ndom, order, list, desc, t, nsm, s);
+        case 16: return launch_solve32_batch<16>(doms, noff, ndom, order, list, desc, t, nsm, s);
+        case 32: return launch_solve32_batch<32>(doms, noff, ndom, order, list, desc, t, nsm, s);
+        case 48: return launch_solve32_batch<48>(doms, noff, ndom, order, list, desc, t, nsm, s);
+        case 64: return launch_solve32_batch<64>(doms, noff, ndom, order, list, desc, t, nsm, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <typename O>
+static cudaError_t launch_solve64_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                        const int32_t* order, const int32_t* list, const int32_t* desc,
+                                        const SweepTables<O>& t, int nsm, cudaStream_t s) {
+    if (kl < 1 || kl > KMAX) return cudaErrorInvalidValue;
+    const size_t smem = warp_smem_bytes<double>(kl) * SOLVE_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(solve_batch_kernel<double, O>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, solve_batch_kernel<double, O>, SOLVE_WARPS * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    solve_batch_kernel<double, O><<<nsm * per_sm, SOLVE_WARPS * 32, smem, s>>>(doms, noff, ndom, order, list, desc, kl, t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_fp64_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                    const int32_t* order, const int32_t* list, const int32_t* desc,
+                                    const SweepTables<double>& t, int nsm, cudaStream_t s) {
+    return launch_solve64_batch<double>(kl, doms, noff, ndom, order, list, desc, t, nsm, s);
+}
+
+cudaError_t launch_solve_fp64_into_fp32_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
+                                              const int32_t* order, const int32_t* list, const int32_t* desc,
+                                              const SweepTables<float>& t, int nsm, cudaStream_t s) {
+    return launch_solve64_batch<float>(kl, doms, noff, ndom, order, list, desc, t, nsm, s);
+}
+
+// ---------------------------------------------------------------------------
 __global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut t, double* c64, float2* c2,
                                 int64_t total) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
@@ -700,7 +848,7 @@ __global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut 
         const int L2 = (int)(r / t.w[1]) - t.e[2];
         const double c = cov_fp64(v, G.dim, dmul((double)L0, G.spacing[0]), dmul((double)L1, G.spacing[1]),
                                   G.dim == 3 ? dmul((double)L2, G.spacing[2]) : 0.0);
-        c64[i] = c;
+        if (c64) c64[i] = c;
         if (c2) {  // normalized by the sill, as (hi, lo) for the FP32 path
             const double cn = c / v.sill;
             const float hi = (float)cn;

@@ -391,14 +391,15 @@ __device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m
 
 // One piece (chunks [c0, c0 + W*G) of the row, clipped to the row) of one
 // node, FP32 values with compensated sums.
-template <int G>
+template <int G, bool CSR>
 __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int k, int64_t pos, int g, int m, int Rp,
                                                 int c0, int W, int lane, const float* __restrict__ z, uint64_t seed,
                                                 float* __restrict__ V) {
     const int cpn = Rp >> 2;
     const int S = 32 / W, s = lane / W, cl = lane % W;
-    const int32_t* idx = t.idx + pos * k;
-    const float2* w = reinterpret_cast<const float2*>(t.w) + pos * k;
+    const int64_t row = CSR ? t.off[pos] : pos * (int64_t)k;
+    const int32_t* idx = t.idx + row;
+    const float2* w = reinterpret_cast<const float2*>(t.w) + row;
     Dot2 a[G][4];
 #pragma unroll
     for (int gi = 0; gi < G; ++gi)
@@ -450,14 +451,15 @@ __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int
 }
 
 // The same for FP64 values (plain FMA sums).
-template <int G>
+template <int G, bool CSR>
 __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, int k, int64_t pos, int g, int m, int Rp,
                                                 int c0, int W, int lane, const double* __restrict__ z, uint64_t seed,
                                                 double* __restrict__ V) {
     const int cpn = Rp >> 2;
     const int S = 32 / W, s = lane / W, cl = lane % W;
-    const int32_t* idx = t.idx + pos * k;
-    const double* w = t.w + pos * k;
+    const int64_t row = CSR ? t.off[pos] : pos * (int64_t)k;
+    const int32_t* idx = t.idx + row;
+    const double* w = t.w + row;
     D4 a[G];
 #pragma unroll
     for (int gi = 0; gi < G; ++gi) a[gi] = {0.0, 0.0, 0.0, 0.0};
@@ -510,13 +512,16 @@ __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, in
     }
 }
 
-template <typename T, int G, int MINB>
+// CSR: packed tables (t.off rows) and the seed read from f.seed_dev, the form
+// used by batches of domains.
+template <typename T, int G, int MINB, bool CSR>
 __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables<T> t, int k, int Rp, int W,
                                                                const T* __restrict__ z, uint64_t seed,
                                                                T* __restrict__ V, const FlowArgs f) {
     const int lane = threadIdx.x & 31;
     const int64_t items = f.item1;
     const int P4 = W * G;
+    if (CSR && f.seed_dev) seed = *f.seed_dev;
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0)
@@ -531,10 +536,10 @@ __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables
             const int g = t.node[pos];
             const int m = t.m[pos];
             int32_t* done_q = f.done + (int64_t)q * f.N;
-            const bool ok = flow_wait(t.idx + pos * k, m, done_q, f, lane);
+            const bool ok = flow_wait(t.idx + (CSR ? t.off[pos] : pos * (int64_t)k), m, done_q, f, lane);
             if (ok) {
-                if constexpr (sizeof(T) == 4) flow_piece_fp32<G>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
-                else flow_piece_fp64<G>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
+                if constexpr (sizeof(T) == 4) flow_piece_fp32<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
+                else flow_piece_fp64<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
             } else if (lane == 0) {
                 atomicExch(f.err, 1);
             }
@@ -569,18 +574,18 @@ int flow_layout(int Rp, int& W, int& G) {
     return (cpn + W * G - 1) / (W * G);
 }
 
-template <typename T, int G, int MINB>
+template <typename T, int G, int MINB, bool CSR>
 static cudaError_t flow_launch(const SweepTables<T>& t, int k, int Rp, int W, const T* z, uint64_t seed, T* V,
                                const FlowArgs& f, int nsm, cudaStream_t s) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_flow_kernel<T, G, MINB>, 256, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_flow_kernel<T, G, MINB, CSR>, 256, 0);
     if (e != cudaSuccess) return e;
     if (f.blocks_per_sm > 0 && f.blocks_per_sm < per_sm) per_sm = f.blocks_per_sm;
     if (per_sm < 1) per_sm = 1;
     const int64_t items = (f.item1 - f.item0 + f.chunk - 1) / f.chunk;
     int64_t blocks = std::min<int64_t>((int64_t)nsm * per_sm, (items + 7) / 8);
     if (blocks < 1) blocks = 1;
-    sweep_flow_kernel<T, G, MINB><<<(int)blocks, 256, 0, s>>>(t, k, Rp, W, z, seed, V, f);
+    sweep_flow_kernel<T, G, MINB, CSR><<<(int)blocks, 256, 0, s>>>(t, k, Rp, W, z, seed, V, f);
     return cudaGetLastError();
 }
 
@@ -588,10 +593,16 @@ template <typename T>
 static cudaError_t sweep_flow(const SweepTables<T>& t, int k, int Rp, int W, int G, const T* z, uint64_t seed, T* V,
                               const FlowArgs& f, int nsm, cudaStream_t s) {
     if (f.item1 <= f.item0) return cudaSuccess;
-    if (G == 2) return f.tight ? flow_launch<T, 2, 4>(t, k, Rp, W, z, seed, V, f, nsm, s)
-                               : flow_launch<T, 2, 1>(t, k, Rp, W, z, seed, V, f, nsm, s);
-    return f.tight ? flow_launch<T, 1, 6>(t, k, Rp, W, z, seed, V, f, nsm, s)
-                   : flow_launch<T, 1, 1>(t, k, Rp, W, z, seed, V, f, nsm, s);
+    if (t.off) {
+        if (G == 2) return f.tight ? flow_launch<T, 2, 4, true>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                                   : flow_launch<T, 2, 1, true>(t, k, Rp, W, z, seed, V, f, nsm, s);
+        return f.tight ? flow_launch<T, 1, 6, true>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                       : flow_launch<T, 1, 1, true>(t, k, Rp, W, z, seed, V, f, nsm, s);
+    }
+    if (G == 2) return f.tight ? flow_launch<T, 2, 4, false>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                               : flow_launch<T, 2, 1, false>(t, k, Rp, W, z, seed, V, f, nsm, s);
+    return f.tight ? flow_launch<T, 1, 6, false>(t, k, Rp, W, z, seed, V, f, nsm, s)
+                   : flow_launch<T, 1, 1, false>(t, k, Rp, W, z, seed, V, f, nsm, s);
 }
 
 cudaError_t launch_sweep_flow_fp32(const SweepTables<float>& t, int k, int Rp, int W, int G, const float* z,
@@ -617,14 +628,14 @@ int sweep_flow_max_blocks_per_sm(bool fp64, int G, bool tight) {
     int per_sm = 0;
     if (fp64) {
         if (G == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, tight ? sweep_flow_kernel<double, 2, 4> : sweep_flow_kernel<double, 2, 1>, 256, 0);
+            &per_sm, tight ? sweep_flow_kernel<double, 2, 4, false> : sweep_flow_kernel<double, 2, 1, false>, 256, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, tight ? sweep_flow_kernel<double, 1, 6> : sweep_flow_kernel<double, 1, 1>, 256, 0);
+            &per_sm, tight ? sweep_flow_kernel<double, 1, 6, false> : sweep_flow_kernel<double, 1, 1, false>, 256, 0);
     } else {
         if (G == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, tight ? sweep_flow_kernel<float, 2, 4> : sweep_flow_kernel<float, 2, 1>, 256, 0);
+            &per_sm, tight ? sweep_flow_kernel<float, 2, 4, false> : sweep_flow_kernel<float, 2, 1, false>, 256, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, tight ? sweep_flow_kernel<float, 1, 6> : sweep_flow_kernel<float, 1, 1>, 256, 0);
+            &per_sm, tight ? sweep_flow_kernel<float, 1, 6, false> : sweep_flow_kernel<float, 1, 1, false>, 256, 0);
     }
     return per_sm;
 }

@@ -24,12 +24,12 @@ from .model import (
     SphericalVariogram,
     georef,
 )
-from .plan import Plan
+from .plan import Batch, Plan
 from .problem import build_problem, clamped_neighbors
 from .simulation import GPUSEQSIM, Ensemble, FieldSimulationMethod, preprocess, rand, randsingle
 
 __all__ = [
-    "ArgumentError", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
+    "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
     "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",

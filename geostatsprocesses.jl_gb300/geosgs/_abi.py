@@ -125,6 +125,29 @@ class SgsInfo(C.Structure):
     ]
 
 
+class SgsBatchInfo(C.Structure):
+    _fields_ = [
+        ("ndomains", C.c_int32),
+        ("nlevels", C.c_int32),
+        ("nnodes", C.c_int64),
+        ("ndata", C.c_int64),
+        ("n_prior", C.c_int64),
+        ("n_fp64_fallback", C.c_int64),
+        ("sum_grid_neighbors", C.c_int64),
+        ("bin_systems", C.c_int64 * 5),
+        ("ms_search", C.c_double),
+        ("ms_levels", C.c_double),
+        ("ms_solve", C.c_double),
+        ("ms_prepare", C.c_double),
+        ("ms_sweep", C.c_double),
+        ("launches", C.c_int64),
+        ("graph_launches", C.c_int64),
+        ("h2d_bytes", C.c_int64),
+        ("d2h_bytes", C.c_int64),
+        ("device_bytes", C.c_int64),
+    ]
+
+
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(PKG_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libgeosgs.so")
@@ -151,6 +174,18 @@ EXPORTS = (
     "sgs_plan_set_sweep",
     "sgs_plan_tune_sweep",
     "sgs_plan_predict_device",
+    "sgs_batch_create",
+    "sgs_batch_prepare",
+    "sgs_batch_simulate",
+    "sgs_batch_simulate_device",
+    "sgs_batch_domain",
+    "sgs_batch_neighbors",
+    "sgs_batch_weights",
+    "sgs_batch_set_sweep",
+    "sgs_batch_tune_sweep",
+    "sgs_batch_info_get",
+    "sgs_batch_destroy",
+    "sgs_batch_last_error",
 )
 
 _lib = None
@@ -209,6 +244,32 @@ def _declare(lib):
     lib.sgs_nn_adam.restype = C.c_int
     lib.sgs_schedule_noalloc.argtypes = [P, P, P, C.c_int64, C.c_int32, P, P, P, C.c_int32, ip, P]
     lib.sgs_schedule_noalloc.restype = C.c_int
+    i64p = C.POINTER(C.c_int64)
+    lib.sgs_batch_create.argtypes = [C.POINTER(SgsProblem), C.c_int32, C.POINTER(P)]
+    lib.sgs_batch_create.restype = C.c_int
+    lib.sgs_batch_prepare.argtypes = [P]
+    lib.sgs_batch_prepare.restype = C.c_int
+    lib.sgs_batch_simulate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp]
+    lib.sgs_batch_simulate.restype = C.c_int
+    lib.sgs_batch_simulate_device.argtypes = [P, C.c_int32, C.c_uint64, P, P]
+    lib.sgs_batch_simulate_device.restype = C.c_int
+    lib.sgs_batch_domain.argtypes = [P, C.c_int32, i64p, i64p]
+    lib.sgs_batch_domain.restype = C.c_int
+    lib.sgs_batch_neighbors.argtypes = [P, C.c_int32, ip, ip]
+    lib.sgs_batch_neighbors.restype = C.c_int
+    lib.sgs_batch_weights.argtypes = [P, C.c_int32, dp, dp, ip]
+    lib.sgs_batch_weights.restype = C.c_int
+    lib.sgs_batch_set_sweep.argtypes = [P, C.POINTER(SgsSweepConfig)]
+    lib.sgs_batch_set_sweep.restype = C.c_int
+    lib.sgs_batch_tune_sweep.argtypes = [P, C.c_int32, C.POINTER(SgsSweepConfig), C.POINTER(SgsSweepConfig),
+                                         C.c_int32, C.POINTER(C.c_int32)]
+    lib.sgs_batch_tune_sweep.restype = C.c_int
+    lib.sgs_batch_info_get.argtypes = [P, C.POINTER(SgsBatchInfo)]
+    lib.sgs_batch_info_get.restype = C.c_int
+    lib.sgs_batch_destroy.argtypes = [P]
+    lib.sgs_batch_destroy.restype = None
+    lib.sgs_batch_last_error.argtypes = [P]
+    lib.sgs_batch_last_error.restype = C.c_char_p
     return lib
 
 
@@ -232,5 +293,12 @@ def load_library(path: str | None = None):
 def check(lib, code: int, plan=None):
     if code != SGS_OK:
         msg = lib.sgs_last_error(plan)
+        raise GeoSGSError(code, msg.decode() if msg else "")
+    return code
+
+
+def check_batch(lib, code: int, batch=None):
+    if code != SGS_OK:
+        msg = lib.sgs_batch_last_error(batch)
         raise GeoSGSError(code, msg.decode() if msg else "")
     return code

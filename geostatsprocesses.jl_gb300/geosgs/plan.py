@@ -133,3 +133,107 @@ class Plan:
         inf = _abi.SgsInfo()
         self._check(self.lib.sgs_plan_info(self.h, C.byref(inf)))
         return inf
+
+
+class Batch:
+    """Owns one sgs_batch: many independent problems (domains) prepared and
+    simulated together, one launch per phase over all domains, CUDA graphs
+    for the prepare sequence and the seeded sweep.
+
+    `problems` is a list of (sgs_problem, keepalive) pairs as returned by
+    build_problem."""
+
+    def __init__(self, problems):
+        self.lib = _abi.load_library()
+        n = len(problems)
+        arr = (_abi.SgsProblem * n)()
+        for i, (p, _) in enumerate(problems):
+            arr[i] = p
+        self._keep = ([k for _, k in problems], arr)
+        h = C.c_void_p()
+        _abi.check_batch(self.lib, self.lib.sgs_batch_create(arr, n, C.byref(h)))
+        self.h = h
+        self.ndomains = n
+        self.first = np.empty(n, dtype=np.int64)
+        self.sizes = np.empty(n, dtype=np.int64)
+        self.k = np.empty(n, dtype=np.int64)
+        for d in range(n):
+            f, c = C.c_int64(), C.c_int64()
+            self._check(self.lib.sgs_batch_domain(self.h, d, C.byref(f), C.byref(c)))
+            self.first[d], self.sizes[d] = f.value, c.value
+            p = problems[d][0]
+            nmax = int(p.maxneighbors)
+            self.k[d] = nmax if 1 <= nmax <= c.value else c.value
+        self.nnodes = int(self.sizes.sum())
+        self.prepared = False
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sgs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        return _abi.check_batch(self.lib, rc, self.h)
+
+    def prepare(self):
+        self._check(self.lib.sgs_batch_prepare(self.h))
+        self.prepared = True
+        return self
+
+    def simulate(self, nreals: int, z=None, seed: int = 0):
+        """List of nreals x N_d realization-major FP64 arrays, one per domain.
+        z: None (seeded draws), or a list of nreals x N_d arrays, or one flat
+        array in the concatenated layout."""
+        out = np.empty(nreals * self.nnodes, dtype=np.float64)
+        zp = None
+        if z is not None:
+            if isinstance(z, (list, tuple)):
+                z = np.concatenate([np.asarray(a, dtype=np.float64).reshape(-1) for a in z])
+            z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).reshape(-1))
+            if z.size != nreals * self.nnodes:
+                raise ValueError("z does not match nreals x nodes")
+            zp = _dp(z)
+        self._check(self.lib.sgs_batch_simulate(self.h, nreals, zp, C.c_uint64(seed), _dp(out)))
+        return [out[nreals * f: nreals * (f + n)].reshape(nreals, n) for f, n in zip(self.first, self.sizes)]
+
+    def simulate_device(self, nreals: int, seed: int, vals_ptr: int, stream: int | None = None):
+        self._check(self.lib.sgs_batch_simulate_device(self.h, nreals, C.c_uint64(seed), C.c_void_p(vals_ptr),
+                                                       C.c_void_p(stream) if stream else None))
+
+    def neighbors(self, d: int):
+        n, k = int(self.sizes[d]), int(self.k[d])
+        idx = np.empty((n, k), dtype=np.int32)
+        cnt = np.empty(n, dtype=np.int32)
+        self._check(self.lib.sgs_batch_neighbors(self.h, d, _ip(idx), _ip(cnt)))
+        return idx, cnt
+
+    def weights(self, d: int):
+        n, k = int(self.sizes[d]), int(self.k[d])
+        w = np.empty((n, k), dtype=np.float64)
+        s = np.empty(n, dtype=np.float64)
+        st = np.empty(n, dtype=np.int32)
+        self._check(self.lib.sgs_batch_weights(self.h, d, _dp(w), _dp(s), _ip(st)))
+        return w, s, st
+
+    def set_sweep(self, chunk=1, blocks_per_sm=0, lanes_g=1, lanes_w=0, tight=0, **_ignored):
+        c = _abi.SgsSweepConfig(_abi.SGS_SWEEP_FLOW, chunk, blocks_per_sm, lanes_g, lanes_w, 0, 0, tight, 0.0)
+        self._check(self.lib.sgs_batch_set_sweep(self.h, C.byref(c)))
+        return self
+
+    def tune_sweep(self, nreals: int):
+        chosen = _abi.SgsSweepConfig()
+        tried = (_abi.SgsSweepConfig * 64)()
+        n = C.c_int32()
+        self._check(self.lib.sgs_batch_tune_sweep(self.h, nreals, C.byref(chosen), tried, 64, C.byref(n)))
+        return chosen.as_dict(), [tried[i].as_dict() for i in range(min(n.value, 64))]
+
+    def info(self) -> _abi.SgsBatchInfo:
+        inf = _abi.SgsBatchInfo()
+        self._check(self.lib.sgs_batch_info_get(self.h, C.byref(inf)))
+        return inf

@@ -16,10 +16,17 @@ the stated seed.  Coordinates are cell units with origin 0 and unit spacing.
       network's training distribution), search ellipsoid = the variogram's,
       k=32, RandomPath seed 5, 64 realizations (the learned warm start's
       evaluation run)
+  c5  a batch of 1,000 independent domains (seed 6): 2D or 3D with equal
+      odds, sides uniform in [32, 256] cells (3D depth in [8, 64]), each its
+      own variogram (spherical / exponential / gaussian with equal odds,
+      isotropic range uniform in [5, 80] cells, nugget uniform in [0, 0.1],
+      sill 1), 0-500 data uniform in the box with N(0,1) values, :range
+      neighbourhood, maxneighbors drawn from {8, 16, 32, 48}, its own
+      RandomPath, 8 realizations
 """
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 from typing import Any
 
 import numpy as np
@@ -98,3 +105,52 @@ def small(dim=2, n=24, k=8, ndata=0, vario="sph", seed=0, nugget=0.0, ranges=(6.
     m = GPUSEQSIM(path=p, maxneighbors=k, neighborhood=ball if ball is not None else "range",
                   precision=precision)
     return Workload(f"small{dim}d_{n}_{vario}_k{k}", proc, grid, data, m, nreals)
+
+
+@dataclass
+class BatchWorkload:
+    """Independent domains simulated together (one Workload per domain)."""
+
+    name: str
+    items: list = field(default_factory=list)
+    nreals: int = 8
+
+    def nodes(self) -> int:
+        return int(sum(w.domain.nelements() for w in self.items))
+
+
+def c5(precision: str = "fp32", nreals: int = 8, ndomains: int = 1000, seed: int = 6, sides=(32, 256),
+       depth=(8, 64), ranges=(5.0, 80.0), nugget=(0.0, 0.1), ndata=(0, 500), ks=(8, 16, 32, 48),
+       name: str | None = None) -> BatchWorkload:
+    """The uneven batch; the keyword ranges shrink it for parity tests."""
+    rng = np.random.default_rng(seed)
+    classes = (SphericalVariogram, ExponentialVariogram, GaussianVariogram)
+    items = []
+    for d in range(ndomains):
+        dim = 3 if rng.random() < 0.5 else 2
+        dims = [int(rng.integers(sides[0], sides[1] + 1)) for _ in range(2)]
+        if dim == 3:
+            dims.append(int(rng.integers(depth[0], depth[1] + 1)))
+        grid = CartesianGrid(tuple(dims))
+        cls = classes[int(rng.integers(0, 3))]
+        rg = float(rng.uniform(*ranges))
+        nug = float(rng.uniform(*nugget))
+        nd = int(rng.integers(ndata[0], ndata[1] + 1))
+        data = None
+        if nd:
+            xyz = rng.uniform(0.0, 1.0, (nd, dim)) * np.asarray(dims, dtype=np.float64)
+            data = georef({"Z": rng.standard_normal(nd)}, xyz)
+        k = int(ks[int(rng.integers(0, len(ks)))])
+        proc = GaussianProcess(cls(range=rg, sill=1.0, nugget=nug), 0.0)
+        m = GPUSEQSIM(path=RandomPath(seed * 1000003 + d), maxneighbors=k, neighborhood="range",
+                      precision=precision)
+        items.append(Workload("c5_domain%d" % d, proc, grid, data, m, nreals))
+    nm = name or "c5_batch_%d_domains_2d3d_sides%d-%d_depth%d-%d_k8-48" % (ndomains, sides[0], sides[1],
+                                                                           depth[0], depth[1])
+    return BatchWorkload(nm, items, nreals)
+
+
+def c5_small(precision: str = "fp32", nreals: int = 8, ndomains: int = 12, seed: int = 60) -> BatchWorkload:
+    """A small uneven batch for parity tests (oracle in seconds)."""
+    return c5(precision, nreals, ndomains, seed, sides=(8, 40), depth=(3, 9), ranges=(3.0, 12.0),
+              nugget=(0.0, 0.1), ndata=(0, 40), ks=(8, 16, 32, 48), name="c5_small_%d_domains" % ndomains)

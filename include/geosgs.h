@@ -272,6 +272,82 @@ int sgs_plan_set_sweep(sgs_plan* plan, const sgs_sweep_config* config);
 int sgs_plan_tune_sweep(sgs_plan* plan, int32_t nreals, sgs_sweep_config* chosen, sgs_sweep_config* tried,
                         int32_t max_tried, int32_t* ntried);
 
+/* ---- batches of independent domains -------------------------------------
+ * Many independent problems (each its own grid, data, variogram, mean,
+ * neighbourhood, maxneighbors and path; one sgs_problem per domain) prepared
+ * and simulated together: every phase is one launch over all domains' nodes
+ * (search, dependency levels, level order, size bins), the kriging systems
+ * are solved in size classes (at most 8, 16, 32, 48, 64 neighbours: one
+ * launch each), and the sweep is one persistent dataflow launch.  The
+ * prepare sequence and the seeded sweep are captured in CUDA graphs and
+ * replayed by later calls.  Replaces a loop of rand(rng, process_d, domain_d,
+ * nreals; data = data_d, method = SEQSIM(...)) calls over the domains
+ * (src/simulation/field.jl:73-124), each of which runs preprocess /
+ * randsingle (seqsim.jl:50-156) on its own.
+ *
+ * All domains use the same device and precision; warm_start and flags must
+ * be 0.  Global node ids number the domains' grid nodes one after another:
+ * domain d owns ids [first_d, first_d + N_d) (sgs_batch_domain).  Host
+ * arrays of realizations are concatenated by domain: domain d's block is
+ * nreals x N_d realization-major and starts at element nreals * first_d. */
+typedef struct sgs_batch sgs_batch;
+
+typedef struct sgs_batch_info {
+    int32_t ndomains;
+    int32_t nlevels;            /* deepest dependency level + 1 over all domains  */
+    int64_t nnodes;             /* grid nodes of all domains                       */
+    int64_t ndata;              /* conditioning points of all domains              */
+    int64_t n_prior;            /* nodes drawn from the prior                      */
+    int64_t n_fp64_fallback;    /* FP32 systems re-solved in FP64                  */
+    int64_t sum_grid_neighbors; /* grid neighbours used by the sweep, all nodes    */
+    int64_t bin_systems[5];     /* systems per size class (<= 8/16/32/48/64 nbrs)  */
+    double  ms_search, ms_levels, ms_solve; /* phases of the last prepare          */
+    double  ms_prepare;         /* the last prepare as a whole                     */
+    double  ms_sweep;           /* the last sweep                                  */
+    int64_t launches;           /* kernels launched, graph nodes included          */
+    int64_t graph_launches;     /* CUDA graph launches                             */
+    int64_t h2d_bytes, d2h_bytes;
+    int64_t device_bytes;       /* device memory held by the batch                 */
+} sgs_batch_info;
+
+/* Validate every problem (the first invalid one is named in the error) and
+ * upload geometry, data, paths and search templates. */
+int sgs_batch_create(const sgs_problem* problems, int32_t ndomains, sgs_batch** batch);
+/* Neighbour search, levels, level order, size bins and kriging solves for
+ * all domains.  The first call sizes the tables, then captures the sequence
+ * in a CUDA graph; every call launches that graph. */
+int sgs_batch_prepare(sgs_batch* batch);
+/* Simulate nreals realizations of every domain into out (host, concatenated
+ * by domain as above).  z: standard normals in the same layout, or NULL for
+ * draws from `seed` (Philox4x32-10 keyed by seed, counter = global node id
+ * and realization / 4). */
+int sgs_batch_simulate(sgs_batch* batch, int32_t nreals, const double* z, uint64_t seed, double* out);
+/* Seeded sweep into vals_dev: device array [nnodes][nreals rounded up to a
+ * multiple of 4] of centred values (v - mean of the node's domain), float for
+ * SGS_PREC_FP32_REFINE, double for SGS_PREC_FP64, rows by global node id.
+ * Captured in a CUDA graph per (nreals, vals_dev, sweep configuration) and
+ * replayed; stream is a cudaStream_t (NULL = the batch's stream). */
+int sgs_batch_simulate_device(sgs_batch* batch, int32_t nreals, uint64_t seed, void* vals_dev, void* stream);
+/* First global node id and node count of domain d. */
+int sgs_batch_domain(const sgs_batch* batch, int32_t domain, int64_t* first, int64_t* nnodes);
+/* Neighbour rows of domain d, as sgs_plan_neighbors (N_d x maxneighbors_d,
+ * local augmented ids: grid nodes 0..N_d-1, data N_d..). */
+int sgs_batch_neighbors(sgs_batch* batch, int32_t domain, int32_t* idx, int32_t* count);
+/* Kriging weights, sigma and status of domain d, as sgs_plan_weights (the
+ * weights are recomputed for the whole batch with an export). */
+int sgs_batch_weights(sgs_batch* batch, int32_t domain, double* weights, double* sigma, int32_t* status);
+/* Sweep configuration (mode must be SGS_SWEEP_FLOW; level_lo/level_hi are
+ * ignored) and its autotuner over the dataflow mappings, as for plans. */
+int sgs_batch_set_sweep(sgs_batch* batch, const sgs_sweep_config* config);
+int sgs_batch_tune_sweep(sgs_batch* batch, int32_t nreals, sgs_sweep_config* chosen, sgs_sweep_config* tried,
+                         int32_t max_tried, int32_t* ntried);
+int sgs_batch_info_get(const sgs_batch* batch, sgs_batch_info* info);
+/* Release all device memory and graphs.  NULL is ignored. */
+void sgs_batch_destroy(sgs_batch* batch);
+/* Message of the last failure on this batch, or of the last failed
+ * sgs_batch_create on this thread when batch is NULL. */
+const char* sgs_batch_last_error(const sgs_batch* batch);
+
 /* ---- allocation-free schedule ------------------------------------------ */
 #define SGS_NOALLOC_MAX_LEVELS 262144
 

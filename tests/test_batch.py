@@ -1,0 +1,146 @@
+"""Batches of independent domains (sgs_batch_*, include/geosgs.h) against the
+FP64 oracle, domain by domain.
+
+A batch prepares and simulates many problems together (one launch per
+phase over all domains, systems solved in size classes, a persistent
+dataflow sweep, CUDA graphs for prepare and the seeded sweep); each domain's
+results must equal what the oracle gives for that domain alone: neighbour
+rows and counts bit-exact, node status identical, weights within 1e-9
+(FP64) / 1e-6 (FP32 refined), values within 1e-6 relative
+(max |v_gpu - v_oracle| / max(|v_oracle|, 1))."""
+import numpy as np
+import pytest
+
+import geosgs
+from geosgs import _abi, workloads
+
+VALUE_TOL = 1e-6
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0))) if a.size else 0.0
+
+
+def problems_of(bw, precision):
+    out = []
+    for w in bw.items:
+        w.method.precision = precision
+        out.append(geosgs.build_problem(w.process, w.domain, w.data, w.method))
+    return out
+
+
+def test_c5_generator_is_seeded_and_in_range():
+    a, b = workloads.c5_small(), workloads.c5_small()
+    assert [w.domain.dims for w in a.items] == [w.domain.dims for w in b.items]
+    full = workloads.c5()
+    assert len(full.items) == 1000 and full.nreals == 8
+    dims = [len(w.domain.dims) for w in full.items]
+    assert 400 < dims.count(3) < 600
+    for w in full.items:
+        d = w.domain.dims
+        assert all(32 <= s <= 256 for s in d[:2])
+        if len(d) == 3:
+            assert 8 <= d[2] <= 64
+        assert 5.0 <= w.process.func.range() <= 80.0
+        assert w.method.maxneighbors in (8, 16, 32, 48)
+        assert w.data is None or 1 <= w.data.nrow() <= 500
+
+
+def test_batch_argument_errors():
+    """Validation happens before any device work (runs without a GPU)."""
+    from geosgs import _build
+
+    _build.build()
+    bw = workloads.c5_small(ndomains=3)
+    probs = problems_of(bw, "fp32")
+    probs[1][0].precision = _abi.SGS_PREC_FP64
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        geosgs.Batch(probs)
+    assert e.value.code == _abi.SGS_ERR_ARG and "domain 1" in str(e.value)
+    probs = problems_of(bw, "fp32")
+    probs[2][0].maxneighbors = 65
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        geosgs.Batch(probs)
+    assert e.value.code == _abi.SGS_ERR_ARG and "domain 2" in str(e.value)
+    probs = problems_of(bw, "fp32")
+    probs[0][0].warm_start = 1
+    with pytest.raises(geosgs.GeoSGSError) as e:
+        geosgs.Batch(probs)
+    assert e.value.code == _abi.SGS_ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_matches_oracle_per_domain(precision, oracle_mod, geosgs_lib):
+    bw = workloads.c5_small(precision)
+    probs = problems_of(bw, precision)
+    B = geosgs.Batch(probs).prepare()
+    info = B.info()
+    assert info.ndomains == len(probs) and info.nnodes == B.nnodes
+    assert info.graph_launches == 1 and sum(info.bin_systems) == B.nnodes
+    R = bw.nreals
+    zs = [np.random.default_rng(100 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
+    vals = B.simulate(R, z=zs)
+    priors = 0
+    for d, (p, keep) in enumerate(probs):
+        O = oracle_mod.OraclePlan(p, keep).prepare()
+        ig, cg = B.neighbors(d)
+        io, co = O.neighbors()
+        np.testing.assert_array_equal(cg, co, err_msg=f"domain {d}")
+        np.testing.assert_array_equal(ig, io, err_msg=f"domain {d}")
+        wg, sg, stg = B.weights(d)
+        wo, so, sto = O.weights()
+        np.testing.assert_array_equal(stg, sto, err_msg=f"domain {d}")
+        tol = 1e-9 if precision == "fp64" else 1e-6
+        np.testing.assert_allclose(wg, wo, rtol=0, atol=tol, err_msg=f"domain {d}")
+        np.testing.assert_allclose(sg, so, rtol=0, atol=tol, err_msg=f"domain {d}")
+        assert rel_err(vals[d], O.simulate(R, zs[d])) <= VALUE_TOL, d
+        priors += int(np.count_nonzero(sto))
+    assert B.info().n_prior == priors
+    B.close()
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_and_seeded_draws(oracle_mod, geosgs_lib):
+    """Replayed graphs give identical results; seeded draws are Philox keyed
+    by the global node id, so the oracle fed those normals agrees."""
+    bw = workloads.c5_small("fp32", ndomains=9, seed=61)
+    probs = problems_of(bw, "fp32")
+    B = geosgs.Batch(probs).prepare()
+    R = 12
+    a = B.simulate(R, seed=11)
+    B.prepare()
+    b = B.simulate(R, seed=11)
+    c = B.simulate(R, seed=12)
+    for d in range(len(probs)):
+        np.testing.assert_array_equal(a[d], b[d])
+        assert not np.array_equal(a[d], c[d])
+    zall = oracle_mod.normals(11, B.nnodes, R)
+    for d, (p, keep) in enumerate(probs):
+        O = oracle_mod.OraclePlan(p, keep).prepare()
+        f, n = int(B.first[d]), int(B.sizes[d])
+        assert rel_err(a[d], O.simulate(R, zall[:, f:f + n])) <= VALUE_TOL, d
+    assert B.info().graph_launches >= 4
+    B.close()
+
+
+@pytest.mark.gpu
+def test_batch_device_values_and_autotuner(oracle_mod, geosgs_lib):
+    torch = pytest.importorskip("torch")
+    bw = workloads.c5_small("fp32", ndomains=7, seed=62)
+    probs = problems_of(bw, "fp32")
+    B = geosgs.Batch(probs).prepare()
+    R = 8
+    chosen, tried = B.tune_sweep(R)
+    assert len(tried) >= 2 and chosen["ms"] == min(t["ms"] for t in tried)
+    host = B.simulate(R, seed=5)
+    V = torch.empty((B.nnodes, R), dtype=torch.float32, device="cuda")
+    B.simulate_device(R, 5, V.data_ptr())
+    info = B.info()
+    assert info.ms_sweep > 0
+    Vh = V.cpu().numpy().astype(np.float64)
+    for d, w in enumerate(bw.items):
+        f, n = int(B.first[d]), int(B.sizes[d])
+        dev = Vh[f:f + n].T + w.process.mean
+        assert rel_err(dev, host[d]) <= 1e-7, d
+    B.close()
