@@ -193,6 +193,27 @@ def run_reference(args):
     ws, rank, _ = dist_setup(args)
     if rank != 0:
         return
+    if args.workload == "c5":
+        from geosgs import workloads
+
+        bw = workloads.c5("fp64", nreals=args.nreals or 8, ndomains=args.ndomains)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, cores, sample = cpu_sample_batch(bw, args.cpu_nodes * 4)
+            if i >= args.warmup:
+                vals.append(v)
+        value = statistics.median(vals)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * bw.nodes() * bw.nreals / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded PCG64 domains, data and paths; Philox normals)",
+            "config": {"workload": bw.name, "ndomains": len(bw.items), "nodes": bw.nodes(), "nreals": bw.nreals},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Julia reference not runnable on this box (no Julia toolchain); timed the FP64 C++ "
+                    "restatement of SEQSIM (oracle/) instead"}))
+        return
     wl = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
     vals, secs = [], []
     for i in range(args.warmup + args.steps):

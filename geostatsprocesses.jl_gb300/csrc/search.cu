@@ -64,6 +64,8 @@ struct SearchSmem {
     long long* dd2;   // [DCAP] data candidates' d2 keys
     int32_t* didx;    // [DCAP] their augmented ids
     int32_t* squ;     // [64] screened data candidates
+    int32_t* rstart;  // [32] first bucket-ordered datum of each of 32 bucket rows
+    int32_t* roff;    // [32] their offsets in the concatenated candidate list
 };
 
 // The neighbour row of node g of the problem described by `a`.
@@ -96,11 +98,13 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
                     hi[j] = a.nb[j] - 1;
                 } else {
                     // bucket range of the neighbourhood's bounding box, in FP32
-                    // with one bucket of margin on each side (a superset)
+                    // with a margin of 1e-3 buckets on each side: far above the
+                    // few FP32 roundings here (~1e-5 buckets) and the FP32
+                    // rounding of the half extent, so the range is a superset
                     const int ij = j == 0 ? i0 : (j == 1 ? i1 : i2);
                     const float xr = ((float)ij + 0.5f) * a.spacing_f[j];
-                    const float l = floorf((xr - a.ext_f[j]) * a.inv_bw_f[j]) - 1.0f;
-                    const float h = floorf((xr + a.ext_f[j]) * a.inv_bw_f[j]) + 1.0f;
+                    const float l = floorf((xr - a.ext_f[j]) * a.inv_bw_f[j] - 1e-3f);
+                    const float h = floorf((xr + a.ext_f[j]) * a.inv_bw_f[j] + 1e-3f);
                     lo[j] = (int)fmaxf(0.0f, fminf(l, (float)(a.nb[j] - 1)));
                     hi[j] = (int)fmaxf(0.0f, fminf(h, (float)(a.nb[j] - 1)));
                 }
@@ -137,34 +141,64 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
                     nbuf = min(nbuf, k);
                 }
             };
-            for (int bz = lo[2]; bz <= hi[2]; ++bz)
-                for (int by = lo[1]; by <= hi[1]; ++by) {
-                    const int row = a.nb[0] * (by + a.nb[1] * bz);
-                    const int s = a.bstart[row + lo[0]], e = a.bstart[row + hi[0] + 1];
-                    for (int base = s; base < e; base += 32) {
-                        const int i = base + lane;
-                        bool maybe = false;
-                        if (i < e) {
-                            // FP32 screen on origin-relative FP32 coordinates;
-                            // bound_f includes a slack above their rounding
-                            const float4 p = a.dxyz_f[i];
-                            maybe = metric_maybe_inside(a.metric, G.dim, p.x - xr[0], p.y - xr[1], p.z - xr[2]);
-                        }
-                        const unsigned b = __ballot_sync(FULL_MASK, maybe);
-                        if (maybe) squ[nq + __popc(b & lt)] = i;
-                        nq += __popc(b);
+            // Candidates: the bucket rows (by, bz) of the bounding box, 32 rows
+            // at a time.  Lane r loads row r's range of bucket-ordered data,
+            // a warp scan gives the rows' offsets in one concatenated list,
+            // and the warp screens that list 32 candidates at a time (each
+            // lane finds its candidate's row by binary search), so the
+            // rows' loads overlap and lanes stay busy across short rows.
+            const int n1 = hi[1] - lo[1] + 1;
+            const int nrows = n1 * (hi[2] - lo[2] + 1);
+            for (int r0 = 0; r0 < nrows; r0 += 32) {
+                const int r = r0 + lane;
+                int rs = 0, len = 0;
+                if (r < nrows) {
+                    const int row = a.nb[0] * ((lo[1] + r % n1) + a.nb[1] * (lo[2] + r / n1));
+                    rs = a.bstart[row + lo[0]];
+                    len = a.bstart[row + hi[0] + 1] - rs;
+                }
+                int incl = len;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL_MASK, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                const int total = __shfl_sync(FULL_MASK, incl, 31);
+                sm.rstart[lane] = rs;
+                sm.roff[lane] = incl - len;
+                __syncwarp();
+                for (int base = 0; base < total; base += 32) {
+                    const int v = base + lane;
+                    bool maybe = false;
+                    int i = 0;
+                    if (v < total) {
+                        // last row whose offset is <= v holds candidate v
+                        int rr = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1)
+                            if (sm.roff[rr + step] <= v) rr += step;
+                        i = sm.rstart[rr] + (v - sm.roff[rr]);
+                        // FP32 screen on origin-relative FP32 coordinates;
+                        // bound_f includes a slack above their rounding
+                        const float4 p = a.dxyz_f[i];
+                        maybe = metric_maybe_inside(a.metric, G.dim, p.x - xr[0], p.y - xr[1], p.z - xr[2]);
+                    }
+                    const unsigned b = __ballot_sync(FULL_MASK, maybe);
+                    if (maybe) squ[nq + __popc(b & lt)] = i;
+                    nq += __popc(b);
+                    __syncwarp();
+                    if (nq >= 32) {
+                        exact(32);
+                        const int rest = nq - 32;
+                        const int vq = lane < rest ? squ[32 + lane] : 0;
                         __syncwarp();
-                        if (nq >= 32) {
-                            exact(32);
-                            const int rest = nq - 32;
-                            const int v = lane < rest ? squ[32 + lane] : 0;
-                            __syncwarp();
-                            if (lane < rest) squ[lane] = v;
-                            __syncwarp();
-                            nq = rest;
-                        }
+                        if (lane < rest) squ[lane] = vq;
+                        __syncwarp();
+                        nq = rest;
                     }
                 }
+                __syncwarp();  // the row table is rewritten by the next 32 rows
+            }
             if (nq > 0) exact(nq);
             if (nbuf > 0) warp_sort_pairs(dd2, didx, nbuf, lane);
             nd = min(nbuf, k);
@@ -172,15 +206,15 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
 
         // ---- grid candidates from the sorted template ----
         int ng = 0;
+        int before = 0;  // data strictly nearer than the current template entry
         for (int base = 0; base < a.T && ng < k; base += 32) {
             // no template entry from here on can enter the k nearest once
-            // ng grid + the data strictly nearer than this entry fill k
+            // ng grid + the data strictly nearer than this entry fill k; the
+            // template keys do not decrease, so `before` only moves forward
+            // through the sorted data keys (same value in every lane)
             if (nd > 0) {
                 const long long dcur = tkey[base];
-                int before = 0;
-                for (int q = lane; q < nd; q += 32) before += dd2[q] < dcur ? 1 : 0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(FULL_MASK, before, o);
+                while (before < nd && dd2[before] < dcur) ++before;
                 if (ng + before >= k) break;
             }
             const int j = base + lane;
@@ -251,9 +285,10 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
     __shared__ long long s_dd2[SEARCH_WARPS][DCAP];                       \
     __shared__ int32_t s_didx[SEARCH_WARPS][DCAP];                        \
     __shared__ int32_t s_squ[SEARCH_WARPS][64];                           \
+    __shared__ int32_t s_rows[SEARCH_WARPS][64];                          \
     const int lane = threadIdx.x & 31;                                    \
     const int wib = threadIdx.x >> 5;                                     \
-    const SearchSmem sm{s_gd2[wib], s_gidx[wib], s_dd2[wib], s_didx[wib], s_squ[wib]}
+    const SearchSmem sm{s_gd2[wib], s_gidx[wib], s_dd2[wib], s_didx[wib], s_squ[wib], s_rows[wib], s_rows[wib] + 32}
 
 __global__ void __launch_bounds__(SEARCH_WARPS * 32) search_kernel(const SearchArgs a) {
     SEARCH_SMEM_DECL;

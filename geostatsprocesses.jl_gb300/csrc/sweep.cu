@@ -344,15 +344,16 @@ cudaError_t launch_sweep_all_fp64(const SweepTables<double>& t, int k, const int
 //
 // Memory ordering: the item's lanes store the piece, each fences (gpu
 // scope), the warp synchronizes, lane 0 stores the flag; a reader's lanes
-// load flags, fence, synchronize, then read rows with L2-only loads
-// (ld.global.cg), so no stale L1 line of a row written by another SM is used.
+// load flags with acquire semantics, synchronize, then read rows with L2-only
+// loads (ld.global.cg), so no stale L1 line of a row written by another SM is
+// used.
 //
 // Lane layout inside a warp: W lanes per slice of the neighbour list (a
 // power of two), S = 32 / W slices, each lane G chunks of the piece
 // (P4 = W * G); the S partial sums are combined across lanes at the end.
-__device__ __forceinline__ int ld_flag(const int32_t* p) {
+__device__ __forceinline__ int ld_flag_acquire(const int32_t* p) {
     int v;
-    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 __device__ __forceinline__ void st_flag(int32_t* p, int v) {
@@ -367,13 +368,15 @@ __device__ __forceinline__ uint64_t global_ns() {
 // Wait until piece q of every grid neighbour is stored in this sweep (flags
 // of piece q: done_q); false when a wait gave up.  A legitimate wait can last
 // as long as the longest dependency chain, so the bound is wall-clock time.
+// The flag that ends a wait is read with acquire semantics, and the warp
+// barrier orders it before every lane's reads of the neighbours' rows.
 __device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m, const int32_t* done_q,
                                           const FlowArgs& f, int lane) {
     bool ok = true;
     for (int j = lane; j < m; j += 32) {
         const int32_t* flag = done_q + idx[j];
         uint64_t t0 = 0;
-        while (ld_flag(flag) != f.epoch) {
+        while (ld_flag_acquire(flag) != f.epoch) {
             const uint64_t now = global_ns();
             if (t0 == 0) t0 = now;
             if (now - t0 > f.wait_ns) {
@@ -384,7 +387,6 @@ __device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m
         }
     }
     ok = __all_sync(FULL_MASK, ok);
-    __threadfence();
     __syncwarp();
     return ok;
 }
