@@ -82,6 +82,7 @@ struct sgs_plan {
     sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0.f};
     int64_t done_cap = 0;         // flags allocated in d_done (pieces x N)
     int last_sweep_mode = SGS_SWEEP_FLOW;  // mode of the last sweep launched
+    int data_only = 0;            // neighbours from the data alone (sgs_krige)
     sgs_info info{};
 };
 
@@ -651,6 +652,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     sa.nbr = P->d_nbr;
     sa.cnt = P->d_cnt;
     sa.ngrid = P->d_ngrid;
+    sa.data_only = P->data_only;
     CK(P, cudaEventRecord(P->ev[0], st));
     LAUNCH(P, 1, launch_search(sa, st));
     CK(P, cudaEventRecord(P->ev[1], st));
@@ -1167,5 +1169,64 @@ extern "C" int sgs_plan_predict_device(sgs_plan* P, float* out, int32_t tensor_c
     if (tensor_cores) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + 12, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CK(P, cudaStreamSynchronize(st));
     if (htc) return set_err(P, SGS_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait exceeded its bound");
+    return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Posterior mean by simple kriging from the data alone: a plan whose search
+// keeps data candidates only, prepared as usual (every node then sits on
+// dependency level 0), and each node's data term b0 = sum_i w_i (d_i - mu)
+// and conditional deviation read back from the sweep tables.
+extern "C" int sgs_krige(const sgs_problem* problem, double* mean, double* var) {
+    if (!problem || !mean) return set_err(nullptr, SGS_ERR_ARG, "null argument");
+    sgs_plan* P = new sgs_plan();
+    auto fail = [&](int code) {
+        g_create_err = P->err.empty() ? g_create_err : P->err;
+        sgs_plan_destroy(P);
+        return code;
+    };
+    int rc = plan_init(P, problem);
+    if (rc != SGS_OK) return fail(rc);
+    const int64_t N = P->N;
+    if (P->D == 0) {  // no data: the prior (priormean, src/expectation/field/gaussian.jl:5-19)
+        for (int64_t g = 0; g < N; ++g) {
+            mean[g] = P->mean;
+            if (var) var[g] = P->vario.sill;
+        }
+        sgs_plan_destroy(P);
+        return SGS_OK;
+    }
+    P->warm_start = 0;
+    P->data_only = 1;
+    if ((rc = sgs_plan_prepare(P)) != SGS_OK) return fail(rc);
+    std::vector<int32_t> node(N);
+    std::vector<int8_t> st(N);
+    std::vector<double> b0(N), sd(N);
+    if (cudaMemcpy(st.data(), P->d_status, N, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(cuda_err(P, cudaGetLastError(), "status read-back"));
+    if (P->precision == SGS_PREC_FP64) {
+        if (cudaMemcpy(node.data(), P->t64.node, N * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(b0.data(), P->t64.b0, N * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(sd.data(), P->t64.sigma, N * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(cuda_err(P, cudaGetLastError(), "table read-back"));
+    } else {
+        std::vector<float> b2(2 * N), s2(2 * N);
+        if (cudaMemcpy(node.data(), P->t32.node, N * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(b2.data(), P->t32.b0, N * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(s2.data(), P->t32.sigma, N * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(cuda_err(P, cudaGetLastError(), "table read-back"));
+        for (int64_t p = 0; p < N; ++p) {
+            b0[p] = (double)b2[2 * p] + (double)b2[2 * p + 1];
+            sd[p] = (double)s2[2 * p] + (double)s2[2 * p + 1];
+        }
+    }
+    const double nan = std::nan("");
+    for (int64_t p = 0; p < N; ++p) {
+        const int32_t g = node[p];
+        const bool ok = st[g] == SGS_NODE_KRIGED;
+        mean[g] = ok ? P->mean + b0[p] : nan;
+        if (var) var[g] = ok ? sd[p] * sd[p] : nan;
+    }
+    sgs_plan_destroy(P);
     return SGS_OK;
 }

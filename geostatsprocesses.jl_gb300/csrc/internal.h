@@ -83,6 +83,7 @@ struct SearchArgs {
     int32_t* nbr;                // N x k, node-indexed
     int32_t* cnt;                // N
     int32_t* ngrid;              // N: grid neighbours among them
+    int data_only;               // 1: data candidates only (kriging from the data)
 };
 
 struct LevelArgs {

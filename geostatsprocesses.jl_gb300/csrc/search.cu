@@ -207,7 +207,8 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
         // ---- grid candidates from the sorted template ----
         int ng = 0;
         int before = 0;  // data strictly nearer than the current template entry
-        for (int base = 0; base < a.T && ng < k; base += 32) {
+        const int T = a.data_only ? 0 : a.T;
+        for (int base = 0; base < T && ng < k; base += 32) {
             // no template entry from here on can enter the k nearest once
             // ng grid + the data strictly nearer than this entry fill k; the
             // template keys do not decrease, so `before` only moves forward
@@ -220,7 +221,7 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
             const int j = base + lane;
             bool ok = false;
             int c = 0;
-            if (j < a.T) {
+            if (j < T) {
                 const TmplEntry e = a.tmpl[j];
                 const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
                 if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {

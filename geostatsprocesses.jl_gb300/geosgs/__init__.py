@@ -26,12 +26,13 @@ from .model import (
 )
 from .plan import Batch, Plan
 from .problem import build_problem, clamped_neighbors
-from .simulation import GPUSEQSIM, Ensemble, FieldSimulationMethod, preprocess, rand, randsingle
+from .simulation import (GPUSEQSIM, Ensemble, FieldSimulationMethod, expectedvalue, mean, posterior, preprocess,
+                         rand, randsingle)
 
 __all__ = [
     "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
     "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
-    "preprocess", "rand", "randsingle",
+    "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

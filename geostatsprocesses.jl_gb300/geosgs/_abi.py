@@ -186,6 +186,10 @@ EXPORTS = (
     "sgs_batch_info_get",
     "sgs_batch_destroy",
     "sgs_batch_last_error",
+    "sgs_krige",
+    "sgs_ensemble_stats",
+    "sgs_ensemble_cdf",
+    "sgs_ensemble_quantile",
 )
 
 _lib = None
@@ -270,6 +274,16 @@ def _declare(lib):
     lib.sgs_batch_destroy.restype = None
     lib.sgs_batch_last_error.argtypes = [P]
     lib.sgs_batch_last_error.restype = C.c_char_p
+    lib.sgs_krige.argtypes = [C.POINTER(SgsProblem), dp, dp]
+    lib.sgs_krige.restype = C.c_int
+    lib.sgs_ensemble_stats.argtypes = [P, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, P, P, P]
+    lib.sgs_ensemble_stats.restype = C.c_int
+    lib.sgs_ensemble_cdf.argtypes = [P, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, dp, C.c_int32,
+                                     C.c_int32, P, P]
+    lib.sgs_ensemble_cdf.restype = C.c_int
+    lib.sgs_ensemble_quantile.argtypes = [P, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, dp,
+                                          C.c_int32, P, P]
+    lib.sgs_ensemble_quantile.restype = C.c_int
     return lib
 
 

@@ -256,6 +256,13 @@ class RandomPath:
     def permutation(self, n: int):
         return np.random.Generator(np.random.PCG64(self.seed)).permutation(n).astype(np.int32)
 
+    def permutations(self, n: int, count: int):
+        """The first `count` permutations the path's generator draws, one
+        after another: what `traverse(domain, path)` yields on successive
+        realizations of the reference's randsingle (seqsim.jl:98)."""
+        gen = np.random.Generator(np.random.PCG64(self.seed))
+        return [gen.permutation(n).astype(np.int32) for _ in range(count)]
+
 
 class ExplicitPath:
     """A caller-given permutation of the grid nodes (0-based)."""

@@ -7,12 +7,20 @@ Ensemble                  src/ensembles.jl:10-52 (container + per-node mean/var)
 
 GPUSEQSIM carries SEQSIM's options (seqsim.jl:42-48: path, minneighbors,
 maxneighbors, neighborhood, distance) plus the GPU options (precision,
-refine_steps, warm_start, device).  The path is drawn once per `rand` call
-and shared by all realizations of that call: with it fixed, neighbour sets
-and kriging weights are the same for every realization, so `preprocess`
-computes them once on the GPU and the first `randsingle` simulates the whole
-block of realizations in one batched sweep; later calls hand out the
-remaining columns.
+refine_steps, warm_start, device).  By default the path is drawn once per
+`rand` call and shared by all realizations of that call: with it fixed,
+neighbour sets and kriging weights are the same for every realization, so
+`preprocess` computes them once on the GPU and the first `randsingle`
+simulates the whole block of realizations in one batched sweep; later calls
+hand out the remaining columns.  With `path_per_realization=True` and a
+RandomPath, each realization follows its own permutation, drawn one after
+another from the path's generator as the reference's
+`traverse(domain, path)` does on every realization (seqsim.jl:98): the
+realizations then run as a batch of independent problems (sgs_batch_*), one
+per realization, with their own neighbour tables and kriging systems.
+
+mean / expectedvalue / posterior   src/expectation/field.jl:17-42 and
+                                   src/expectation/field/gaussian.jl:5-25
 """
 from __future__ import annotations
 
@@ -21,8 +29,9 @@ from typing import Any
 
 import numpy as np
 
-from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, LinearPath
-from .plan import Plan
+from . import _abi
+from .model import ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess, GeoTable, LinearPath, RandomPath
+from .plan import Batch, Plan
 from .problem import build_problem
 
 
@@ -45,6 +54,7 @@ class GPUSEQSIM(FieldSimulationMethod):
     device: int = 0
     one_launch_sweep: bool = False  # all dependency levels in one cooperative launch
     level_sweep: bool = False       # one launch per dependency level (default: dataflow)
+    path_per_realization: bool = False  # RandomPath: a new permutation per realization
 
 
 class Ensemble:
@@ -74,13 +84,20 @@ class Ensemble:
 
 @dataclass
 class _Preproc:
-    plan: Plan
+    plan: Any
     var: str
     seed: int
     z: Any = None
     block: Any = None
     cursor: int = 0
     nreals: int = 1
+    batches: Any = None  # per-realization paths: [(Batch, first realization, count)]
+
+    def close(self):
+        if self.plan is not None:
+            self.plan.close()
+        for b, _, _ in self.batches or []:
+            b.close()
 
 
 def _varname(process, data):
@@ -95,17 +112,51 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     schedule and kriging solves (seqsim.jl:50-70 plus the hoisted search!/fit
     of seqsim.jl:107-131).  `init` is ignored like SEQSIM ignores it
     (seqsim.jl:267-271 always uses ExplicitInit with data appended)."""
+    seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
+    if method.path_per_realization and isinstance(method.path, RandomPath):
+        return _Preproc(plan=None, var=_varname(process, data), seed=seed, z=z, nreals=nreals,
+                        batches=_per_realization_batches(process, domain, data, method, nreals))
     problem, keep = build_problem(process, domain, data, method)
     plan = Plan(problem, keep).prepare()
-    seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
     return _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+
+
+# node budget of one batch of per-realization problems (about 500 bytes of
+# device tables per node)
+BATCH_NODES = 1 << 27
+
+
+def _per_realization_batches(process, domain, data, method, nreals):
+    """One problem per realization, each with its own permutation of the
+    RandomPath's generator, grouped into batches of at most BATCH_NODES."""
+    n = domain.nelements()
+    perms = method.path.permutations(n, nreals)
+    per = max(1, BATCH_NODES // max(1, n))
+    out = []
+    for r0 in range(0, nreals, per):
+        probs = []
+        for r in range(r0, min(nreals, r0 + per)):
+            m = GPUSEQSIM(**{**method.__dict__, "path": ExplicitPath(perms[r]), "path_per_realization": False})
+            probs.append(build_problem(process, domain, data, m))
+        out.append((Batch(probs).prepare(), r0, len(probs)))
+    return out
 
 
 def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc) -> dict:
     """One realization as {var: values} (seqsim.jl:72-156).  The first call
     simulates the whole block of `preproc.nreals` realizations on the GPU."""
     if preproc.block is None:
-        preproc.block = preproc.plan.simulate(preproc.nreals, z=preproc.z, seed=preproc.seed)
+        if preproc.batches is not None:
+            rows = []
+            for b, r0, cnt in preproc.batches:
+                z = None
+                if preproc.z is not None:
+                    zz = np.asarray(preproc.z, dtype=np.float64).reshape(preproc.nreals, -1)
+                    z = [zz[r0 + i: r0 + i + 1] for i in range(cnt)]
+                rows += [v[0] for v in b.simulate(1, z=z, seed=preproc.seed + r0)]
+            preproc.block = np.stack(rows)
+        else:
+            preproc.block = preproc.plan.simulate(preproc.nreals, z=preproc.z, seed=preproc.seed)
         preproc.cursor = 0
     if preproc.cursor >= preproc.block.shape[0]:
         raise ArgumentError("more realizations requested than the prepared block holds")
@@ -154,7 +205,60 @@ def rand(*args, data=None, method=None, init=None, workers=None, async_=False,
     try:
         reals = [randsingle(rng, process, smethod, domain, data, pre) for _ in range(n)]
     finally:
-        pre.plan.close()
+        pre.close()
     if nreals is None:
         return reals[0]
     return Ensemble(domain, reals)
+
+
+# ----------------------------------------------------------------- expectation
+@dataclass
+class _KrigingOptions:
+    """Neighbourhood of the posterior-mean prediction (GeoStatsModels
+    fitpredict's options: k nearest data, optionally inside a ball)."""
+
+    maxneighbors: int = 10
+    minneighbors: int = 1
+    neighborhood: Any = None
+    distance: str = "euclidean"
+    precision: str = "fp64"
+    refine_steps: int = 2
+    device: int = 0
+    path: Any = field(default_factory=LinearPath)
+
+
+def posterior(process: GaussianProcess, domain: CartesianGrid, data: GeoTable, *, maxneighbors: int = 10,
+              minneighbors: int = 1, neighborhood=None, precision: str = "fp64", device: int = 0):
+    """(mean, variance) of the process at every node conditioned on the data:
+    simple kriging (src/expectation/field/gaussian.jl:21-25), computed on the
+    GPU by sgs_krige; NaN where fewer than minneighbors data are found or the
+    system is singular."""
+    opts = _KrigingOptions(maxneighbors=maxneighbors, minneighbors=minneighbors, neighborhood=neighborhood,
+                           precision=precision, device=device)
+    problem, keep = build_problem(process, domain, data, opts)
+    lib = _abi.load_library()
+    n = domain.nelements()
+    m = np.empty(n, dtype=np.float64)
+    v = np.empty(n, dtype=np.float64)
+    import ctypes as C
+
+    _abi.check(lib, lib.sgs_krige(C.byref(problem), m.ctypes.data_as(C.POINTER(C.c_double)),
+                                  v.ctypes.data_as(C.POINTER(C.c_double))))
+    del keep
+    return m, v
+
+
+def mean(process: GaussianProcess, domain: CartesianGrid, *, data: GeoTable | None = None, init=None, **kwargs):
+    """mean(process, domain; data, init, kwargs...) (src/expectation/field.jl:
+    26-42): the prior mean without data (priormean), simple kriging from the
+    data otherwise (posteriormean); {var: values}."""
+    if data is None:
+        return {"field": np.full(domain.nelements(), float(process.mean))}
+    m, _ = posterior(process, domain, data, **kwargs)
+    return {_varname(process, data): m}
+
+
+def expectedvalue(process: GaussianProcess, domain: CartesianGrid, **kwargs):
+    """expectedvalue(process, domain; kwargs...) (src/expectation/field.jl:
+    5-23): the mean of a continuous analytical process."""
+    return mean(process, domain, **kwargs)

@@ -348,6 +348,41 @@ void sgs_batch_destroy(sgs_batch* batch);
  * sgs_batch_create on this thread when batch is NULL. */
 const char* sgs_batch_last_error(const sgs_batch* batch);
 
+/* ---- posterior mean (simple kriging from the data) ---------------------
+ * Mean and variance of the process at every grid node conditioned on the
+ * data alone: the reference's mean(process, domain; data) for a
+ * GaussianProcess, which is simple kriging (posteriormean,
+ * src/expectation/field/gaussian.jl:21-25, GeoStatsModels.fitpredict with
+ * Kriging(func, mean)).  Each node takes its problem->maxneighbors nearest
+ * data inside problem->search's neighbourhood (SGS_SEARCH_NEAREST: no
+ * radius; the path is not used), mean = mu + w'(d - mu), var = C(0) - w'c.
+ * Nodes with fewer than minneighbors data, or whose system is singular
+ * (pivot <= 1e-10 sill), get NaN (the reference's `missing`); with no data
+ * at all every node gets the prior: mu and the sill.  mean and var are host
+ * arrays of N (var may be NULL).  Errors: sgs_last_error(NULL). */
+int sgs_krige(const sgs_problem* problem, double* mean, double* var);
+
+/* ---- ensemble statistics on the device ----------------------------------
+ * Per-node statistics over nreals realizations held on the device in the
+ * node-major layout of sgs_plan_simulate_device / sgs_batch_simulate_device
+ * (rows of nreals values, row_stride elements apart; float when precision is
+ * SGS_PREC_FP32_REFINE, double for SGS_PREC_FP64); `offset` is added to every
+ * value (the process mean, as those values are centred).  Replaces the
+ * Ensemble statistics of src/ensembles.jl:42-52 (mean, var with the n - 1
+ * divisor, cdf, ccdf, quantile with linear interpolation between order
+ * statistics).  Outputs are device arrays: mean / var (N; either may be
+ * NULL), cdf (N x nx: fraction of values <= x[i], or > x[i] with complement
+ * = 1), quantile (N x np, p[i] in [0, 1], nreals <= 1024).  x and p are
+ * host arrays.  Nothing is allocated; stream is a cudaStream_t (NULL = the
+ * default stream) and the calls return after launching.  Errors:
+ * sgs_last_error(NULL). */
+int sgs_ensemble_stats(const void* vals, int32_t precision, int64_t nnodes, int32_t nreals, int32_t row_stride,
+                       double offset, double* mean, double* var, void* stream);
+int sgs_ensemble_cdf(const void* vals, int32_t precision, int64_t nnodes, int32_t nreals, int32_t row_stride,
+                     double offset, const double* x, int32_t nx, int32_t complement, double* out, void* stream);
+int sgs_ensemble_quantile(const void* vals, int32_t precision, int64_t nnodes, int32_t nreals, int32_t row_stride,
+                          double offset, const double* p, int32_t np, double* out, void* stream);
+
 /* ---- allocation-free schedule ------------------------------------------ */
 #define SGS_NOALLOC_MAX_LEVELS 262144
 

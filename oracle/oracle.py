@@ -45,6 +45,7 @@ def load():
     lib.oracle_search.argtypes = [P, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int]
     lib.oracle_solve.argtypes = [P, C.c_int64, C.c_int64, C.c_int64, C.c_int]
     lib.oracle_simulate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp, C.c_int64, C.c_int]
+    lib.oracle_krige.argtypes = [P, dp, dp, C.c_int]
     lib.oracle_neighbors.argtypes = [P, ip, ip]
     lib.oracle_weights.argtypes = [P, dp, dp, ip]
     lib.oracle_levels.argtypes = [P, ip, ip]
@@ -112,6 +113,13 @@ class OraclePlan:
         self._rc(self.lib.oracle_simulate(self.h, nreals, zp, seed, _dp(out),
                                           self.N if t_end is None else t_end, nthreads))
         return out
+
+    def krige(self, nthreads=0):
+        """Posterior (mean, var) by simple kriging from the data alone."""
+        m = np.empty(self.N, dtype=np.float64)
+        v = np.empty(self.N, dtype=np.float64)
+        self._rc(self.lib.oracle_krige(self.h, _dp(m), _dp(v), nthreads))
+        return m, v
 
     def neighbors(self):
         idx = np.empty((self.N, self.k), dtype=np.int32)

@@ -551,6 +551,54 @@ extern "C" int oracle_solve(oracle_plan* P, int64_t t0, int64_t t1, int64_t stri
 }
 
 // ---------------------------------------------------------------------------
+// Posterior mean of the process by simple kriging from the data alone
+// (src/expectation/field/gaussian.jl:21-25: GeoStatsModels.fitpredict with
+// Kriging(func, mean), restated): per node the k nearest data inside the
+// neighbourhood in canonical order, the same FP64 SK system and Cholesky as
+// solve_node, mean = mu + w'(d - mu), var = sill - w'c; NaN for fewer than
+// nmin data or a singular system; the prior (mu, sill) when there is no data.
+extern "C" int oracle_krige(oracle_plan* P, double* mean, double* var, int nthreads) {
+    if (!P || !mean) return fail(SGS_ERR_ARG, "null argument");
+    const double nan = std::nan("");
+    if (P->D == 0) {
+        for (int64_t g = 0; g < P->N; ++g) {
+            mean[g] = P->mean;
+            if (var) var[g] = P->vario.sill;
+        }
+        return SGS_OK;
+    }
+    const int k = P->nmax;
+    const int nt = nthreads_or_all(nthreads);
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<Cand> data;
+        std::vector<double> K, c;
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t g = 0; g < P->N; ++g) {
+            data_candidates(P, g, false, data);
+            int32_t* nb = &P->nbr[(size_t)g * k];
+            int m = 0;
+            for (; m < k && m < (int)data.size(); ++m) nb[m] = (int32_t)data[m].idx;
+            for (int q = m; q < k; ++q) nb[q] = -1;
+            P->cnt[g] = m;
+            P->searched[g] = 1;
+            solve_node(P, g, K, c);
+            if (P->status[g] != SGS_NODE_KRIGED) {
+                mean[g] = nan;
+                if (var) var[g] = nan;
+                continue;
+            }
+            const double* w = &P->w[(size_t)g * k];
+            double s = 0.0;
+            for (int a = 0; a < m; ++a) s += w[a] * (P->dval[nb[a] - P->N] - P->mean);
+            mean[g] = P->mean + s;
+            if (var) var[g] = P->sigma[g] * P->sigma[g];
+        }
+    }
+    return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw 2011, "Parallel random numbers:
 // as easy as 1, 2, 3") and the Box-Muller transform; the seeded draws of the
 // library follow the same definition.

@@ -54,6 +54,10 @@ int oracle_solve(oracle_plan* plan, int64_t t_begin, int64_t t_end, int64_t stri
 int oracle_simulate(oracle_plan* plan, int32_t nreals, const double* z, uint64_t seed,
                     double* out, int64_t t_end, int nthreads);
 
+/* Posterior mean and variance by simple kriging from the data alone, every
+ * grid node (NaN where the reference's prediction is missing). */
+int oracle_krige(oracle_plan* plan, double* mean, double* var, int nthreads);
+
 int oracle_neighbors(const oracle_plan* plan, int32_t* idx, int32_t* count);
 int oracle_weights(const oracle_plan* plan, double* weights, double* sigma, int32_t* status);
 int oracle_levels(const oracle_plan* plan, int32_t* level, int32_t* nlevels);
