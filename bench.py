@@ -607,7 +607,9 @@ def main():
                 ", levels %d-%d by per-level launches" % (sc["level_lo"], sc["level_hi"] - 1)
                 if sc["level_hi"] > sc["level_lo"] else ""),
             1: "sweep_all_kernel (one cooperative launch)",
-            2: "sweep_level_kernel (one launch per level)"}[sc["mode"]]
+            2: ("sweep_levelN_kernel<%d> (one launch per level, %d chunks of 4 realizations per thread)"
+                % (sc["lanes_g"], sc["lanes_g"]) if sc["lanes_g"] in (2, 4)
+                else "sweep_level_kernel (one launch per level)")}[sc["mode"]]
     roofline = {"kernel": form + ": all launches of one sweep", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_src, "traffic": traffic,

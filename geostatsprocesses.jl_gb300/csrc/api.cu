@@ -849,7 +849,7 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
             if (P->precision == SGS_PREC_FP64)
                 e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
             else
-                e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st);
+                e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g);
             if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
             if (p1 > p0) P->info.launches++;
         }
@@ -867,7 +867,7 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         if (P->precision == SGS_PREC_FP64)
             e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
         else
-            e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st);
+            e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g);
         if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
         if (p1 > p0) P->info.launches++;
     }
@@ -1061,6 +1061,8 @@ extern "C" int sgs_plan_set_sweep(sgs_plan* P, const sgs_sweep_config* c) {
          c->lanes_g > 2 || c->lanes_w < 0 || c->lanes_w > 32 || (c->lanes_w & (c->lanes_w - 1)) ||
          c->level_lo < 0 || c->level_hi < 0 || c->tight < 0 || c->tight > 1))
         return set_err(P, SGS_ERR_ARG, "invalid dataflow sweep parameters");
+    if (c->mode == SGS_SWEEP_LEVELS && (c->lanes_g < 0 || c->lanes_g > 4 || c->lanes_g == 3))
+        return set_err(P, SGS_ERR_ARG, "invalid per-level sweep parameters (lanes_g 0, 1, 2 or 4)");
     P->sweep = *c;
     if (P->sweep.chunk < 1) P->sweep.chunk = 1;
     return SGS_OK;
@@ -1110,6 +1112,9 @@ extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* cho
     int p2 = 1;
     while (p2 < cpn && p2 < 32) p2 <<= 1;
     rc = run({SGS_SWEEP_LEVELS, 1, 0, 1, 0, 0, 0, 0, 0.f});
+    // per-level launches with 2 or 4 chunks of 4 realizations per thread
+    for (int G = 2; !rc && !fp64 && G <= 4 && cpn > 16 && Rp % (4 * G) == 0; G *= 2)
+        rc = run({SGS_SWEEP_LEVELS, 1, 0, G, 0, 0, 0, 0, 0.f});
     for (int W = p2; !rc && W >= std::max(1, p2 / 4); W >>= 1)
         for (int G = 1; !rc && G <= (cpn >= 2 * W ? 2 : 1); ++G)
             for (int tight = 0; !rc && tight <= 1; ++tight)

@@ -218,8 +218,11 @@ cudaError_t launch_solve_fp64_batch(int kl, const SolveArgs* doms, const int64_t
 cudaError_t launch_solve_fp64_into_fp32_batch(int kl, const SolveArgs* doms, const int64_t* noff, int ndom,
                                               const int32_t* order, const int32_t* list, const int32_t* desc,
                                               const SweepTables<float>& t, int nsm, cudaStream_t s);
+// pairs = 2 or 4: one thread per 2 or 4 chunks of 4 realizations (rows of a
+// multiple of 8 or 16 realizations, more than 64 of them); otherwise one
+// thread per chunk
 cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp,
-                              const float* z, uint64_t seed, float* V, cudaStream_t s);
+                              const float* z, uint64_t seed, float* V, cudaStream_t s, int pairs = 1);
 cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
                               const double* z, uint64_t seed, double* V, cudaStream_t s);
 // all levels in one cooperative launch (loff: device level offsets, nlevels + 1)

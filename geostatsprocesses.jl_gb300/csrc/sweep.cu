@@ -131,6 +131,60 @@ __device__ __forceinline__ void sweep_item_fp64(const SweepTables<double>& t, in
     store_d4(V + (int64_t)g * Rp + 4 * ch, acc);
 }
 
+// CH consecutive chunks of 4 realizations (ch .. ch + CH - 1 < cpn) of one
+// node, FP32: CH independent row loads per neighbour in flight per thread.
+template <int CH>
+__device__ __forceinline__ void sweep_itemN_fp32(const SweepTables<float>& t, int k, int64_t pos, int ch, int Rp,
+                                                 const float* __restrict__ z, uint64_t seed, float* __restrict__ V) {
+    const int g = t.node[pos];
+    const int m = t.m[pos];
+    const float2 b0 = reinterpret_cast<const float2*>(t.b0)[pos];
+    Dot2 a[4 * CH];
+#pragma unroll
+    for (int q = 0; q < 4 * CH; ++q) a[q].init(b0.x, b0.y);
+    const int32_t* idx = t.idx + pos * k;
+    const float2* w = reinterpret_cast<const float2*>(t.w) + pos * k;
+#pragma unroll 4
+    for (int j = 0; j < m; ++j) {
+        const float* row = V + (int64_t)idx[j] * Rp + 4 * ch;
+        float4 v[CH];
+#pragma unroll
+        for (int h = 0; h < CH; ++h) v[h] = Vec4<float>::load(row + 4 * h);
+        const float2 wj = w[j];
+#pragma unroll
+        for (int h = 0; h < CH; ++h) {
+            a[4 * h + 0].add(wj.x, wj.y, v[h].x);
+            a[4 * h + 1].add(wj.x, wj.y, v[h].y);
+            a[4 * h + 2].add(wj.x, wj.y, v[h].z);
+            a[4 * h + 3].add(wj.x, wj.y, v[h].w);
+        }
+    }
+    const float2 sg = reinterpret_cast<const float2*>(t.sigma)[pos];
+#pragma unroll
+    for (int h = 0; h < CH; ++h) {
+        const float4 zz = z ? Vec4<float>::load(z + (int64_t)g * Rp + 4 * (ch + h)) : normals4(seed, g, ch + h);
+        a[4 * h + 0].add(sg.x, sg.y, zz.x);
+        a[4 * h + 1].add(sg.x, sg.y, zz.y);
+        a[4 * h + 2].add(sg.x, sg.y, zz.z);
+        a[4 * h + 3].add(sg.x, sg.y, zz.w);
+        Vec4<float>::store(V + (int64_t)g * Rp + 4 * (ch + h),
+                           make_float4(a[4 * h].value(), a[4 * h + 1].value(), a[4 * h + 2].value(), a[4 * h + 3].value()));
+    }
+}
+
+// One level per launch, FP32, rows of a multiple of CH chunks: one thread
+// per (node, CH consecutive chunks).
+template <int CH>
+__global__ void __launch_bounds__(256) sweep_levelN_kernel(const SweepTables<float> t, int k, int64_t p0, int64_t p1,
+                                                           int Rp, const float* __restrict__ z, uint64_t seed,
+                                                           float* __restrict__ V) {
+    const int cpg = Rp / (4 * CH);  // chunk groups per node
+    const int64_t total = (p1 - p0) * cpg;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x)
+        sweep_itemN_fp32<CH>(t, k, p0 + i / cpg, CH * (int)(i % cpg), Rp, z, seed, V);
+}
+
 // One level per launch: one thread per (node, chunk of 4 realizations).
 template <typename T>
 __global__ void __launch_bounds__(256) sweep_level_kernel(const SweepTables<T> t, int k, int64_t p0, int64_t p1, int Rp,
@@ -292,7 +346,16 @@ static cudaError_t sweep_level(const SweepTables<T>& t, int k, int64_t p0, int64
 }
 
 cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp, const float* z,
-                              uint64_t seed, float* V, cudaStream_t s) {
+                              uint64_t seed, float* V, cudaStream_t s, int pairs) {
+    // pairs: chunks of 4 realizations per thread (1, 2 or 4)
+    if ((pairs == 2 || pairs == 4) && Rp % (4 * pairs) == 0 && !use_warp_sweep(Rp)) {
+        if (p1 <= p0) return cudaSuccess;
+        if (pairs == 2)
+            sweep_levelN_kernel<2><<<sweep_blocks((p1 - p0) * (Rp / 8)), 256, 0, s>>>(t, k, p0, p1, Rp, z, seed, V);
+        else
+            sweep_levelN_kernel<4><<<sweep_blocks((p1 - p0) * (Rp / 16)), 256, 0, s>>>(t, k, p0, p1, Rp, z, seed, V);
+        return cudaGetLastError();
+    }
     return sweep_level<float>(t, k, p0, p1, Rp, z, seed, V, s);
 }
 

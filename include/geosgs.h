@@ -246,7 +246,10 @@ typedef struct sgs_sweep_config {
     int32_t mode;             /* SGS_SWEEP_*                                         */
     int32_t chunk;            /* flow: work items a warp takes per ticket            */
     int32_t blocks_per_sm;    /* flow: resident 256-thread blocks per SM (0 = max)   */
-    int32_t lanes_g;          /* flow: chunks of 4 realizations per lane, 1 or 2     */
+    int32_t lanes_g;          /* flow: chunks of 4 realizations per lane, 1 or 2;
+                                 levels (FP32, more than 64 realizations, a
+                                 multiple of 4 * lanes_g): 2 or 4 chunks per
+                                 thread                                        */
     int32_t lanes_w;          /* flow: lanes per slice of the neighbour list, a power
                                  of two <= 32 (0 = the row's chunks, at most 32);
                                  32 / lanes_w slices split the neighbour list and a

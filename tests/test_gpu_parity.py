@@ -208,6 +208,8 @@ SWEEP_FORMS = [
     dict(mode=_abi.SGS_SWEEP_FLOW, level_lo=5, level_hi=12),           # dataflow, per-level, dataflow
     dict(mode=_abi.SGS_SWEEP_FLOW, level_lo=0, level_hi=10 ** 6),      # every level by per-level launches
     dict(mode=_abi.SGS_SWEEP_LEVELS),
+    dict(mode=_abi.SGS_SWEEP_LEVELS, lanes_g=2),                       # two chunks per thread (R > 64)
+    dict(mode=_abi.SGS_SWEEP_LEVELS, lanes_g=4),                       # four chunks per thread
     dict(mode=_abi.SGS_SWEEP_COOPERATIVE),
 ]
 
