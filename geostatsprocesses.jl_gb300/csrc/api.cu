@@ -79,7 +79,7 @@ struct sgs_plan {
     int32_t* d_done = nullptr;    // dataflow sweep: per-node epoch flags
     unsigned long long* d_flow = nullptr;  // dataflow sweep: ticket, error flag
     int32_t flow_epoch = 0;
-    sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0.f};
+    sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0, 0.f};
     int64_t done_cap = 0;         // flags allocated in d_done (pieces x N)
     int last_sweep_mode = SGS_SWEEP_FLOW;  // mode of the last sweep launched
     int data_only = 0;            // neighbours from the data alone (sgs_krige)
@@ -849,7 +849,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
             if (P->precision == SGS_PREC_FP64)
                 e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
             else
-                e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g);
+                e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g,
+                                      (p1 - p0) < (int64_t)c.split_nodes);
             if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
             if (p1 > p0) P->info.launches++;
         }
@@ -867,7 +868,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         if (P->precision == SGS_PREC_FP64)
             e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
         else
-            e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g);
+            e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g,
+                                  (p1 - p0) < (int64_t)c.split_nodes);
         if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
         if (p1 > p0) P->info.launches++;
     }
@@ -1059,10 +1061,10 @@ extern "C" int sgs_plan_set_sweep(sgs_plan* P, const sgs_sweep_config* c) {
     if (c->mode == SGS_SWEEP_FLOW &&
         (c->chunk < 0 || c->chunk > 64 || c->blocks_per_sm < 0 || c->blocks_per_sm > 32 || c->lanes_g < 0 ||
          c->lanes_g > 2 || c->lanes_w < 0 || c->lanes_w > 32 || (c->lanes_w & (c->lanes_w - 1)) ||
-         c->level_lo < 0 || c->level_hi < 0 || c->tight < 0 || c->tight > 1))
+         c->level_lo < 0 || c->level_hi < 0 || c->tight < 0 || c->tight > 1 || c->split_nodes < 0))
         return set_err(P, SGS_ERR_ARG, "invalid dataflow sweep parameters");
-    if (c->mode == SGS_SWEEP_LEVELS && (c->lanes_g < 0 || c->lanes_g > 4 || c->lanes_g == 3))
-        return set_err(P, SGS_ERR_ARG, "invalid per-level sweep parameters (lanes_g 0, 1, 2 or 4)");
+    if (c->mode == SGS_SWEEP_LEVELS && (c->lanes_g < 0 || c->lanes_g > 4 || c->lanes_g == 3 || c->split_nodes < 0))
+        return set_err(P, SGS_ERR_ARG, "invalid per-level sweep parameters (lanes_g 0, 1, 2 or 4, split_nodes >= 0)");
     P->sweep = *c;
     if (P->sweep.chunk < 1) P->sweep.chunk = 1;
     return SGS_OK;
@@ -1111,16 +1113,28 @@ extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* cho
     // stage 1: per-level launches and whole-sweep dataflow mappings
     int p2 = 1;
     while (p2 < cpn && p2 < 32) p2 <<= 1;
-    rc = run({SGS_SWEEP_LEVELS, 1, 0, 1, 0, 0, 0, 0, 0.f});
+    rc = run({SGS_SWEEP_LEVELS, 1, 0, 1, 0, 0, 0, 0, 0, 0.f});
     // per-level launches with 2 or 4 chunks of 4 realizations per thread
     for (int G = 2; !rc && !fp64 && G <= 4 && cpn > 16 && Rp % (4 * G) == 0; G *= 2)
-        rc = run({SGS_SWEEP_LEVELS, 1, 0, G, 0, 0, 0, 0, 0.f});
+        rc = run({SGS_SWEEP_LEVELS, 1, 0, G, 0, 0, 0, 0, 0, 0.f});
+    // the best per-level form with small levels split over a block's warps
+    if (!rc && !fp64 && Rp % 8 == 0) {
+        int bl = -1;
+        for (int i = 0; i < (int)done.size(); ++i)
+            if (done[i].mode == SGS_SWEEP_LEVELS && (bl < 0 || done[i].ms < done[bl].ms)) bl = i;
+        for (int thr : {256, 1024, 4096, 16384}) {
+            if (rc || bl < 0) break;
+            sgs_sweep_config c = done[bl];
+            c.split_nodes = thr;
+            rc = run(c);
+        }
+    }
     for (int W = p2; !rc && W >= std::max(1, p2 / 4); W >>= 1)
         for (int G = 1; !rc && G <= (cpn >= 2 * W ? 2 : 1); ++G)
             for (int tight = 0; !rc && tight <= 1; ++tight)
                 for (int chunk : {1, 2}) {
                     if (rc) break;
-                    rc = run({SGS_SWEEP_FLOW, chunk, 0, G, W, 0, 0, tight, 0.f});
+                    rc = run({SGS_SWEEP_FLOW, chunk, 0, G, W, 0, 0, tight, 0, 0.f});
                 }
     // stage 2: the best dataflow mapping, with the span of large levels
     // (from the first to the last level holding at least `thr` nodes) swept
@@ -1144,6 +1158,36 @@ extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* cho
             c.level_lo = lo;
             c.level_hi = hi;
             if ((rc = run(c))) break;
+        }
+    }
+    // stage 3: the small leading levels (a long chain of levels holding few
+    // nodes) by one dataflow launch whose lanes split each neighbour list
+    // (W lanes per slice, 32 / W slices), every level from the first one
+    // holding at least `thr` nodes by the best per-level form
+    if (!rc && !fp64) {
+        int bl = -1;
+        for (int i = 0; i < (int)done.size(); ++i)
+            if (done[i].mode == SGS_SWEEP_LEVELS && (bl < 0 || done[i].ms < done[bl].ms)) bl = i;
+        int last_lo = -1;
+        for (int64_t thr : {(int64_t)P->nsm * 2, (int64_t)P->nsm * 8, (int64_t)P->nsm * 32}) {
+            int lo = -1;
+            for (int l = 0; l < P->nlevels && lo < 0; ++l)
+                if (P->h_loff[l + 1] - P->h_loff[l] >= thr) lo = l;
+            if (bl < 0 || lo <= 0 || lo == last_lo) continue;
+            last_lo = lo;
+            for (int W : {2, 4, 8}) {
+                if (rc || W > p2) break;
+                sgs_sweep_config c = done[bl];
+                c.mode = SGS_SWEEP_FLOW;
+                c.chunk = 1;
+                c.lanes_w = W;
+                c.level_lo = lo;
+                c.level_hi = P->nlevels;
+                // the per-level part keeps the best per-level form; the
+                // dataflow part takes 2 chunks per lane only when they fit
+                if (c.lanes_g > 2 || cpn < 2 * W) c.lanes_g = 1;
+                rc = run(c);
+            }
         }
     }
     dfree(P, V);

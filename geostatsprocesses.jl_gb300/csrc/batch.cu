@@ -373,7 +373,7 @@ struct sgs_batch {
     int sweep_Rp = 0;
     void* sweep_V = nullptr;
     cudaStream_t sweep_stream = nullptr;
-    sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0.f};
+    sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0, 0.f};
     bool sweep_graph_valid = false;
     bool sweep_pending = false;    // a device-resident sweep not yet checked
     sgs_batch_info info{};
@@ -1114,7 +1114,7 @@ extern "C" int sgs_batch_set_sweep(sgs_batch* B, const sgs_sweep_config* c) {
         c->tight > 1)
         return berr(B, SGS_ERR_ARG, "invalid dataflow sweep parameters");
     B->sweep = *c;
-    B->sweep.level_lo = B->sweep.level_hi = 0;
+    B->sweep.level_lo = B->sweep.level_hi = B->sweep.split_nodes = 0;
     if (B->sweep.chunk < 1) B->sweep.chunk = 1;
     B->sweep_graph_valid = false;
     return SGS_OK;
@@ -1162,7 +1162,7 @@ extern "C" int sgs_batch_tune_sweep(sgs_batch* B, int32_t R, sgs_sweep_config* c
             for (int tight = 0; !rc && tight <= 1; ++tight)
                 for (int chunk : {1, 2}) {
                     if (rc) break;
-                    rc = time_one({SGS_SWEEP_FLOW, chunk, 0, G, W, 0, 0, tight, 0.f});
+                    rc = time_one({SGS_SWEEP_FLOW, chunk, 0, G, W, 0, 0, tight, 0, 0.f});
                 }
     bfree(B, V);
     if (rc || best < 0) {

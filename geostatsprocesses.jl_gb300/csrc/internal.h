@@ -220,9 +220,11 @@ cudaError_t launch_solve_fp64_into_fp32_batch(int kl, const SolveArgs* doms, con
                                               const SweepTables<float>& t, int nsm, cudaStream_t s);
 // pairs = 2 or 4: one thread per 2 or 4 chunks of 4 realizations (rows of a
 // multiple of 8 or 16 realizations, more than 64 of them); otherwise one
-// thread per chunk
+// thread per chunk.  split = 1 (rows of a multiple of 8 realizations): one
+// block per node, the neighbour list split over its warps (small levels).
 cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp,
-                              const float* z, uint64_t seed, float* V, cudaStream_t s, int pairs = 1);
+                              const float* z, uint64_t seed, float* V, cudaStream_t s, int pairs = 1,
+                              int split = 0);
 cudaError_t launch_sweep_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
                               const double* z, uint64_t seed, double* V, cudaStream_t s);
 // all levels in one cooperative launch (loff: device level offsets, nlevels + 1)

@@ -67,6 +67,13 @@ struct Dot2 {
     __device__ __forceinline__ float value() const { return __fadd_rn(s, c); }
 };
 
+// Adds another compensated sum (s2, c2) to a (TwoSum of the leading parts).
+__device__ __forceinline__ void dot2_merge(Dot2& a, float s2, float c2) {
+    const DF t = df_two_sum(a.s, s2);
+    a.s = t.hi;
+    a.c = __fadd_rn(a.c, __fadd_rn(c2, t.lo));
+}
+
 // Update one node's chunk of 4 realizations (FP32 values, compensated sum).
 __device__ __forceinline__ void sweep_item_fp32(const SweepTables<float>& t, int k, int64_t pos, int ch, int Rp,
                                                 const float* __restrict__ z, uint64_t seed, float* __restrict__ V) {
@@ -185,6 +192,80 @@ __global__ void __launch_bounds__(256) sweep_levelN_kernel(const SweepTables<flo
         sweep_itemN_fp32<CH>(t, k, p0 + i / cpg, CH * (int)(i % cpg), Rp, z, seed, V);
 }
 
+// One level per launch for levels of few nodes (FP32, rows of a multiple of
+// 8 realizations): one block per node, its SPLIT_WARPS warps splitting the
+// node's neighbour list (warp s takes every SPLIT_WARPS-th neighbour from
+// s), each lane 2 chunks of 4 realizations (64 chunks per pass over the
+// row), so each thread's chain of dependent row loads is SPLIT_WARPS times
+// shorter; warp 0 merges the warps' compensated partial sums (error-free
+// TwoSum merges) from shared memory, adds b0 and sigma z and stores.
+constexpr int SPLIT_WARPS = 8;
+
+__global__ void __launch_bounds__(SPLIT_WARPS * 32) sweep_split_kernel(const SweepTables<float> t, int k, int64_t p0,
+                                                                       int64_t p1, int Rp, const float* __restrict__ z,
+                                                                       uint64_t seed, float* __restrict__ V) {
+    __shared__ float2 part[SPLIT_WARPS - 1][8][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int cpn = Rp >> 2;
+    for (int64_t pos = p0 + blockIdx.x; pos < p1; pos += gridDim.x) {
+        const int g = t.node[pos];
+        const int m = t.m[pos];
+        const int32_t* idx = t.idx + pos * k;
+        const float2* w = reinterpret_cast<const float2*>(t.w) + pos * k;
+        for (int c0 = 0; c0 < cpn; c0 += 64) {
+            const int ch = c0 + 2 * lane;  // chunks ch and ch + 1 (cpn is even)
+            const bool act = ch < cpn;
+            Dot2 a[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) a[q].init(0.f, 0.f);
+            if (act) {
+#pragma unroll 2
+                for (int j = wid; j < m; j += SPLIT_WARPS) {
+                    const float* row = V + (int64_t)idx[j] * Rp + 4 * ch;
+                    const float4 v0 = Vec4<float>::load(row);
+                    const float4 v1 = Vec4<float>::load(row + 4);
+                    const float2 wj = w[j];
+                    a[0].add(wj.x, wj.y, v0.x);
+                    a[1].add(wj.x, wj.y, v0.y);
+                    a[2].add(wj.x, wj.y, v0.z);
+                    a[3].add(wj.x, wj.y, v0.w);
+                    a[4].add(wj.x, wj.y, v1.x);
+                    a[5].add(wj.x, wj.y, v1.y);
+                    a[6].add(wj.x, wj.y, v1.z);
+                    a[7].add(wj.x, wj.y, v1.w);
+                }
+            }
+            if (wid > 0)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) part[wid - 1][q][lane] = make_float2(a[q].s, a[q].c);
+            __syncthreads();
+            if (wid == 0 && act) {
+#pragma unroll 1
+                for (int s = 0; s < SPLIT_WARPS - 1; ++s)
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) dot2_merge(a[q], part[s][q][lane].x, part[s][q][lane].y);
+                const float2 b0 = reinterpret_cast<const float2*>(t.b0)[pos];
+                const float2 sg = reinterpret_cast<const float2*>(t.sigma)[pos];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float4 zz =
+                        z ? Vec4<float>::load(z + (int64_t)g * Rp + 4 * (ch + h)) : normals4(seed, g, ch + h);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) dot2_merge(a[4 * h + q], b0.x, b0.y);
+                    a[4 * h + 0].add(sg.x, sg.y, zz.x);
+                    a[4 * h + 1].add(sg.x, sg.y, zz.y);
+                    a[4 * h + 2].add(sg.x, sg.y, zz.z);
+                    a[4 * h + 3].add(sg.x, sg.y, zz.w);
+                    Vec4<float>::store(V + (int64_t)g * Rp + 4 * (ch + h),
+                                       make_float4(a[4 * h].value(), a[4 * h + 1].value(), a[4 * h + 2].value(),
+                                                   a[4 * h + 3].value()));
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // One level per launch: one thread per (node, chunk of 4 realizations).
 template <typename T>
 __global__ void __launch_bounds__(256) sweep_level_kernel(const SweepTables<T> t, int k, int64_t p0, int64_t p1, int Rp,
@@ -228,11 +309,6 @@ __global__ void __launch_bounds__(256) sweep_all_kernel(const SweepTables<T> t, 
 // chunk walking all neighbours (the small levels are latency-bound); the S
 // partial sums are then combined across lanes (error-free for the
 // compensated FP32 sums).
-__device__ __forceinline__ void dot2_merge(Dot2& a, float s2, float c2) {
-    const DF t = df_two_sum(a.s, s2);
-    a.s = t.hi;
-    a.c = __fadd_rn(a.c, __fadd_rn(c2, t.lo));
-}
 
 template <typename T>
 __global__ void __launch_bounds__(256) sweep_warp_kernel(const SweepTables<T> t, int k, int64_t p0, int64_t p1, int Rp,
@@ -346,8 +422,16 @@ static cudaError_t sweep_level(const SweepTables<T>& t, int k, int64_t p0, int64
 }
 
 cudaError_t launch_sweep_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp, const float* z,
-                              uint64_t seed, float* V, cudaStream_t s, int pairs) {
-    // pairs: chunks of 4 realizations per thread (1, 2 or 4)
+                              uint64_t seed, float* V, cudaStream_t s, int pairs, int split) {
+    // pairs: chunks of 4 realizations per thread (1, 2 or 4); split: one
+    // block per node with the neighbour list split over its warps
+    if (split && Rp % 8 == 0) {
+        if (p1 <= p0) return cudaSuccess;
+        const int64_t nodes = p1 - p0;
+        sweep_split_kernel<<<(unsigned)std::min<int64_t>(nodes, 1 << 20), SPLIT_WARPS * 32, 0, s>>>(t, k, p0, p1, Rp,
+                                                                                                   z, seed, V);
+        return cudaGetLastError();
+    }
     if ((pairs == 2 || pairs == 4) && Rp % (4 * pairs) == 0 && !use_warp_sweep(Rp)) {
         if (p1 <= p0) return cudaSuccess;
         if (pairs == 2)

@@ -96,6 +96,7 @@ class SgsSweepConfig(C.Structure):
         ("level_lo", C.c_int32),
         ("level_hi", C.c_int32),
         ("tight", C.c_int32),
+        ("split_nodes", C.c_int32),
         ("ms", C.c_float),
     ]
 

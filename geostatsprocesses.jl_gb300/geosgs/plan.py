@@ -34,7 +34,7 @@ class Plan:
         self.prepared = False
         self._sweep = _abi.SgsSweepConfig(2 if problem.flags & _abi.SGS_FLAG_LEVEL_SWEEP else
                                           1 if problem.flags & _abi.SGS_FLAG_ONE_LAUNCH_SWEEP else 0,
-                                          1, 0, 1, 0, 0, 0, 0, 0.0).as_dict()
+                                          1, 0, 1, 0, 0, 0, 0, 0, 0.0).as_dict()
 
     def close(self):
         if getattr(self, "h", None):
@@ -101,11 +101,12 @@ class Plan:
         return self
 
     def set_sweep(self, mode=_abi.SGS_SWEEP_FLOW, chunk=1, blocks_per_sm=0, lanes_g=1, lanes_w=0, level_lo=0,
-                  level_hi=0, tight=0, **_ignored):
+                  level_hi=0, tight=0, split_nodes=0, **_ignored):
         """How simulate() runs the sweep (SGS_SWEEP_* mode and dataflow
         mapping; see sgs_sweep_config).  Accepts a dict returned by
         tune_sweep() as keyword arguments."""
-        c = _abi.SgsSweepConfig(mode, chunk, blocks_per_sm, lanes_g, lanes_w, level_lo, level_hi, tight, 0.0)
+        c = _abi.SgsSweepConfig(mode, chunk, blocks_per_sm, lanes_g, lanes_w, level_lo, level_hi, tight, split_nodes,
+                                0.0)
         self._check(self.lib.sgs_plan_set_sweep(self.h, C.byref(c)))
         self._sweep = c.as_dict()
         return self
@@ -222,7 +223,7 @@ class Batch:
         return w, s, st
 
     def set_sweep(self, chunk=1, blocks_per_sm=0, lanes_g=1, lanes_w=0, tight=0, **_ignored):
-        c = _abi.SgsSweepConfig(_abi.SGS_SWEEP_FLOW, chunk, blocks_per_sm, lanes_g, lanes_w, 0, 0, tight, 0.0)
+        c = _abi.SgsSweepConfig(_abi.SGS_SWEEP_FLOW, chunk, blocks_per_sm, lanes_g, lanes_w, 0, 0, tight, 0, 0.0)
         self._check(self.lib.sgs_batch_set_sweep(self.h, C.byref(c)))
         return self
 

@@ -260,6 +260,10 @@ typedef struct sgs_sweep_config {
                                  after them by one dataflow launch each             */
     int32_t tight;            /* flow: 1 = the kernel variant compiled for higher
                                  residency (register cap)                           */
+    int32_t split_nodes;      /* levels (FP32, rows of a multiple of 8 realizations):
+                                 levels of fewer nodes than this take one block per
+                                 node, its 8 warps splitting the neighbour list
+                                 (0 = never)                                       */
     float   ms;               /* sgs_plan_tune_sweep: measured time of this config   */
 } sgs_sweep_config;
 

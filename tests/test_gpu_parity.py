@@ -210,6 +210,9 @@ SWEEP_FORMS = [
     dict(mode=_abi.SGS_SWEEP_LEVELS),
     dict(mode=_abi.SGS_SWEEP_LEVELS, lanes_g=2),                       # two chunks per thread (R > 64)
     dict(mode=_abi.SGS_SWEEP_LEVELS, lanes_g=4),                       # four chunks per thread
+    dict(mode=_abi.SGS_SWEEP_LEVELS, lanes_g=2, split_nodes=40),       # small levels: block per node
+    dict(mode=_abi.SGS_SWEEP_LEVELS, split_nodes=1 << 30),             # every level: block per node
+    dict(mode=_abi.SGS_SWEEP_FLOW, lanes_w=2, lanes_g=2, level_lo=6, level_hi=10 ** 6, split_nodes=30),
     dict(mode=_abi.SGS_SWEEP_COOPERATIVE),
 ]
 

@@ -62,6 +62,8 @@ int main(void){
    offsetof(sgs_problem, mean), offsetof(sgs_problem, ball), offsetof(sgs_problem, path),
    offsetof(sgs_problem, flags), sizeof(sgs_info), offsetof(sgs_info, ms_sweep),
    sizeof(sgs_sweep_config), offsetof(sgs_sweep_config, ms));
+ printf("%zu %zu %zu\n", sizeof(sgs_batch_info), offsetof(sgs_batch_info, ms_search),
+   offsetof(sgs_batch_info, device_bytes));
  return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -70,9 +72,10 @@ int main(void){
         exe = os.path.join(d, "p")
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
-    P, I, W = _abi.SgsProblem, _abi.SgsInfo, _abi.SgsSweepConfig
+    P, I, W, B = _abi.SgsProblem, _abi.SgsInfo, _abi.SgsSweepConfig, _abi.SgsBatchInfo
     want = [C.sizeof(P), P.variogram.offset, P.mean.offset, P.ball.offset, P.path.offset, P.flags.offset,
-            C.sizeof(I), I.ms_sweep.offset, C.sizeof(W), W.ms.offset]
+            C.sizeof(I), I.ms_sweep.offset, C.sizeof(W), W.ms.offset, C.sizeof(B), B.ms_search.offset,
+            B.device_bytes.offset]
     assert got == want
 
 
