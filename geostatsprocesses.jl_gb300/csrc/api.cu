@@ -419,6 +419,9 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
             }
         }
         m.bound_f = (float)((m.kind == METRIC_ISO ? m.rr : 1.0) * (1.0 + 1e-3) + slack);
+        if (m.kind == METRIC_NEAREST) m.bound_f = INFINITY;
+        m.slack_f = (float)slack;
+        m.dh_f = (float)(dh * (1.0 + 1e-3));
     }
     return SGS_OK;
 #undef HERR

@@ -48,10 +48,11 @@ __device__ __forceinline__ double metric_d2(const MetricDev& m, int dim, double 
 }
 
 // FP32 evaluation of the same metric, used only to discard candidates that
-// are clearly outside (bound_f carries a 1e-3 relative margin, far above the
-// FP32 rounding of these few operations), so the FP64 decision is unchanged.
-__device__ __forceinline__ bool metric_maybe_inside(const MetricDev& m, int dim, float h0, float h1, float h2) {
-    if (m.kind == METRIC_NEAREST) return true;
+// are clearly outside `bound` (bound_f, or a tighter bound for a smaller
+// distance; each carries a 1e-3 relative margin and a slack above the FP32
+// rounding of these few operations), so the FP64 decision is unchanged.
+__device__ __forceinline__ bool metric_maybe_within(const MetricDev& m, int dim, float h0, float h1, float h2,
+                                                    float bound) {
     float s;
     if (m.kind != METRIC_ELLIPSOID) {
         s = h0 * h0 + h1 * h1 + (dim == 3 ? h2 * h2 : 0.0f);
@@ -66,7 +67,7 @@ __device__ __forceinline__ bool metric_maybe_inside(const MetricDev& m, int dim,
             }
         }
     }
-    return s <= m.bound_f;
+    return s <= bound;
 }
 
 __device__ __forceinline__ bool metric_inside(const MetricDev& m, double d2) {

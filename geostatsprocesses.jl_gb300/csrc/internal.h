@@ -37,7 +37,10 @@ struct MetricDev {
     double ext[3];      // bounding-box half extents (physical units)
     float Rf[9];        // FP32 copies for the conservative prefilter
     float invf[3];
-    float bound_f;      // FP32 prefilter bound: (1 + 1e-3) * (r*r or 1)
+    float bound_f;      // FP32 prefilter bound: (1 + 1e-3) * (r*r or 1) + slack_f
+                        // (+infinity for the unbounded nearest-neighbour metric)
+    float slack_f;      // FP32 rounding allowance of the screen near the boundary
+    float dh_f;         // bound on the FP32 rounding of an origin-relative coordinate
 };
 
 struct VarioDev {

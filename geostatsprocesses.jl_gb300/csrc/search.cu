@@ -84,27 +84,78 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
         int i0, i1, i2;
         cell_of(G, g, i0, i1, i2);
 
-        // ---- data candidates inside the neighbourhood, sorted ----
+        // ---- grid candidates from the sorted template ----
+        int ng = 0;
+        const int T = a.data_only ? 0 : a.T;
+        for (int base = 0; base < T && ng < k; base += 32) {
+            const int j = base + lane;
+            bool ok = false;
+            int c = 0;
+            if (j < T) {
+                const TmplEntry e = a.tmpl[j];
+                const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
+                if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {
+                    c = g + e.dlin;
+                    ok = a.rank[c] < t;
+                }
+            }
+            const unsigned b = __ballot_sync(FULL_MASK, ok);
+            if (ok) {
+                const int p = ng + __popc(b & lt);
+                if (p < k) {
+                    gidx[p] = c;
+                    gd2[p] = tkey[j];
+                }
+            }
+            ng += __popc(b);
+        }
+        ng = min(ng, k);
+        __syncwarp();
+
+        // ---- data candidates, sorted ----
+        // With k grid neighbours found, only data strictly nearer than the
+        // k-th can enter the row (at equal distance grid nodes come first),
+        // so that distance bounds the bucket box, the FP32 screen and the
+        // exact test; otherwise every datum inside the neighbourhood counts.
         int nd = 0;
         if (a.D > 0) {
+            const bool bounded = ng == k;
+            const double tmax = bounded ? __longlong_as_double(gd2[k - 1]) : 0.0;
+            const float tf = (float)tmax * 1.001f;
+            const float rho = sqrtf(tf) + a.metric.dh_f;  // the bound's radius, metric units
+            const float dimf = (float)G.dim;
+            float bnd = a.metric.bound_f;
+            if (bounded) {
+                if (a.metric.kind == METRIC_NEAREST)
+                    bnd = tf + 2.0f * sqrtf(dimf * tf) * a.metric.dh_f + dimf * a.metric.dh_f * a.metric.dh_f;
+                else
+                    bnd = fminf(bnd, tf + a.metric.slack_f);
+            }
             double x[3];
             x[0] = centroid(G, 0, i0);
             x[1] = centroid(G, 1, i1);
             x[2] = G.dim == 3 ? centroid(G, 2, i2) : 0.0;
             int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
             for (int j = 0; j < G.dim; ++j) {
-                if (a.metric.kind == METRIC_NEAREST) {
+                if (a.metric.kind == METRIC_NEAREST && !bounded) {
                     lo[j] = 0;
                     hi[j] = a.nb[j] - 1;
                 } else {
-                    // bucket range of the neighbourhood's bounding box, in FP32
-                    // with a margin of 1e-3 buckets on each side: far above the
-                    // few FP32 roundings here (~1e-5 buckets) and the FP32
-                    // rounding of the half extent, so the range is a superset
+                    // bucket range of the bounding box (of the neighbourhood,
+                    // or of its part within the bound), in FP32 with a margin
+                    // of 1e-3 buckets on each side: far above the few FP32
+                    // roundings here (~1e-5 buckets) and the FP32 rounding of
+                    // the half extent, so the range is a superset
+                    float ext = a.ext_f[j];
+                    if (bounded) {
+                        if (a.metric.kind == METRIC_ELLIPSOID) ext *= fminf(1.0f, rho);
+                        else if (a.metric.kind == METRIC_ISO) ext = fminf(ext, rho);
+                        else ext = rho;
+                    }
                     const int ij = j == 0 ? i0 : (j == 1 ? i1 : i2);
                     const float xr = ((float)ij + 0.5f) * a.spacing_f[j];
-                    const float l = floorf((xr - a.ext_f[j]) * a.inv_bw_f[j] - 1e-3f);
-                    const float h = floorf((xr + a.ext_f[j]) * a.inv_bw_f[j] + 1e-3f);
+                    const float l = floorf((xr - ext) * a.inv_bw_f[j] - 1e-3f);
+                    const float h = floorf((xr + ext) * a.inv_bw_f[j] + 1e-3f);
                     lo[j] = (int)fmaxf(0.0f, fminf(l, (float)(a.nb[j] - 1)));
                     hi[j] = (int)fmaxf(0.0f, fminf(h, (float)(a.nb[j] - 1)));
                 }
@@ -126,7 +177,7 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
                     const double h1 = dsub(a.dxyz[3 * (int64_t)i + 1], x[1]);
                     const double h2 = G.dim == 3 ? dsub(a.dxyz[3 * (int64_t)i + 2], x[2]) : 0.0;
                     d2 = metric_d2(a.metric, G.dim, h0, h1, h2);
-                    ok = metric_inside(a.metric, d2);
+                    ok = metric_inside(a.metric, d2) && (!bounded || d2 < tmax);
                 }
                 const unsigned b = __ballot_sync(FULL_MASK, ok);
                 if (ok) {
@@ -181,7 +232,7 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
                         // FP32 screen on origin-relative FP32 coordinates;
                         // bound_f includes a slack above their rounding
                         const float4 p = a.dxyz_f[i];
-                        maybe = metric_maybe_inside(a.metric, G.dim, p.x - xr[0], p.y - xr[1], p.z - xr[2]);
+                        maybe = metric_maybe_within(a.metric, G.dim, p.x - xr[0], p.y - xr[1], p.z - xr[2], bnd);
                     }
                     const unsigned b = __ballot_sync(FULL_MASK, maybe);
                     if (maybe) squ[nq + __popc(b & lt)] = i;
@@ -203,44 +254,6 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
             if (nbuf > 0) warp_sort_pairs(dd2, didx, nbuf, lane);
             nd = min(nbuf, k);
         }
-
-        // ---- grid candidates from the sorted template ----
-        int ng = 0;
-        int before = 0;  // data strictly nearer than the current template entry
-        const int T = a.data_only ? 0 : a.T;
-        for (int base = 0; base < T && ng < k; base += 32) {
-            // no template entry from here on can enter the k nearest once
-            // ng grid + the data strictly nearer than this entry fill k; the
-            // template keys do not decrease, so `before` only moves forward
-            // through the sorted data keys (same value in every lane)
-            if (nd > 0) {
-                const long long dcur = tkey[base];
-                while (before < nd && dd2[before] < dcur) ++before;
-                if (ng + before >= k) break;
-            }
-            const int j = base + lane;
-            bool ok = false;
-            int c = 0;
-            if (j < T) {
-                const TmplEntry e = a.tmpl[j];
-                const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
-                if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {
-                    c = g + e.dlin;
-                    ok = a.rank[c] < t;
-                }
-            }
-            const unsigned b = __ballot_sync(FULL_MASK, ok);
-            if (ok) {
-                const int p = ng + __popc(b & lt);
-                if (p < k) {
-                    gidx[p] = c;
-                    gd2[p] = tkey[j];
-                }
-            }
-            ng += __popc(b);
-        }
-        ng = min(ng, k);
-        __syncwarp();
 
         // ---- merge (d2, id): grid entries precede data entries at equal d2 ----
         int32_t* out = a.nbr + (int64_t)g * k;
