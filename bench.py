@@ -305,15 +305,25 @@ def time_e2e(wl, args, torch, ws, steps, sweep=None):
     out = torch.empty((R, N), dtype=torch.float64, pin_memory=True).numpy()
     p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
 
+    split = {"create": 0.0, "prepare": 0.0, "simulate": 0.0, "destroy": 0.0}
+
     def step(i):
+        t = time.perf_counter()
         plan = geosgs.Plan(p, keep)
         if sweep:
             plan.set_sweep(**sweep)
+        t1 = time.perf_counter()
         plan.prepare()
+        t2 = time.perf_counter()
         plan._check(plan.lib.sgs_plan_simulate(plan.h, R, None, 77 + i,
                                                out.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))))
+        t3 = time.perf_counter()
         inf = plan.info()
         plan.close()
+        t4 = time.perf_counter()
+        if i > 0:
+            for k_, v_ in zip(split, (t1 - t, t2 - t1, t3 - t2, t4 - t3)):
+                split[k_] += v_
         return inf
 
     step(0)
@@ -323,6 +333,7 @@ def time_e2e(wl, args, torch, ws, steps, sweep=None):
     infs = [step(1 + i) for i in range(steps)]
     torch.cuda.synchronize()
     dt = max_over_ranks(ws, (time.perf_counter() - t0) / steps)
+    time_e2e.split_ms = {k_: round(1e3 * v_ / steps, 2) for k_, v_ in split.items()}
     return dt, infs[-1], float(out[0, :8].sum())
 
 
@@ -573,7 +584,8 @@ def main():
         e2e = {"value": ws * N * R / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(e2e_inf.h2d_bytes), "d2h_bytes_per_step": int(e2e_inf.d2h_bytes),
                "ms_per_step": 1e3 * e2e_s,
-               "path": "sgs_plan_create + sgs_plan_prepare + sgs_plan_simulate (FP64 out to pinned host) + sgs_plan_destroy"}
+               "path": "sgs_plan_create + sgs_plan_prepare + sgs_plan_simulate (FP64 out to pinned host) + sgs_plan_destroy",
+               "calls_ms": getattr(time_e2e, "split_ms", None)}
 
     if rank != 0:
         return

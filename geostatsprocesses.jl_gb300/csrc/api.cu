@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/geosgs.h"
@@ -309,14 +310,39 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
         HERR("unknown search kind");
     }
 
-    // path and ranks
+    // path and ranks: rank[path[t]] = t, then a check that every rank
+    // points back (a path with a repeated or out-of-range entry fails it);
+    // large grids in parallel
     H.path.resize(H.N);
     H.rank.assign(H.N, -1);
-    for (int64_t t = 0; t < H.N; ++t) {
-        const int64_t g = pr->path ? pr->path[t] : t;
-        if (g < 0 || g >= H.N || H.rank[g] != -1) HERR("path is not a permutation of the grid nodes");
-        H.path[t] = (int32_t)g;
-        H.rank[g] = (int32_t)t;
+    {
+        const int64_t N = H.N;
+        const int nt = N >= ((int64_t)1 << 20) ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
+        std::vector<int> bad(nt, 0);
+        auto run = [&](int w, int pass) {
+            const int64_t t0 = N * w / nt, t1 = N * (w + 1) / nt;
+            for (int64_t t = t0; t < t1; ++t) {
+                const int64_t g = pr->path ? pr->path[t] : t;
+                if (pass == 0) {
+                    if (g < 0 || g >= N) {
+                        bad[w] = 1;
+                        continue;
+                    }
+                    H.path[t] = (int32_t)g;
+                    __atomic_store_n(&H.rank[g], (int32_t)t, __ATOMIC_RELAXED);
+                } else if (H.rank[g] != (int32_t)t) {
+                    bad[w] = 1;
+                }
+            }
+        };
+        for (int pass = 0; pass < 2; ++pass) {
+            std::vector<std::thread> th;
+            for (int w = 1; w < nt; ++w) th.emplace_back(run, w, pass);
+            run(0, pass);
+            for (auto& x : th) x.join();
+            for (int w = 0; w < nt; ++w)
+                if (bad[w]) HERR("path is not a permutation of the grid nodes");
+        }
     }
 
     // template: cell offsets inside the neighbourhood in canonical order
@@ -469,9 +495,9 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     P->sweep.mode = (pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) ? SGS_SWEEP_COOPERATIVE
                     : (pr->flags & SGS_FLAG_LEVEL_SWEEP)   ? SGS_SWEEP_LEVELS
                                                            : SGS_SWEEP_FLOW;
-    P->h_path = H.path;
-    P->h_tmpl = H.tmpl;
-    P->h_tmpl_d2 = H.tmpl_d2;
+    P->h_path = std::move(H.path);
+    P->h_tmpl = std::move(H.tmpl);
+    P->h_tmpl_d2 = std::move(H.tmpl_d2);
     for (int j = 0; j < 3; ++j) {
         P->tmpl_ext[j] = H.tmpl_ext[j];
         P->nb[j] = H.nb[j];
@@ -921,12 +947,22 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     rc = run_sweep(P, R, Rp, zr, seed, V, st);
     if (rc) return rc;
     CK(P, cudaEventRecord(P->ev[6], st));
-    // realization-major FP64 output, in chunks of realizations
+    // realization-major FP64 output: written by the transposing kernel
+    // straight into `out` when it is page-locked host memory the device can
+    // address, else in chunks of realizations through a device buffer
+    double* dout = pinned_device_view(out);
+    if (dout) {
+        if (P->precision == SGS_PREC_FP64)
+            LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V, N, R, Rp, P->mean, dout, st));
+        else
+            LAUNCH(P, 1, launch_rows_to_out_fp32((const float*)V, N, R, Rp, P->mean, dout, st));
+        P->info.d2h_bytes += (int64_t)N * R * sizeof(double);
+    }
     const int64_t chunk_bytes = (int64_t)1 << 29;
     int64_t rchunk = std::max<int64_t>(1, std::min<int64_t>(R, chunk_bytes / (N * (int64_t)sizeof(double))));
     double* ob = nullptr;
-    if ((rc = dalloc(P, &ob, (size_t)N * rchunk))) return rc;
-    for (int64_t r0 = 0; r0 < R; r0 += rchunk) {
+    if (!dout && (rc = dalloc(P, &ob, (size_t)N * rchunk))) return rc;
+    for (int64_t r0 = 0; !dout && r0 < R; r0 += rchunk) {
         const int rn = (int)std::min<int64_t>(rchunk, R - r0);
         // rows_to_out reads realizations [r0, r0+rn) of each row
         if (P->precision == SGS_PREC_FP64)

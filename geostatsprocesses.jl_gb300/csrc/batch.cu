@@ -1008,15 +1008,24 @@ extern "C" int sgs_batch_simulate(sgs_batch* B, int32_t R, const double* z, uint
         cleanup();
         return rc;
     }
-    // realization-major FP64 output by domain, the domain's mean added
+    // realization-major FP64 output by domain, the domain's mean added:
+    // written by the transposing kernels straight into `out` when it is
+    // page-locked host memory, else through a device buffer
+    double* dout = pinned_device_view(out);
+    for (int d = 0; dout && d < B->ndom; ++d) {
+        const int64_t n0 = B->noff[d], n = B->noff[d + 1] - n0;
+        if (f64) BLAUNCH(B, launch_rows_to_out_fp64((const double*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
+        else BLAUNCH(B, launch_rows_to_out_fp32((const float*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
+        B->info.d2h_bytes += (int64_t)n * R * sizeof(double);
+    }
     double* ob = nullptr;
     const int64_t chunk_bytes = (int64_t)1 << 28;
     const int64_t ob_elems = std::max<int64_t>(1, std::min<int64_t>((int64_t)R * maxn, chunk_bytes / 8 + maxn));
-    if ((rc = balloc(B, &ob, (size_t)ob_elems))) {
+    if (!dout && (rc = balloc(B, &ob, (size_t)ob_elems))) {
         cleanup();
         return rc;
     }
-    for (int d = 0; d < B->ndom; ++d) {
+    for (int d = 0; !dout && d < B->ndom; ++d) {
         const int64_t n0 = B->noff[d], n = B->noff[d + 1] - n0;
         const int64_t rchunk = std::max<int64_t>(1, std::min<int64_t>(R, ob_elems / std::max<int64_t>(1, n)));
         for (int64_t r0 = 0; r0 < R; r0 += rchunk) {

@@ -195,6 +195,19 @@ int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err);
 // The geometry fields of a domain's SearchArgs (device pointers left as they are).
 void search_args_of(const HostDomain& H, SearchArgs& sa);
 
+// Device address of a page-locked host buffer (cudaHostAlloc'd or
+// registered), or nullptr for any other pointer (pageable memory is never
+// handed to a kernel).
+inline double* pinned_device_view(double* host) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+    return static_cast<double*>(a.devicePointer);
+}
+
 // Message returned by sgs_last_error(NULL) on this host thread.
 void set_thread_error(const char* msg);
 inline void set_thread_error(const std::string& msg) { set_thread_error(msg.c_str()); }

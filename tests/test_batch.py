@@ -134,6 +134,12 @@ def test_batch_device_values_and_autotuner(oracle_mod, geosgs_lib):
     chosen, tried = B.tune_sweep(R)
     assert len(tried) >= 2 and chosen["ms"] == min(t["ms"] for t in tried)
     host = B.simulate(R, seed=5)
+    # the same realizations written straight into page-locked host memory
+    import ctypes as C
+
+    pinned = torch.empty(R * B.nnodes, dtype=torch.float64, pin_memory=True)
+    B._check(B.lib.sgs_batch_simulate(B.h, R, None, C.c_uint64(5), C.cast(pinned.data_ptr(), C.POINTER(C.c_double))))
+    np.testing.assert_array_equal(pinned.numpy(), np.concatenate([h.reshape(-1) for h in host]))
     V = torch.empty((B.nnodes, R), dtype=torch.float32, device="cuda")
     B.simulate_device(R, 5, V.data_ptr())
     info = B.info()
