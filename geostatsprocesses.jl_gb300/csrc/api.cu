@@ -84,6 +84,11 @@ struct sgs_plan {
     int64_t done_cap = 0;         // flags allocated in d_done (pieces x N)
     int last_sweep_mode = SGS_SWEEP_FLOW;  // mode of the last sweep launched
     int data_only = 0;            // neighbours from the data alone (sgs_krige)
+    // indicator simulation (sgs_plan_set_indicator)
+    int ind_ncat = 0;
+    double ind_prob[IND_MAX_CAT] = {};
+    int32_t* d_ind_cat = nullptr;
+    double *d_ind_wsum = nullptr, *d_ind_dsum = nullptr;
     sgs_info info{};
 };
 
@@ -595,6 +600,12 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     s.w_full = w_full;
     s.sigma_full = sigma_full;
     s.sum_m = P->d_sum_m;
+    if (P->ind_ncat) {
+        s.ind_cat = P->d_ind_cat;
+        s.ncat = P->ind_ncat;
+        s.ind_wsum = P->d_ind_wsum;
+        s.ind_dsum = P->d_ind_dsum;
+    }
     CK(P, cudaMemsetAsync(P->d_sum_m, 0, sizeof(unsigned long long), P->stream));
     if (P->precision == SGS_PREC_FP64) {
         LAUNCH(P, 1, launch_solve_fp64(s, P->t64, P->stream));
@@ -769,6 +780,10 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         }
     }
     if (!P->d_flow && (rc = dalloc(P, &P->d_flow, 2))) return rc;
+    if (P->ind_ncat && !P->d_ind_wsum) {
+        if ((rc = dalloc(P, &P->d_ind_wsum, N))) return rc;
+        if ((rc = dalloc(P, &P->d_ind_dsum, (size_t)N * P->ind_ncat))) return rc;
+    }
     CK(P, cudaEventRecord(P->ev[3], st));
     if ((rc = run_solve(P, nullptr, nullptr))) return rc;
     CK(P, cudaEventRecord(P->ev[4], st));
@@ -1316,5 +1331,102 @@ extern "C" int sgs_krige(const sgs_problem* problem, double* mean, double* var) 
         if (var) var[g] = ok ? sd[p] * sd[p] : nan;
     }
     sgs_plan_destroy(P);
+    return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Sequential indicator simulation (indicator.cu): the plan's variogram is the
+// categories' common correlogram, data_values are ignored in favour of the
+// data categories.
+extern "C" int sgs_plan_set_indicator(sgs_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (ncat < 2 || ncat > IND_MAX_CAT) return set_err(P, SGS_ERR_ARG, "ncat must be in 2..8");
+    if (!prob) return set_err(P, SGS_ERR_ARG, "null probabilities");
+    double s = 0.0;
+    for (int l = 0; l < ncat; ++l) {
+        if (!(prob[l] >= 0.0) || !std::isfinite(prob[l])) return set_err(P, SGS_ERR_ARG, "probabilities must be >= 0");
+        s += prob[l];
+    }
+    if (!(s > 0.0)) return set_err(P, SGS_ERR_ARG, "probabilities must not all be 0");
+    if (P->D > 0 && !data_cat) return set_err(P, SGS_ERR_ARG, "null data categories");
+    std::vector<int32_t> cat(std::max<int64_t>(P->D, 1), 0);
+    for (int64_t i = 0; i < P->D; ++i) {
+        if (data_cat[i] < 0 || data_cat[i] >= ncat) return set_err(P, SGS_ERR_ARG, "data category out of range");
+        cat[i] = data_cat[i];
+    }
+    CK(P, cudaSetDevice(P->device));
+    if (P->ind_ncat != ncat) {  // table sizes change: reallocate at the next prepare
+        dfree(P, P->d_ind_wsum);
+        dfree(P, P->d_ind_dsum);
+        P->d_ind_wsum = P->d_ind_dsum = nullptr;
+    }
+    dfree(P, P->d_ind_cat);
+    P->d_ind_cat = nullptr;
+    int rc;
+    if ((rc = upload(P, &P->d_ind_cat, cat.data(), cat.size()))) return rc;
+    CK(P, cudaStreamSynchronize(P->stream));
+    P->ind_ncat = ncat;
+    for (int l = 0; l < IND_MAX_CAT; ++l) P->ind_prob[l] = l < ncat ? prob[l] / s : 0.0;
+    P->prepared = false;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_simulate_indicator(sgs_plan* P, int32_t R, const double* u, uint64_t seed, int32_t* out) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->ind_ncat) return set_err(P, SGS_ERR_STATE, "no indicator set (sgs_plan_set_indicator)");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "simulate before prepare");
+    if (R < 1 || !out) return set_err(P, SGS_ERR_ARG, "invalid nreals or output");
+    CK(P, cudaSetDevice(P->device));
+    const int64_t N = P->N;
+    const int Rp = (R + 3) / 4 * 4;
+    cudaStream_t st = P->stream;
+    int rc;
+    uint8_t* C = nullptr;
+    double *uin = nullptr, *ur = nullptr;
+    int32_t* od = nullptr;
+    auto cleanup = [&]() {
+        dfree(P, C);
+        dfree(P, uin);
+        dfree(P, ur);
+        dfree(P, od);
+    };
+    if ((rc = dalloc(P, &C, (size_t)N * Rp))) return rc;
+    if (u) {
+        if ((rc = dalloc(P, &uin, (size_t)N * R)) || (rc = dalloc(P, &ur, (size_t)N * Rp))) {
+            cleanup();
+            return rc;
+        }
+        CK(P, cudaMemcpyAsync(uin, u, (size_t)N * R * sizeof(double), cudaMemcpyHostToDevice, st));
+        P->info.h2d_bytes += (int64_t)N * R * sizeof(double);
+        LAUNCH(P, 1, launch_z_to_rows_fp64(uin, N, R, Rp, ur, st));
+    }
+    IndArgs ia{};
+    ia.ncat = P->ind_ncat;
+    for (int l = 0; l < IND_MAX_CAT; ++l) ia.prob[l] = P->ind_prob[l];
+    ia.wsum = P->d_ind_wsum;
+    ia.dsum = P->d_ind_dsum;
+    CK(P, cudaEventRecord(P->ev[5], st));
+    for (int l = 0; l < P->nlevels; ++l) {
+        const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
+        cudaError_t e = P->precision == SGS_PREC_FP64
+                            ? launch_sis_level_fp64(P->t64, P->k, p0, p1, Rp, ia, ur, seed, C, st)
+                            : launch_sis_level_fp32(P->t32, P->k, p0, p1, Rp, ia, ur, seed, C, st);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cuda_err(P, e, "indicator sweep launch");
+        }
+        if (p1 > p0) P->info.launches++;
+    }
+    CK(P, cudaEventRecord(P->ev[6], st));
+    if ((rc = dalloc(P, &od, (size_t)N * R))) {
+        cleanup();
+        return rc;
+    }
+    LAUNCH(P, 1, launch_cats_to_out(C, N, R, Rp, od, st));
+    CK(P, cudaMemcpyAsync(out, od, (size_t)N * R * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    P->info.d2h_bytes += (int64_t)N * R * sizeof(int32_t);
+    CK(P, cudaStreamSynchronize(st));
+    P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
+    cleanup();
     return SGS_OK;
 }

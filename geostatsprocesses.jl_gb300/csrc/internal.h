@@ -168,7 +168,28 @@ struct SolveArgs {
     unsigned long long* n_warm;  // counts systems accepted from the warm start
     int64_t node0;               // added to node ids written to the sweep tables (the
                                  // domain's first global id in a batch; 0 for a plan)
+    // indicator simulation (nullptr otherwise): per position, the sum of all
+    // weights and, per category, the sum of the weights of data of that
+    // category (zero for prior nodes)
+    const int32_t* ind_cat;      // D data categories, 0 .. ncat-1
+    int ncat;
+    double* ind_wsum;            // [P]
+    double* ind_dsum;            // [P][ncat]
 };
+
+// Sequential indicator simulation (indicator.cu).
+constexpr int IND_MAX_CAT = 8;
+struct IndArgs {
+    int ncat;
+    double prob[IND_MAX_CAT];    // prior probabilities (normalized)
+    const double* wsum;          // [P] sum of a system's weights (0 for the prior)
+    const double* dsum;          // [P][ncat] weights of data of each category
+};
+cudaError_t launch_sis_level_fp32(const SweepTables<float>& t, int k, int64_t p0, int64_t p1, int Rp,
+                                  const IndArgs& ia, const double* u, uint64_t seed, uint8_t* C, cudaStream_t s);
+cudaError_t launch_sis_level_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
+                                  const IndArgs& ia, const double* u, uint64_t seed, uint8_t* C, cudaStream_t s);
+cudaError_t launch_cats_to_out(const uint8_t* C, int64_t N, int R, int Rp, int32_t* out, cudaStream_t s);
 
 // Host-side description of one problem (api.cu: host_domain): everything
 // sgs_plan_create derives on the host before uploading.

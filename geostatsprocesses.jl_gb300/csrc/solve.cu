@@ -142,6 +142,37 @@ __host__ __device__ constexpr size_t warp_smem_bytes(int k) {
            ((size_t)k * sizeof(T) + 15) / 16 * 16 + (size_t)k * sizeof(NbInfo);
 }
 
+// Indicator sums of one system (SolveArgs::ind_*): w holds the weights of the
+// system's n neighbours (FP64 values `wq(q)`), kriged = false for a prior
+// node (all sums zero).
+template <typename WF>
+__device__ __forceinline__ void write_indicator_sums(const SolveArgs& a, int64_t pos, int n, const NbInfo* info,
+                                                     bool kriged, WF wq, int lane) {
+    double ws = 0.0;
+    double ds[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) ds[l] = 0.0;
+    if (kriged)
+        for (int q = lane; q < n; q += 32) {
+            const double v = wq(q);
+            ws += v;
+            if (info[q].did >= 0) {
+                const int c = a.ind_cat[info[q].did];
+#pragma unroll
+                for (int l = 0; l < 8; ++l)
+                    if (l == c) ds[l] += v;
+            }
+        }
+    ws = warp_sum(ws);
+    if (lane == 0) a.ind_wsum[pos] = ws;
+#pragma unroll
+    for (int l = 0; l < 8; ++l)
+        if (l < a.ncat) {
+            const double v = warp_sum(ds[l]);
+            if (lane == 0) a.ind_dsum[pos * a.ncat + l] = v;
+        }
+}
+
 // Store an FP64 value into a table entry: as is, or as an FP32 (hi, lo) pair.
 __device__ __forceinline__ void put(double* t, int64_t i, double v) { t[i] = v; }
 __device__ __forceinline__ void put(float* t, int64_t i, double v) {
@@ -174,6 +205,8 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
         }
         b0 = warp_sum(b0);
     }
+    if (a.ind_wsum)
+        write_indicator_sums(a, pos, n, info, status == SGS_NODE_KRIGED_, [&](int q) { return w[q]; }, lane);
     if (lane == 0) {
         if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
         tab.node[pos] = g + (int32_t)a.node0;
@@ -688,6 +721,9 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
             }
         }
         const DF b0 = warp_sum_df(b0acc.value());
+        if (a.ind_wsum)
+            write_indicator_sums(a, pos, n, info, status == SGS_NODE_KRIGED_,
+                                 [&](int q) { return (double)w[q].hi + (double)w[q].lo; }, lane);
         if (lane == 0) {
             if (a.sum_m) atomicAdd(a.sum_m, (unsigned long long)m);
             tab.node[pos] = g + (int32_t)a.node0;

@@ -15,12 +15,16 @@ from .model import (
     GaussianProcess,
     GaussianVariogram,
     GeoTable,
+    ExponentialTransiogram,
+    GaussianTransiogram,
+    IndicatorProcess,
     LinearPath,
     MetricBall,
     RandomPath,
     RotX,
     RotY,
     RotZ,
+    SphericalTransiogram,
     SphericalVariogram,
     georef,
 )
@@ -32,7 +36,8 @@ from .simulation import (GPUSEQSIM, Ensemble, FieldSimulationMethod, expectedval
 __all__ = [
     "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
-    "GeoTable", "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
+    "GeoTable", "ExponentialTransiogram", "GaussianTransiogram", "IndicatorProcess", "SphericalTransiogram",
+    "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
     "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
     "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

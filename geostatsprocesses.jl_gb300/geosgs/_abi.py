@@ -36,6 +36,7 @@ SGS_FLAG_NN_FP32 = 4
 
 SGS_NN_FEATURES = 8
 SGS_NN_PARAMS = 2401
+SGS_IND_MAX_CATEGORIES = 8
 
 SGS_NODE_KRIGED = 0
 SGS_NODE_PRIOR_NMIN = 1
@@ -188,6 +189,8 @@ EXPORTS = (
     "sgs_batch_destroy",
     "sgs_batch_last_error",
     "sgs_krige",
+    "sgs_plan_set_indicator",
+    "sgs_plan_simulate_indicator",
     "sgs_ensemble_stats",
     "sgs_ensemble_cdf",
     "sgs_ensemble_quantile",
@@ -275,6 +278,10 @@ def _declare(lib):
     lib.sgs_batch_destroy.restype = None
     lib.sgs_batch_last_error.argtypes = [P]
     lib.sgs_batch_last_error.restype = C.c_char_p
+    lib.sgs_plan_set_indicator.argtypes = [P, C.c_int32, dp, ip]
+    lib.sgs_plan_set_indicator.restype = C.c_int
+    lib.sgs_plan_simulate_indicator.argtypes = [P, C.c_int32, dp, C.c_uint64, ip]
+    lib.sgs_plan_simulate_indicator.restype = C.c_int
     lib.sgs_krige.argtypes = [C.POINTER(SgsProblem), dp, dp]
     lib.sgs_krige.restype = C.c_int
     lib.sgs_ensemble_stats.argtypes = [P, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, P, P, P]

@@ -163,6 +163,64 @@ class GaussianProcess:
         self.mean = float(mean)
 
 
+class _Transiogram:
+    """A proportional transiogram: t_ab(h) = p_b + (delta_ab - p_b) (1 - g(h))
+    with g a unit-sill variogram shape (GeoStatsFunctions' Spherical /
+    Exponential / Gaussian transiograms with `range` and `proportions`).  Its
+    indicator covariances p_a (t_ab(h) - p_b) = (diag(p) - p p')_ab (1 - g(h))
+    are separable: every category shares the correlogram 1 - g."""
+
+    SHAPE = None
+
+    def __init__(self, ball=None, *, range=None, ranges=None, rotation=None, proportions=(0.5, 0.5)):
+        self.shape = self.SHAPE(ball, range=range, ranges=ranges, rotation=rotation, sill=1.0, nugget=0.0)
+        p = np.asarray(proportions, dtype=np.float64)
+        if p.ndim != 1 or len(p) < 2 or np.any(p < 0) or not p.sum() > 0:
+            raise ArgumentError("proportions must be at least two non-negative numbers")
+        self.proportions = tuple(float(x) for x in p / p.sum())
+
+
+class SphericalTransiogram(_Transiogram):
+    SHAPE = SphericalVariogram
+
+
+class ExponentialTransiogram(_Transiogram):
+    SHAPE = ExponentialVariogram
+
+
+class GaussianTransiogram(_Transiogram):
+    SHAPE = GaussianVariogram
+
+
+class IndicatorProcess:
+    """IndicatorProcess(func, prob) — src/processes/field/indicator.jl:5-45.
+
+    On the GPU path `func` is a separable indicator model: a transiogram
+    above (prob defaults to its proportions) or a variogram taken as the
+    categories' common correlogram with explicit `prob`; prob is normalized
+    to sum to one (indicator.jl:40-43)."""
+
+    def __init__(self, func, prob=None):
+        if isinstance(func, _Transiogram):
+            corr = func.shape
+            prob = func.proportions if prob is None else prob
+        elif isinstance(func, _Variogram):
+            corr = func
+            if prob is None:
+                raise ArgumentError("an indicator process on a variogram needs its probabilities")
+        else:
+            raise ArgumentError("IndicatorProcess on the GPU path takes a transiogram or a variogram")
+        p = np.asarray(prob, dtype=np.float64)
+        if p.ndim != 1 or len(p) < 2 or np.any(p < 0) or np.any(p > 1) or not p.sum() > 0:
+            raise ArgumentError("probabilities must be in [0, 1], at least two of them")
+        if len(p) > _abi.SGS_IND_MAX_CATEGORIES:
+            raise ArgumentError("at most %d categories on the GPU" % _abi.SGS_IND_MAX_CATEGORIES)
+        self.func = func
+        self.corr = corr
+        self.prob = tuple(float(x) for x in p / p.sum())
+        self.mean = 0.0
+
+
 # -------------------------------------------------------------------- domain
 class CartesianGrid:
     """Regular grid: CartesianGrid(dims) or CartesianGrid(start, finish, dims=...)
@@ -219,7 +277,10 @@ class GeoTable:
     """Point data: one variable per column and D x dim coordinates."""
 
     def __init__(self, values: dict, coords):
-        self.values = {k: np.asarray(v, dtype=np.float64) for k, v in values.items()}
+        # numeric columns as FP64, categorical ones (integer or string
+        # labels of an indicator process) as given
+        self.values = {k: (np.asarray(v, dtype=np.float64) if np.asarray(v).dtype.kind == "f" else np.asarray(v))
+                       for k, v in values.items()}
         c = np.asarray(coords, dtype=np.float64)
         if c.ndim == 1:
             c = c[:, None]

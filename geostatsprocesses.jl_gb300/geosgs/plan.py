@@ -83,6 +83,27 @@ class Plan:
         self._check(self.lib.sgs_plan_weights(self.h, _dp(w), _dp(s), _ip(st)))
         return w, s, st
 
+    def set_indicator(self, prob, data_cat=None):
+        """Sequential indicator simulation: prior probabilities of the
+        categories and the data's category indices (0-based); call before
+        prepare()."""
+        prob = np.ascontiguousarray(np.asarray(prob, dtype=np.float64))
+        dc = np.ascontiguousarray(np.asarray(data_cat if data_cat is not None else np.zeros(1), dtype=np.int32))
+        self._ind = (prob, dc)
+        self._check(self.lib.sgs_plan_set_indicator(self.h, len(prob), _dp(prob), _ip(dc)))
+        self.prepared = False
+        return self
+
+    def simulate_indicator(self, nreals: int, u=None, seed: int = 0) -> np.ndarray:
+        """nreals x N realization-major category indices (int32)."""
+        out = np.empty((nreals, self.N), dtype=np.int32)
+        up = None
+        if u is not None:
+            u = np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(nreals, self.N))
+            up = _dp(u)
+        self._check(self.lib.sgs_plan_simulate_indicator(self.h, nreals, up, C.c_uint64(seed), _ip(out)))
+        return out
+
     def levels(self):
         lv = np.empty(self.N, dtype=np.int32)
         n = C.c_int32()

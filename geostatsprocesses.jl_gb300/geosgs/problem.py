@@ -13,15 +13,31 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, MetricBall
+from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, IndicatorProcess, MetricBall
 
 _PREC = {"fp64": _abi.SGS_PREC_FP64, "fp32": _abi.SGS_PREC_FP32_REFINE}
 
 
-def build_problem(process: GaussianProcess, domain: CartesianGrid, data: GeoTable | None, method):
-    """Return (sgs_problem, keepalive) — keepalive owns the arrays it points to."""
-    if not isinstance(process, GaussianProcess):
-        raise ArgumentError("the GPU SEQSIM path simulates GaussianProcess")
+def indicator_levels(process: IndicatorProcess, data: GeoTable | None):
+    """(levels, data categories): the categories are the data's distinct
+    values in sorted order (the one-hot transform, seqsim.jl:247-249), or
+    1..L without data (seqsim.jl:253-261); categories are 0-based indices."""
+    L = len(process.prob)
+    if data is None or data.nrow() == 0:
+        return list(range(1, L + 1)), np.zeros(0, dtype=np.int32)
+    col = np.asarray(next(iter(data.values.values())))
+    levels, cat = np.unique(col, return_inverse=True)
+    if len(levels) != L:
+        raise ArgumentError(f"probabilities must have {len(levels)} components, received {L}")
+    return list(levels), cat.astype(np.int32)
+
+
+def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method):
+    """Return (sgs_problem, keepalive) — keepalive owns the arrays it points to.
+    An IndicatorProcess becomes the problem of its common correlogram, with
+    the data's category indices as data values."""
+    if not isinstance(process, (GaussianProcess, IndicatorProcess)):
+        raise ArgumentError("the GPU SEQSIM path simulates GaussianProcess and IndicatorProcess")
     if not isinstance(domain, CartesianGrid):
         raise ArgumentError("the GPU SEQSIM path simulates on a CartesianGrid")
     dim = domain.dim
@@ -38,14 +54,17 @@ def build_problem(process: GaussianProcess, domain: CartesianGrid, data: GeoTabl
         if len(data.values) != 1:
             raise ArgumentError("the GPU path simulates one variable")
         xy = np.ascontiguousarray(data.coords, dtype=np.float64)
-        val = np.ascontiguousarray(next(iter(data.values.values())), dtype=np.float64)
+        if isinstance(process, IndicatorProcess):
+            val = np.ascontiguousarray(indicator_levels(process, data)[1], dtype=np.float64)
+        else:
+            val = np.ascontiguousarray(next(iter(data.values.values())), dtype=np.float64)
         keep += [xy, val]
         p.ndata = xy.shape[0]
         p.data_coords = xy.ctypes.data_as(C.POINTER(C.c_double))
         p.data_values = val.ctypes.data_as(C.POINTER(C.c_double))
     else:
         p.ndata = 0
-    p.variogram = process.func.to_c(dim)
+    p.variogram = (process.corr if isinstance(process, IndicatorProcess) else process.func).to_c(dim)
     p.mean = process.mean
     p.minneighbors = int(method.minneighbors)
     p.maxneighbors = int(method.maxneighbors)

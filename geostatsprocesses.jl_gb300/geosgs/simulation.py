@@ -30,9 +30,10 @@ from typing import Any
 import numpy as np
 
 from . import _abi
-from .model import ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess, GeoTable, LinearPath, RandomPath
+from .model import (ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess, GeoTable, IndicatorProcess,
+                    LinearPath, RandomPath)
 from .plan import Batch, Plan
-from .problem import build_problem
+from .problem import build_problem, indicator_levels
 
 
 class FieldSimulationMethod:
@@ -92,6 +93,7 @@ class _Preproc:
     cursor: int = 0
     nreals: int = 1
     batches: Any = None  # per-realization paths: [(Batch, first realization, count)]
+    levels: Any = None   # indicator simulation: category labels
 
     def close(self):
         if self.plan is not None:
@@ -113,6 +115,15 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     of seqsim.jl:107-131).  `init` is ignored like SEQSIM ignores it
     (seqsim.jl:267-271 always uses ExplicitInit with data appended)."""
     seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
+    if isinstance(process, IndicatorProcess):
+        if method.path_per_realization:
+            raise ArgumentError("per-realization paths are available for GaussianProcess")
+        levels, dcat = indicator_levels(process, data)
+        problem, keep = build_problem(process, domain, data, method)
+        plan = Plan(problem, keep).set_indicator(process.prob, dcat).prepare()
+        pre = _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+        pre.levels = levels
+        return pre
     if method.path_per_realization and isinstance(method.path, RandomPath):
         return _Preproc(plan=None, var=_varname(process, data), seed=seed, z=z, nreals=nreals,
                         batches=_per_realization_batches(process, domain, data, method, nreals))
@@ -146,7 +157,11 @@ def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc)
     """One realization as {var: values} (seqsim.jl:72-156).  The first call
     simulates the whole block of `preproc.nreals` realizations on the GPU."""
     if preproc.block is None:
-        if preproc.batches is not None:
+        if preproc.levels is not None:
+            cats = preproc.plan.simulate_indicator(preproc.nreals, u=preproc.z, seed=preproc.seed)
+            preproc.block = np.asarray(preproc.levels, dtype=object if isinstance(preproc.levels[0], str)
+                                       else None)[cats]
+        elif preproc.batches is not None:
             rows = []
             for b, r0, cnt in preproc.batches:
                 z = None
@@ -183,11 +198,13 @@ def rand(*args, data=None, method=None, init=None, workers=None, async_=False,
     generator's draws, for reproducible comparisons."""
     args = list(args)
     rng = None
-    if args and not isinstance(args[0], GaussianProcess):
+    if args and not isinstance(args[0], (GaussianProcess, IndicatorProcess)):
         rng = _rng_of(args.pop(0))
     if len(args) not in (2, 3):
         raise ArgumentError("rand([rng], process, domain, [nreals]; kwargs...)")
     process, domain = args[0], args[1]
+    if not isinstance(process, (GaussianProcess, IndicatorProcess)):
+        raise ArgumentError("rand(process, ...) takes a GaussianProcess or an IndicatorProcess")
     nreals = args[2] if len(args) == 3 else None
     rng = rng if rng is not None else _rng_of(None)
     smethod = method if method is not None else GPUSEQSIM()

@@ -355,6 +355,27 @@ void sgs_batch_destroy(sgs_batch* batch);
  * sgs_batch_create on this thread when batch is NULL. */
 const char* sgs_batch_last_error(const sgs_batch* batch);
 
+/* ---- sequential indicator simulation ------------------------------------
+ * An IndicatorProcess(func, prob) simulated with SEQSIM
+ * (src/processes/field/indicator.jl, src/simulation/field/seqsim.jl:247-261
+ * one-hot data, :292-310 Kriging(func, prob) with a Categorical prior and
+ * conditional, :342-347 categorical draw) for a separable indicator
+ * covariance C_ab(h) = A_ab rho(h) — including the proportional transiogram
+ * t_ab(h) = p_b + (delta_ab - p_b) rho(h) — where rho is the plan's
+ * variogram model taken as the categories' common correlogram: every
+ * category's simple cokriging weights are then rho's simple kriging weights,
+ * and p_l = prob_l + sum_i w_i (I_l(x_i) - prob_l) is clamped to [0, 1],
+ * normalized, and drawn from by the inverse cdf at a uniform.
+ * sgs_plan_set_indicator (before sgs_plan_prepare): ncat categories (2..8),
+ * prior probabilities prob (normalized here), data categories data_cat
+ * (problem->ndata values in 0..ncat-1; the problem's data_values are not
+ * used).  sgs_plan_simulate_indicator: out = nreals x N categories
+ * (realization-major, int32); u = nreals x N uniforms in (0, 1) or NULL for
+ * Philox4x32-10 uniforms from `seed`. */
+#define SGS_IND_MAX_CATEGORIES 8
+int sgs_plan_set_indicator(sgs_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat);
+int sgs_plan_simulate_indicator(sgs_plan* plan, int32_t nreals, const double* u, uint64_t seed, int32_t* out);
+
 /* ---- posterior mean (simple kriging from the data) ---------------------
  * Mean and variance of the process at every grid node conditioned on the
  * data alone: the reference's mean(process, domain; data) for a

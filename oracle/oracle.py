@@ -46,6 +46,9 @@ def load():
     lib.oracle_solve.argtypes = [P, C.c_int64, C.c_int64, C.c_int64, C.c_int]
     lib.oracle_simulate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp, C.c_int64, C.c_int]
     lib.oracle_krige.argtypes = [P, dp, dp, C.c_int]
+    lib.oracle_simulate_indicator.argtypes = [P, C.c_int32, dp, ip, C.c_int32, dp, C.c_uint64, ip, C.c_int]
+    lib.oracle_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_int32, dp]
+    lib.oracle_uniforms.restype = None
     lib.oracle_neighbors.argtypes = [P, ip, ip]
     lib.oracle_weights.argtypes = [P, dp, dp, ip]
     lib.oracle_levels.argtypes = [P, ip, ip]
@@ -121,6 +124,19 @@ class OraclePlan:
         self._rc(self.lib.oracle_krige(self.h, _dp(m), _dp(v), nthreads))
         return m, v
 
+    def simulate_indicator(self, nreals, prob, data_cat=None, u=None, seed=0, nthreads=0):
+        """nreals x N categories (sequential indicator simulation)."""
+        prob = np.ascontiguousarray(np.asarray(prob, dtype=np.float64))
+        dc = np.ascontiguousarray(np.asarray(data_cat if data_cat is not None else np.zeros(1), dtype=np.int32))
+        out = np.empty((nreals, self.N), dtype=np.int32)
+        up = None
+        if u is not None:
+            u = np.ascontiguousarray(u, dtype=np.float64).reshape(nreals, self.N)
+            up = _dp(u)
+        self._rc(self.lib.oracle_simulate_indicator(self.h, len(prob), _dp(prob), _ip(dc), nreals, up, seed,
+                                                    _ip(out), nthreads))
+        return out
+
     def neighbors(self):
         idx = np.empty((self.N, self.k), dtype=np.int32)
         cnt = np.empty(self.N, dtype=np.int32)
@@ -148,6 +164,12 @@ def normals(seed: int, nnodes: int, nreals: int) -> np.ndarray:
     z = np.empty((nreals, nnodes), dtype=np.float64)
     load().oracle_normals(seed, nnodes, nreals, _dp(z))
     return z
+
+
+def uniforms(seed: int, nnodes: int, nreals: int) -> np.ndarray:
+    u = np.empty((nreals, nnodes), dtype=np.float64)
+    load().oracle_uniforms(seed, nnodes, nreals, _dp(u))
+    return u
 
 
 def covariance(variogram_c, dim, lag) -> float:

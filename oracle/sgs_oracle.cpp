@@ -672,6 +672,83 @@ extern "C" int oracle_simulate(oracle_plan* P, int32_t R, const double* z, uint6
     return SGS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Sequential indicator simulation (IndicatorProcess + SEQSIM, seqsim.jl:
+// 247-261 one-hot data, :292-310 Kriging(func, prob) with Categorical prior
+// and conditional, :342-347 categorical draw), restated for a separable
+// indicator covariance A_ab rho(h): every category's simple cokriging weights
+// are rho's simple kriging weights w (this plan's solve), so
+//   p_l = prob_l + sum_a w_a (I_l(x_a) - prob_l),
+// clamped to [0, 1], normalized, and drawn from by the inverse cdf at u.
+static inline double uniform_of(uint64_t seed, int64_t g, int32_t r) {
+    uint32_t c[4] = {(uint32_t)g, (uint32_t)((uint64_t)g >> 32), (uint32_t)(r >> 2), 0x5349u};
+    philox10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    return u24(c[r & 3]);
+}
+
+extern "C" void oracle_uniforms(uint64_t seed, int64_t N, int32_t R, double* u) {
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < N; ++g)
+        for (int32_t r = 0; r < R; ++r) u[(size_t)r * N + g] = uniform_of(seed, g, r);
+}
+
+extern "C" int oracle_simulate_indicator(oracle_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat,
+                                         int32_t R, const double* u, uint64_t seed, int32_t* out, int nthreads) {
+    if (!P || !out || R < 0 || ncat < 2 || !prob) return fail(SGS_ERR_ARG, "invalid argument");
+    double ps = 0.0;
+    for (int l = 0; l < ncat; ++l) ps += prob[l];
+    std::vector<double> pr(ncat);
+    for (int l = 0; l < ncat; ++l) pr[l] = prob[l] / ps;
+    const int k = P->nmax;
+    const int nt = nthreads_or_all(nthreads);
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<int32_t> cat(P->N + P->D);
+        std::vector<double> p(ncat);
+#pragma omp for schedule(dynamic, 1)
+        for (int32_t r = 0; r < R; ++r) {
+            std::fill(cat.begin(), cat.end(), -1);
+            for (int64_t i = 0; i < P->D; ++i) cat[P->N + i] = data_cat[i];  // ExplicitInit
+            for (int64_t t = 0; t < P->N; ++t) {
+                const int64_t g = P->path[t];
+                if (P->status[g] != SGS_NODE_KRIGED) {
+                    for (int l = 0; l < ncat; ++l) p[l] = pr[l];
+                } else {
+                    const int32_t* nb = &P->nbr[(size_t)g * k];
+                    const double* w = &P->w[(size_t)g * k];
+                    for (int l = 0; l < ncat; ++l) {
+                        double s = pr[l];
+                        for (int a = 0; a < P->cnt[g]; ++a) s += w[a] * ((cat[nb[a]] == l ? 1.0 : 0.0) - pr[l]);
+                        p[l] = s;
+                    }
+                }
+                double tot = 0.0;
+                for (int l = 0; l < ncat; ++l) {
+                    p[l] = std::min(std::max(p[l], 0.0), 1.0);
+                    tot += p[l];
+                }
+                if (!(tot > 0.0)) {
+                    for (int l = 0; l < ncat; ++l) p[l] = pr[l];
+                    tot = 1.0;
+                }
+                const double uu = u ? u[(size_t)r * P->N + g] : uniform_of(seed, g, r);
+                int c = ncat - 1;
+                double cum = 0.0;
+                for (int l = 0; l < ncat - 1; ++l) {
+                    cum += p[l] / tot;
+                    if (uu < cum) {
+                        c = l;
+                        break;
+                    }
+                }
+                cat[g] = c;
+            }
+            for (int64_t g = 0; g < P->N; ++g) out[(size_t)r * P->N + g] = cat[g];
+        }
+    }
+    return SGS_OK;
+}
+
 extern "C" int oracle_neighbors(const oracle_plan* P, int32_t* idx, int32_t* count) {
     if (!P) return fail(SGS_ERR_ARG, "null plan");
     if (idx) std::memcpy(idx, P->nbr.data(), P->nbr.size() * sizeof(int32_t));

@@ -54,6 +54,14 @@ int oracle_solve(oracle_plan* plan, int64_t t_begin, int64_t t_end, int64_t stri
 int oracle_simulate(oracle_plan* plan, int32_t nreals, const double* z, uint64_t seed,
                     double* out, int64_t t_end, int nthreads);
 
+/* Sequential indicator simulation on the prepared plan: ncat categories,
+ * prior probabilities prob, data categories data_cat (D); u: nreals x N
+ * uniforms or NULL (oracle_uniforms of seed); out: nreals x N categories. */
+int oracle_simulate_indicator(oracle_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat,
+                              int32_t nreals, const double* u, uint64_t seed, int32_t* out, int nthreads);
+/* Uniforms of the seeded indicator draws: u[r*nnodes + g]. */
+void oracle_uniforms(uint64_t seed, int64_t nnodes, int32_t nreals, double* u);
+
 /* Posterior mean and variance by simple kriging from the data alone, every
  * grid node (NaN where the reference's prediction is missing). */
 int oracle_krige(oracle_plan* plan, double* mean, double* var, int nthreads);
