@@ -19,6 +19,7 @@ Under torchrun each rank simulates its own 256 realizations on its own GPU
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -26,6 +27,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "geostatsprocesses.jl_gb300"))
@@ -249,16 +252,16 @@ def time_device(wl, args, torch, ws, network=None):
         plan.set_network(network)
     R = wl.nreals
     Rp = (R + 3) // 4 * 4
-    dt = torch.float64 if wl.method.precision == "fp64" else torch.float32
-    V = torch.empty(plan.N * Rp, dtype=dt, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
+    # sweep autotuner: once per plan, outside the timed region
+    plan.prepare()
+    dt = torch.float64 if plan.values_fp64() else torch.float32
+    V = torch.empty(plan.N * Rp, dtype=dt, device="cuda")
 
     def step(i):
         plan.prepare()
-        plan.simulate_device(R, None, 1000 + i, V.data_ptr(), stream)
+        plan.simulate_device(R, None, 1000 + i, V, stream)
 
-    # sweep autotuner: once per plan, outside the timed region
-    plan.prepare()
     if args.sweep_config:
         plan.set_sweep(**json.loads(args.sweep_config))
         sweep_cfg, sweep_tried = dict(plan.sweep_config()), []
@@ -286,10 +289,18 @@ def time_device(wl, args, torch, ws, network=None):
     barrier(ws)
     ms = e0.elapsed_time(e1) / args.steps
     inf = plan.info()
+    # kriging-system sizes (grid + data neighbours of every node that solved
+    # a system), after the timed region: the solve's algorithmic FLOPs
+    cnt = np.empty(plan.N, dtype=np.int32)
+    st = np.empty(plan.N, dtype=np.int32)
+    plan._check(plan.lib.sgs_plan_neighbors(plan.h, None, cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    plan._check(plan.lib.sgs_plan_weights(plan.h, None, None, st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+    sizes = np.bincount(cnt[st == 0], minlength=plan.k + 1)
     res = dict(ms=max_over_ranks(ws, ms), launches=(inf.launches - launches0), info=inf,
                sweep_config=sweep_cfg, sweep_tried=sweep_tried,
                ms_sweep=statistics.mean(sweeps), ms_solve=statistics.mean(solves),
-               ms_search=statistics.mean(searches), ms_levels=statistics.mean(levels))
+               ms_search=statistics.mean(searches), ms_levels=statistics.mean(levels),
+               system_sizes=sizes)
     plan.close()
     del V
     return res
@@ -352,8 +363,8 @@ def time_batch(bw, args, torch, ws, precision):
     t_create = time.perf_counter() - t0
     R = bw.nreals
     Rp = (R + 3) // 4 * 4
-    dt = torch.float64 if precision == "fp64" else torch.float32
     B.prepare()
+    dt = torch.float64 if B.values_fp64() else torch.float32
     V = torch.empty(B.nnodes * Rp, dtype=dt, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
     if args.sweep_config:
@@ -364,7 +375,7 @@ def time_batch(bw, args, torch, ws, precision):
 
     def step(i):
         B.prepare()
-        B.simulate_device(R, 1000 + i, V.data_ptr(), stream)
+        B.simulate_device(R, 1000 + i, V, stream)
 
     for i in range(args.warmup):
         step(i)
@@ -474,7 +485,8 @@ def main_batch(args, torch, ws, rank, uuid):
     # neighbour row reads + value writes (rows of Rp values), and per grid
     # neighbour an int32 index and a (hi, lo) weight, per node its id, count,
     # CSR row start, (hi, lo) b0 and sigma
-    alg_bytes = (sum_m + N) * Rp * 4 + sum_m * 12 + N * 32
+    sv = 8 if inf.values_fp64 else 4
+    alg_bytes = (sum_m + N) * Rp * sv + sum_m * 12 + N * 32
     try:
         peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
     except Exception:
@@ -489,15 +501,16 @@ def main_batch(args, torch, ws, rank, uuid):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32",
+        "vs_baseline": None, "dtype": "f32 (f64 values)" if inf.values_fp64 else "f32",
         "data": "synthetic (seeded PCG64 domains, variograms, data and paths; on-device Philox normals)",
         "config": {"workload": bw.name, "ndomains": len(bw.items), "nodes": N, "nreals": R,
-                   "ndata": int(inf.ndata), "precision": "FP32 LHS+Cholesky, FP64 refinement residual and variance",
+                   "ndata": int(inf.ndata), "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
                    "parallelism": f"replicas x{ws}",
                    "l2": "inputs larger than L2 (sweep tables %.1f GB)" % ((sum_m * 12 + N * 32) / 1e9)},
         "phases_ms": fast["phases"], "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior),
         "n_fp64_fallback": int(inf.n_fp64_fallback), "bin_systems": [int(x) for x in inf.bin_systems],
         "device_gb": inf.device_bytes / 1e9, "s_create": round(fast["s_create"], 2),
+        "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
         "roofline": {"kernel": "sweep_flow_kernel<float, CSR> (one persistent dataflow launch)", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": None, "algorithmic_bytes": alg_bytes, "ms": ms_sweep},
@@ -593,7 +606,7 @@ def main():
     # roofline of the sweep (kernel c): algorithmic bytes of one sweep
     inf = fast["info"]
     sum_m = int(inf.sum_grid_neighbors)
-    sv = 4
+    sv = 8 if inf.values_fp64 else 4
     # neighbour row reads + value writes, plus the sweep tables: per grid
     # neighbour an int32 index and a (hi, lo) float2 weight, per node its id,
     # neighbour count, (hi, lo) b0 and (hi, lo) sigma
@@ -629,6 +642,22 @@ def main():
                 "algorithmic_bytes": alg_bytes,
                 "ms": fast["ms_sweep"]}
 
+    # the solve (kernel b) is bound by the FP32 pipe: per kriging system of n
+    # neighbours, Gauss-Jordan inversion 2 n^3 FLOPs plus two refinement steps
+    # (residual and correction, 2 n^2 each) = 2 n^3 + 8 n^2; peak = 152 SMs x
+    # 128 FP32 lanes x 2 FLOPs x the maximum SM clock (nominal, not measured)
+    sz = fast["system_sizes"]
+    nn = np.arange(sz.size, dtype=np.float64)
+    solve_flops = float(np.sum(sz * (2 * nn ** 3 + 8 * nn ** 2)))
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    solve_roof = {"kernel": "solve_fp32_kernel<NMAX> (+ lag table, FP64 fallbacks): one solve phase",
+                  "bound": "fp32", "achieved": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12,
+                  "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": "nominal (SM count x lanes x max clock)",
+                  "frac": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12 / fp32_peak,
+                  "algorithmic_flops": solve_flops, "systems": int(sz.sum()),
+                  "mean_system_size": float(np.sum(sz * nn) / max(1, sz.sum())), "ms": fast["ms_solve"]}
+
     cpu = None
     if not args.no_cpu:
         v, cores, sample, _ = cpu_sample(wl, args.cpu_nodes)
@@ -638,17 +667,19 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32",
+        "vs_baseline": None, "dtype": "f32 (f64 values)" if inf.values_fp64 else "f32",
         "data": "synthetic (seeded PCG64 grid data and path; on-device Philox normals)",
         "config": {"workload": wl.name, "grid": list(wl.domain.dims), "nodes": N,
                    "ndata": 0 if wl.data is None else wl.data.nrow(), "maxneighbors": wl.method.maxneighbors,
-                   "nreals": R, "precision": "FP32 LHS+Cholesky, FP64 refinement residual and variance",
+                   "nreals": R, "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
                    "warm_start": False, "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (value array %.1f GB)" % (N * R * 4 / 1e9)},
+                   "l2": "inputs larger than L2 (value array %.1f GB)" % (N * R * sv / 1e9)},
         "phases_ms": {"search": fast["ms_search"], "levels": fast["ms_levels"], "solve": fast["ms_solve"],
                       "sweep": fast["ms_sweep"]},
         "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior), "n_fp64_fallback": int(inf.n_fp64_fallback),
+        "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
         "roofline": roofline,
+        "solve_roofline": solve_roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(fast["launches"]),

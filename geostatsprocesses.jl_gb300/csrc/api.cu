@@ -89,8 +89,17 @@ struct sgs_plan {
     double ind_prob[IND_MAX_CAT] = {};
     int32_t* d_ind_cat = nullptr;
     double *d_ind_wsum = nullptr, *d_ind_dsum = nullptr;
+    // FP32 refinement whose weights amplify the rounding of FP32 values: the
+    // sweep keeps FP64 values, from FP64 copies of the (hi, lo) tables
+    unsigned int* d_wl1 = nullptr;
+    bool promote = false;
+    SweepTables<double> t64p{};
     sgs_info info{};
 };
+
+// the sweep's value type and the tables it reads
+static bool values_fp64(const sgs_plan* P) { return P->precision == SGS_PREC_FP64 || P->promote; }
+static const SweepTables<double>& sweep64(const sgs_plan* P) { return P->promote ? P->t64p : P->t64; }
 
 // ---------------------------------------------------------------------------
 namespace {
@@ -600,6 +609,8 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     s.w_full = w_full;
     s.sigma_full = sigma_full;
     s.sum_m = P->d_sum_m;
+    s.wl1_max = P->d_wl1;
+    CK(P, cudaMemsetAsync(P->d_wl1, 0, sizeof(unsigned int), P->stream));
     if (P->ind_ncat) {
         s.ind_cat = P->d_ind_cat;
         s.ncat = P->ind_ncat;
@@ -664,6 +675,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         if ((rc = dalloc(P, &P->d_status, N))) return rc;
         if ((rc = dalloc(P, &P->d_scratch, 16))) return rc;
         if ((rc = dalloc(P, &P->d_sum_m, 1))) return rc;
+        if ((rc = dalloc(P, &P->d_wl1, 1))) return rc;
     }
     cudaStream_t st = P->stream;
 
@@ -786,6 +798,25 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     }
     CK(P, cudaEventRecord(P->ev[3], st));
     if ((rc = run_solve(P, nullptr, nullptr))) return rc;
+    {
+        unsigned int wl1 = 0;
+        CK(P, cudaMemcpyAsync(&wl1, P->d_wl1, sizeof(wl1), cudaMemcpyDeviceToHost, st));
+        CK(P, cudaStreamSynchronize(st));
+        P->info.d2h_bytes += sizeof(wl1);
+        float f;
+        std::memcpy(&f, &wl1, sizeof(f));
+        P->info.weight_l1_max = f;
+        P->promote = P->precision == SGS_PREC_FP32_REFINE && f > SGS_FP32_VALUE_L1_LIMIT && !P->data_only;
+        P->info.values_fp64 = values_fp64(P) ? 1 : 0;
+        if (P->promote) {
+            if (!P->t64p.w) {
+                if ((rc = dalloc(P, &P->t64p.w, (size_t)N * k))) return rc;
+                if ((rc = dalloc(P, &P->t64p.b0, N))) return rc;
+                if ((rc = dalloc(P, &P->t64p.sigma, N))) return rc;
+            }
+            LAUNCH(P, 1, launch_tables_to_fp64(P->t32, P->t64p, N, N * (int64_t)k, st));
+        }
+    }
     CK(P, cudaEventRecord(P->ev[4], st));
     CK(P, cudaStreamSynchronize(st));
     dfree(P, d_lcount);
@@ -826,8 +857,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         // all levels in one cooperative launch (per-level launches if the
         // device or the launch configuration does not allow it)
         cudaError_t e;
-        if (P->precision == SGS_PREC_FP64)
-            e = launch_sweep_all_fp64(P->t64, P->k, P->d_loff, P->nlevels, Rp, (const double*)z, seed, (double*)V, st);
+        if (values_fp64(P))
+            e = launch_sweep_all_fp64(sweep64(P), P->k, P->d_loff, P->nlevels, Rp, (const double*)z, seed, (double*)V, st);
         else
             e = launch_sweep_all_fp32(P->t32, P->k, P->d_loff, P->nlevels, Rp, (const float*)z, seed, (float*)V, st);
         if (e == cudaSuccess) {
@@ -877,8 +908,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
             f.tight = c.tight;
             f.wait_ns = 10000000000ull;  // 10 s: far beyond any dependency chain
             cudaError_t e;
-            if (P->precision == SGS_PREC_FP64)
-                e = launch_sweep_flow_fp64(P->t64, P->k, Rp, W, G, (const double*)z, seed, (double*)V, f, P->nsm, st);
+            if (values_fp64(P))
+                e = launch_sweep_flow_fp64(sweep64(P), P->k, Rp, W, G, (const double*)z, seed, (double*)V, f, P->nsm, st);
             else
                 e = launch_sweep_flow_fp32(P->t32, P->k, Rp, W, G, (const float*)z, seed, (float*)V, f, P->nsm, st);
             if (e != cudaSuccess) return cuda_err(P, e, "sweep launch");
@@ -890,8 +921,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         for (int l = lo; l < hi; ++l) {
             const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
             cudaError_t e;
-            if (P->precision == SGS_PREC_FP64)
-                e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
+            if (values_fp64(P))
+                e = launch_sweep_fp64(sweep64(P), P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
             else
                 e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g,
                                       (p1 - p0) < (int64_t)c.split_nodes);
@@ -899,7 +930,7 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
             if (p1 > p0) P->info.launches++;
         }
         if (phi < P->N) {
-            const int32_t* node = P->precision == SGS_PREC_FP64 ? P->t64.node : P->t32.node;
+            const int32_t* node = values_fp64(P) ? sweep64(P).node : P->t32.node;
             if (phi > plo) LAUNCH(P, 1, launch_flow_mark(node, plo, phi, H, P->N, P->d_done, epoch, st));
             if (plo > 0) CK(P, cudaMemsetAsync(P->d_flow, 0, sizeof(unsigned long long), st));  // ticket only
             if ((rc = flow(phi, P->N))) return rc;
@@ -909,8 +940,8 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
     for (int l = 0; l < P->nlevels; ++l) {
         const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
         cudaError_t e;
-        if (P->precision == SGS_PREC_FP64)
-            e = launch_sweep_fp64(P->t64, P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
+        if (values_fp64(P))
+            e = launch_sweep_fp64(sweep64(P), P->k, p0, p1, Rp, (const double*)z, seed, (double*)V, st);
         else
             e = launch_sweep_fp32(P->t32, P->k, p0, p1, Rp, (const float*)z, seed, (float*)V, st, c.lanes_g,
                                   (p1 - p0) < (int64_t)c.split_nodes);
@@ -943,7 +974,7 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     CK(P, cudaSetDevice(P->device));
     const int64_t N = P->N;
     const int Rp = (R + 3) / 4 * 4;
-    const size_t es = P->precision == SGS_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t es = values_fp64(P) ? sizeof(double) : sizeof(float);
     cudaStream_t st = P->stream;
     int rc;
     void* V = nullptr;
@@ -955,7 +986,7 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
         if ((rc = dalloc(P, (unsigned char**)&zr, (size_t)N * Rp * es))) { dfree(P, V); dfree(P, zin); return rc; }
         CK(P, cudaMemcpyAsync(zin, z, (size_t)N * R * sizeof(double), cudaMemcpyHostToDevice, st));
         P->info.h2d_bytes += (int64_t)N * R * sizeof(double);
-        if (P->precision == SGS_PREC_FP64) LAUNCH(P, 1, launch_z_to_rows_fp64(zin, N, R, Rp, (double*)zr, st));
+        if (values_fp64(P)) LAUNCH(P, 1, launch_z_to_rows_fp64(zin, N, R, Rp, (double*)zr, st));
         else LAUNCH(P, 1, launch_z_to_rows_fp32(zin, N, R, Rp, (float*)zr, st));
     }
     CK(P, cudaEventRecord(P->ev[5], st));
@@ -967,7 +998,7 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     // address, else in chunks of realizations through a device buffer
     double* dout = pinned_device_view(out);
     if (dout) {
-        if (P->precision == SGS_PREC_FP64)
+        if (values_fp64(P))
             LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V, N, R, Rp, P->mean, dout, st));
         else
             LAUNCH(P, 1, launch_rows_to_out_fp32((const float*)V, N, R, Rp, P->mean, dout, st));
@@ -980,7 +1011,7 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     for (int64_t r0 = 0; !dout && r0 < R; r0 += rchunk) {
         const int rn = (int)std::min<int64_t>(rchunk, R - r0);
         // rows_to_out reads realizations [r0, r0+rn) of each row
-        if (P->precision == SGS_PREC_FP64)
+        if (values_fp64(P))
             LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V + r0, N, rn, Rp, P->mean, ob, st));
         else
             LAUNCH(P, 1, launch_rows_to_out_fp32((const float*)V + r0, N, rn, Rp, P->mean, ob, st));
@@ -1147,7 +1178,7 @@ extern "C" int sgs_plan_tune_sweep(sgs_plan* P, int32_t R, sgs_sweep_config* cho
     CK(P, cudaSetDevice(P->device));
     const int Rp = (R + 3) / 4 * 4;
     const int cpn = Rp / 4;
-    const bool fp64 = P->precision == SGS_PREC_FP64;
+    const bool fp64 = values_fp64(P);
     const size_t es = fp64 ? sizeof(double) : sizeof(float);
     void* V = nullptr;
     int rc;

@@ -376,8 +376,27 @@ struct sgs_batch {
     sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0, 0.f};
     bool sweep_graph_valid = false;
     bool sweep_pending = false;    // a device-resident sweep not yet checked
+    unsigned int* d_wl1 = nullptr; // largest sum of |grid weights| (FP32 bits)
+    bool promote = false;          // FP32 refinement, FP64 values (weights amplify rounding)
+    bool sweep_promote = false;    // value type the captured sweep graph was built for
     sgs_batch_info info{};
 };
+
+// the sweep's value type; promoted batches read the packed (hi, lo) FP32
+// tables through an FP64-typed view (FlowArgs::pairs)
+static bool values_fp64(const sgs_batch* B) { return B->precision == SGS_PREC_FP64 || B->promote; }
+static SweepTables<double> sweep64(const sgs_batch* B) {
+    if (!B->promote) return B->t64;
+    SweepTables<double> v{};
+    v.node = B->t32.node;
+    v.m = B->t32.m;
+    v.idx = B->t32.idx;
+    v.w = reinterpret_cast<double*>(B->t32.w);
+    v.b0 = reinterpret_cast<double*>(B->t32.b0);
+    v.sigma = reinterpret_cast<double*>(B->t32.sigma);
+    v.off = B->t32.off;
+    return v;
+}
 
 namespace {
 
@@ -616,6 +635,7 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
     if ((rc = balloc(B, &B->d_sums, 4))) return rc;
     if ((rc = balloc(B, &B->d_flow, 2))) return rc;
     if ((rc = balloc(B, &B->d_seed, 1))) return rc;
+    if ((rc = balloc(B, &B->d_wl1, 1))) return rc;
 
     // descriptors
     B->search.resize(nd);
@@ -664,6 +684,7 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
         s.fallback = B->d_fallback;
         s.nfallback = B->d_fbdesc;
         s.sum_m = B->d_sums + 1;
+        s.wl1_max = B->d_wl1;
         s.node0 = B->noff[d];
 
         ld[d] = LevelDom{B->noff[d], B->nbr0[d], (int32_t)h.N, h.k};
@@ -745,6 +766,7 @@ static int enqueue_prepare(sgs_batch* B, int64_t& launched) {
     // kriging systems by size class
     BCK(B, cudaMemsetAsync(B->d_fbdesc, 0, 2 * sizeof(int32_t), st));
     BCK(B, cudaMemsetAsync(B->d_sums + 1, 0, sizeof(unsigned long long), st));
+    BCK(B, cudaMemsetAsync(B->d_wl1, 0, sizeof(unsigned int), st));
     for (int b = 0; b < NBIN; ++b) {
         if (B->precision == SGS_PREC_FP64)
             BLAUNCH(B, launch_solve_fp64_batch(bin_nmax(b), B->d_solve, B->d_noff, nd, B->d_order, B->d_blist,
@@ -828,13 +850,22 @@ extern "C" int sgs_batch_prepare(sgs_batch* B) {
     int32_t hs[4] = {0, 0, 0, 0};
     unsigned long long su[4] = {0, 0, 0, 0};
     int32_t hb[2 * NBIN], hf[2];
+    unsigned int wl1 = 0;
+    BCK(B, cudaMemcpyAsync(&wl1, B->d_wl1, sizeof(wl1), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hs, B->d_scratch, sizeof(hs), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(su, B->d_sums, sizeof(su), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hb, B->d_bdesc, sizeof(hb), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hf, B->d_fbdesc, sizeof(hf), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaStreamSynchronize(st));
-    B->info.d2h_bytes += sizeof(hs) + sizeof(su) + sizeof(hb) + sizeof(hf);
+    B->info.d2h_bytes += sizeof(hs) + sizeof(su) + sizeof(hb) + sizeof(hf) + sizeof(wl1);
     if (hs[1]) return berr(B, SGS_ERR_TIMEOUT, "dependency-level wait exceeded its bound");
+    {
+        float f;
+        std::memcpy(&f, &wl1, sizeof(f));
+        B->info.weight_l1_max = f;
+        B->promote = B->precision == SGS_PREC_FP32_REFINE && f > SGS_FP32_VALUE_L1_LIMIT;
+        B->info.values_fp64 = values_fp64(B) ? 1 : 0;
+    }
     B->info.nlevels = hs[0] + 1;
     B->info.sum_grid_neighbors = (int64_t)su[1];
     B->info.n_prior = (int64_t)su[2];
@@ -872,8 +903,9 @@ static int enqueue_sweep(sgs_batch* B, int Rp, const void* z, void* V, cudaStrea
     f.tight = c.tight;
     f.wait_ns = 10000000000ull;  // 10 s: far beyond any dependency chain
     f.seed_dev = B->d_seed;
-    if (B->precision == SGS_PREC_FP64)
-        BLAUNCH(B, launch_sweep_flow_fp64(B->t64, B->kmax, Rp, W, G, (const double*)z, 0, (double*)V, f, B->nsm, st));
+    f.pairs = B->promote ? 1 : 0;
+    if (values_fp64(B))
+        BLAUNCH(B, launch_sweep_flow_fp64(sweep64(B), B->kmax, Rp, W, G, (const double*)z, 0, (double*)V, f, B->nsm, st));
     else
         BLAUNCH(B, launch_sweep_flow_fp32(B->t32, B->kmax, Rp, W, G, (const float*)z, 0, (float*)V, f, B->nsm, st));
     return SGS_OK;
@@ -908,7 +940,8 @@ static int check_sweep_error(sgs_batch* B) {
 static int run_sweep_graph(sgs_batch* B, int Rp, uint64_t seed, void* V, cudaStream_t st) {
     int rc;
     if ((rc = ensure_flags(B, Rp))) return rc;
-    if (!B->sweep_exec || B->sweep_Rp != Rp || B->sweep_V != V || B->sweep_stream != st || !B->sweep_graph_valid) {
+    if (!B->sweep_exec || B->sweep_Rp != Rp || B->sweep_V != V || B->sweep_stream != st || !B->sweep_graph_valid ||
+        B->sweep_promote != B->promote) {
         if (B->sweep_exec) {
             BCK(B, cudaStreamSynchronize(B->sweep_stream ? B->sweep_stream : B->stream));
             cudaGraphExecDestroy(B->sweep_exec);
@@ -934,6 +967,7 @@ static int run_sweep_graph(sgs_batch* B, int Rp, uint64_t seed, void* V, cudaStr
         B->sweep_Rp = Rp;
         B->sweep_V = V;
         B->sweep_stream = st;
+        B->sweep_promote = B->promote;
         B->sweep_graph_valid = true;
     }
     *B->h_seed = seed;
@@ -965,7 +999,7 @@ extern "C" int sgs_batch_simulate(sgs_batch* B, int32_t R, const double* z, uint
     BCK(B, cudaSetDevice(B->device));
     cudaStream_t st = B->stream;
     const int Rp = (R + 3) / 4 * 4;
-    const bool f64 = B->precision == SGS_PREC_FP64;
+    const bool f64 = values_fp64(B);
     const size_t es = f64 ? sizeof(double) : sizeof(float);
     int rc;
     unsigned char* V = nullptr;
@@ -1136,7 +1170,7 @@ extern "C" int sgs_batch_tune_sweep(sgs_batch* B, int32_t R, sgs_sweep_config* c
     if (R < 1) return berr(B, SGS_ERR_ARG, "invalid nreals");
     BCK(B, cudaSetDevice(B->device));
     const int Rp = (R + 3) / 4 * 4, cpn = Rp / 4;
-    const size_t es = B->precision == SGS_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t es = values_fp64(B) ? sizeof(double) : sizeof(float);
     int rc;
     unsigned char* V = nullptr;
     if ((rc = balloc(B, &V, (size_t)B->Ntot * Rp * es))) return rc;

@@ -138,6 +138,8 @@ struct FlowArgs {
     uint64_t wait_ns;            // longest wait for one flag before giving up
     const uint64_t* seed_dev;    // nullptr, or the draw seed in device memory (read at
                                  // launch; lets a captured graph take a new seed)
+    int pairs;                   // FP64 values, packed tables: every 8-byte weight, b0
+                                 // and sigma entry is an FP32 (hi, lo) pair
 };
 
 struct SolveArgs {
@@ -175,6 +177,8 @@ struct SolveArgs {
     int ncat;
     double* ind_wsum;            // [P]
     double* ind_dsum;            // [P][ncat]
+    unsigned int* wl1_max;       // optional: FP32 bit pattern of the largest sum of
+                                 // |weights| of grid neighbours over the systems
 };
 
 // Sequential indicator simulation (indicator.cu).
@@ -286,6 +290,10 @@ cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, d
 // node-major centred values -> realization-major double with the mean added
 cudaError_t launch_rows_to_out_fp32(const float* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
 cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, double mu, double* out, cudaStream_t s);
+// FP64 copies of packed (hi, lo) sweep tables: w of `entries` weights, b0 and
+// sigma of P positions (node, m, idx and off are shared with the source)
+cudaError_t launch_tables_to_fp64(const SweepTables<float>& src, SweepTables<double>& dst, int64_t P,
+                                  int64_t entries, cudaStream_t s);
 cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2, cudaStream_t s);
 // learned warm start (learned.cu)
 cudaError_t launch_nn_features(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,

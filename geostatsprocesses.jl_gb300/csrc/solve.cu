@@ -188,7 +188,7 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
     const int k = a.k;
     const int64_t row = table_row(tab, pos, k);
     int m = 0;
-    double b0 = 0.0;
+    double b0 = 0.0, l1 = 0.0;
     if (status == SGS_NODE_KRIGED_) {
         for (int base = 0; base < n; base += 32) {
             const int q = base + lane;
@@ -198,12 +198,17 @@ __device__ void write_row(const SolveArgs& a, const SweepTables<O>& tab, int64_t
                 const int j = m + __popc(b & lanemask_lt());
                 tab.idx[row + j] = a.nbr[(int64_t)g * k + q] + (int32_t)a.node0;
                 put(tab.w, row + j, w[q]);
+                l1 += fabs(w[q]);
             } else if (q < n) {
                 b0 += w[q] * (a.data_val[info[q].did] - a.mu);
             }
             m += __popc(b);
         }
         b0 = warp_sum(b0);
+        if (a.wl1_max) {
+            l1 = warp_sum(l1);
+            if (lane == 0) atomicMax(a.wl1_max, __float_as_uint((float)l1));
+        }
     }
     if (a.ind_wsum)
         write_indicator_sums(a, pos, n, info, status == SGS_NODE_KRIGED_, [&](int q) { return w[q]; }, lane);
@@ -705,6 +710,7 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
         const int64_t row = table_row(tab, pos, k);
         DFAcc b0acc;
         b0acc.init({0.0f, 0.0f});
+        float l1 = 0.0f;
         if (status == SGS_NODE_KRIGED_) {
             for (int b = 0; b < n; b += 32) {
                 const int q = b + lane;
@@ -714,10 +720,16 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     const int j = m + __popc(bal & lanemask_lt());
                     tab.idx[row + j] = a.nbr[(int64_t)g * k + q] + (int32_t)a.node0;
                     reinterpret_cast<float2*>(tab.w)[row + j] = make_float2(w[q].hi, w[q].lo);
+                    l1 += fabsf(w[q].hi);
                 } else if (q < n) {
                     b0acc.add_prod(w[q], df_from_double(a.data_val[info[q].did] - a.mu));
                 }
                 m += __popc(bal);
+            }
+            if (a.wl1_max) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) l1 += __shfl_xor_sync(FULL_MASK, l1, o);
+                if (lane == 0) atomicMax(a.wl1_max, __float_as_uint(l1));
             }
         }
         const DF b0 = warp_sum_df(b0acc.value());
@@ -872,6 +884,32 @@ cudaError_t launch_solve_fp64_into_fp32_batch(int kl, const SolveArgs* doms, con
                                               const int32_t* order, const int32_t* list, const int32_t* desc,
                                               const SweepTables<float>& t, int nsm, cudaStream_t s) {
     return launch_solve64_batch<float>(kl, doms, noff, ndom, order, list, desc, t, nsm, s);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void tables_to_fp64_kernel(const SweepTables<float> src, SweepTables<double> dst, int64_t P,
+                                      int64_t entries) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < entries; i += stride)
+        dst.w[i] = (double)src.w[2 * i] + (double)src.w[2 * i + 1];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P; i += stride) {
+        dst.b0[i] = (double)src.b0[2 * i] + (double)src.b0[2 * i + 1];
+        dst.sigma[i] = (double)src.sigma[2 * i] + (double)src.sigma[2 * i + 1];
+    }
+}
+
+cudaError_t launch_tables_to_fp64(const SweepTables<float>& src, SweepTables<double>& dst, int64_t P, int64_t entries,
+                                  cudaStream_t s) {
+    dst.node = src.node;
+    dst.m = src.m;
+    dst.idx = src.idx;
+    dst.off = src.off;
+    const int64_t n = entries > P ? entries : P;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 65535) blocks = 65535;
+    if (blocks < 1) blocks = 1;
+    tables_to_fp64_kernel<<<blocks, 256, 0, s>>>(src, dst, P, entries);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

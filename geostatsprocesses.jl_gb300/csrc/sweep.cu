@@ -603,19 +603,27 @@ __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int
 template <int G, bool CSR>
 __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, int k, int64_t pos, int g, int m, int Rp,
                                                 int c0, int W, int lane, const double* __restrict__ z, uint64_t seed,
-                                                double* __restrict__ V) {
+                                                double* __restrict__ V, int pairs) {
     const int cpn = Rp >> 2;
     const int S = 32 / W, s = lane / W, cl = lane % W;
     const int64_t row = CSR ? t.off[pos] : pos * (int64_t)k;
     const int32_t* idx = t.idx + row;
     const double* w = t.w + row;
+    // pairs: each 8-byte table entry holds an FP32 (hi, lo) pair
+    auto entry = [pairs](const double* p, int64_t i) {
+        if (pairs) {
+            const float2 v = reinterpret_cast<const float2*>(p)[i];
+            return (double)v.x + (double)v.y;
+        }
+        return p[i];
+    };
     D4 a[G];
 #pragma unroll
     for (int gi = 0; gi < G; ++gi) a[gi] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll 4
     for (int j = s; j < m; j += S) {
         const double2* row = reinterpret_cast<const double2*>(V + (int64_t)idx[j] * Rp);
-        const double wj = w[j];
+        const double wj = entry(w, j);
 #pragma unroll
         for (int gi = 0; gi < G; ++gi) {
             const int ch = c0 + cl + gi * W;
@@ -638,7 +646,7 @@ __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, in
             a[gi].w += __shfl_xor_sync(FULL_MASK, a[gi].w, o);
         }
     if (s == 0) {
-        const double b0 = t.b0[pos], sg = t.sigma[pos];
+        const double b0 = entry(t.b0, pos), sg = entry(t.sigma, pos);
 #pragma unroll
         for (int gi = 0; gi < G; ++gi) {
             const int ch = c0 + cl + gi * W;
@@ -688,7 +696,7 @@ __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables
             const bool ok = flow_wait(t.idx + (CSR ? t.off[pos] : pos * (int64_t)k), m, done_q, f, lane);
             if (ok) {
                 if constexpr (sizeof(T) == 4) flow_piece_fp32<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
-                else flow_piece_fp64<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
+                else flow_piece_fp64<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V, CSR ? f.pairs : 0);
             } else if (lane == 0) {
                 atomicExch(f.err, 1);
             }

@@ -124,6 +124,9 @@ class SgsInfo(C.Structure):
         ("h2d_bytes", C.c_int64),
         ("d2h_bytes", C.c_int64),
         ("sum_grid_neighbors", C.c_int64),
+        ("weight_l1_max", C.c_double),
+        ("values_fp64", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -147,6 +150,9 @@ class SgsBatchInfo(C.Structure):
         ("h2d_bytes", C.c_int64),
         ("d2h_bytes", C.c_int64),
         ("device_bytes", C.c_int64),
+        ("weight_l1_max", C.c_double),
+        ("values_fp64", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

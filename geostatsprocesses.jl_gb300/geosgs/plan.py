@@ -16,6 +16,19 @@ def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int32))
 
 
+def _device_values(vals, nnodes: int, nreals: int, fp64: bool):
+    """Pointer of a device value array: an int is taken as is; a tensor (any
+    object with data_ptr / element_size / numel) must hold nnodes rows of
+    nreals rounded up to 4 values of the sweep's value type."""
+    if isinstance(vals, int):
+        return vals
+    rp = (nreals + 3) // 4 * 4
+    es = 8 if fp64 else 4
+    if vals.element_size() != es or vals.numel() < nnodes * rp:
+        raise ValueError(f"device values must be {nnodes} x {rp} {'float64' if fp64 else 'float32'} elements")
+    return vals.data_ptr()
+
+
 class Plan:
     """Owns one sgs_plan: geometry, neighbour/weight tables and the sweep schedule
     on the GPU.  `prepare()` runs the neighbour search, the level schedule and
@@ -65,10 +78,19 @@ class Plan:
         self._check(self.lib.sgs_plan_simulate(self.h, nreals, zp, C.c_uint64(seed), _dp(out)))
         return out
 
-    def simulate_device(self, nreals: int, z_ptr: int | None, seed: int, vals_ptr: int, stream: int | None = None):
+    def values_fp64(self) -> bool:
+        """Whether the sweep keeps FP64 values (sgs_info.values_fp64): FP64
+        precision, or FP32 refinement whose weights amplify FP32 rounding."""
+        return bool(self.info().values_fp64)
+
+    def simulate_device(self, nreals: int, z_ptr: int | None, seed: int, vals, stream: int | None = None):
+        """Sweep into device memory: `vals` is a device pointer or a CUDA
+        tensor of N x (nreals rounded up to 4) values of the sweep's type
+        (values_fp64()); tensors are checked."""
+        ptr = _device_values(vals, self.N, nreals, self.values_fp64())
         self._check(self.lib.sgs_plan_simulate_device(
             self.h, nreals, C.c_void_p(z_ptr) if z_ptr else None, C.c_uint64(seed),
-            C.c_void_p(vals_ptr), C.c_void_p(stream) if stream else None))
+            C.c_void_p(ptr), C.c_void_p(stream) if stream else None))
 
     def neighbors(self):
         idx = np.empty((self.N, self.k), dtype=np.int32)
@@ -224,8 +246,16 @@ class Batch:
         self._check(self.lib.sgs_batch_simulate(self.h, nreals, zp, C.c_uint64(seed), _dp(out)))
         return [out[nreals * f: nreals * (f + n)].reshape(nreals, n) for f, n in zip(self.first, self.sizes)]
 
-    def simulate_device(self, nreals: int, seed: int, vals_ptr: int, stream: int | None = None):
-        self._check(self.lib.sgs_batch_simulate_device(self.h, nreals, C.c_uint64(seed), C.c_void_p(vals_ptr),
+    def values_fp64(self) -> bool:
+        """Whether the sweep keeps FP64 values (sgs_batch_info.values_fp64)."""
+        return bool(self.info().values_fp64)
+
+    def simulate_device(self, nreals: int, seed: int, vals, stream: int | None = None):
+        """Seeded sweep into device memory: a device pointer or a CUDA tensor
+        of nnodes x (nreals rounded up to 4) values of the sweep's type
+        (values_fp64()); tensors are checked."""
+        ptr = _device_values(vals, self.nnodes, nreals, self.values_fp64())
+        self._check(self.lib.sgs_batch_simulate_device(self.h, nreals, C.c_uint64(seed), C.c_void_p(ptr),
                                                        C.c_void_p(stream) if stream else None))
 
     def neighbors(self, d: int):

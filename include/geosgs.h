@@ -137,7 +137,20 @@ typedef struct sgs_info {
     int64_t h2d_bytes;        /* bytes copied host -> device by this plan so far */
     int64_t d2h_bytes;        /* bytes copied device -> host by this plan so far */
     int64_t sum_grid_neighbors; /* sum over nodes of grid neighbours used by the sweep */
+    double  weight_l1_max;    /* largest sum of |weights| of a node's grid neighbours:
+                                 how much the sweep amplifies the rounding of stored
+                                 values (nugget-free Gaussian models reach ~100) */
+    int32_t values_fp64;      /* 1: the sweep keeps FP64 values (SGS_PREC_FP64, or
+                                 SGS_PREC_FP32_REFINE with weight_l1_max above
+                                 SGS_FP32_VALUE_L1_LIMIT); sgs_plan_simulate_device
+                                 then takes double arrays                          */
+    int32_t reserved;
 } sgs_info;
+
+/* SGS_PREC_FP32_REFINE stores values in FP32 while weight_l1_max stays below
+ * this; above it the rounding of FP32 values, amplified by the weights, could
+ * exceed 1e-6 relative, so the sweep keeps FP64 values (same weights). */
+#define SGS_FP32_VALUE_L1_LIMIT 4.0
 
 /* Validate the problem, copy geometry, data and path to the device.
  * Replaces preprocess(rng, process, ::SEQSIM, init, domain, data),
@@ -161,8 +174,9 @@ int sgs_plan_simulate(sgs_plan* plan, int32_t nreals, const double* z,
                       uint64_t seed, double* out);
 
 /* Device-resident variant of sgs_plan_simulate: z_dev (node-major
- * [N][nreals], float for SGS_PREC_FP32_REFINE or double for SGS_PREC_FP64,
- * or NULL for seeded draws) and vals_dev (node-major [N][nreals], same type,
+ * [N][nreals rounded up to a multiple of 4], float when sgs_info.values_fp64
+ * is 0 — SGS_PREC_FP32_REFINE with moderate weights — and double when it is
+ * 1, or NULL for seeded draws) and vals_dev (node-major, same shape and type,
  * centred values v - mean) are device pointers; stream is a cudaStream_t
  * (NULL = the plan's stream).  Same reference counterpart as
  * sgs_plan_simulate. */
@@ -315,6 +329,10 @@ typedef struct sgs_batch_info {
     int64_t graph_launches;     /* CUDA graph launches                             */
     int64_t h2d_bytes, d2h_bytes;
     int64_t device_bytes;       /* device memory held by the batch                 */
+    double  weight_l1_max;      /* as sgs_info: largest sum of |grid weights|       */
+    int32_t values_fp64;        /* 1: FP64 values (sgs_batch_simulate_device takes
+                                   double arrays), as sgs_info                      */
+    int32_t reserved;
 } sgs_batch_info;
 
 /* Validate every problem (the first invalid one is named in the error) and
@@ -330,8 +348,8 @@ int sgs_batch_prepare(sgs_batch* batch);
  * and realization / 4). */
 int sgs_batch_simulate(sgs_batch* batch, int32_t nreals, const double* z, uint64_t seed, double* out);
 /* Seeded sweep into vals_dev: device array [nnodes][nreals rounded up to a
- * multiple of 4] of centred values (v - mean of the node's domain), float for
- * SGS_PREC_FP32_REFINE, double for SGS_PREC_FP64, rows by global node id.
+ * multiple of 4] of centred values (v - mean of the node's domain), float when
+ * sgs_batch_info.values_fp64 is 0, double when it is 1, rows by global id.
  * Captured in a CUDA graph per (nreals, vals_dev, sweep configuration) and
  * replayed; stream is a cudaStream_t (NULL = the batch's stream). */
 int sgs_batch_simulate_device(sgs_batch* batch, int32_t nreals, uint64_t seed, void* vals_dev, void* stream);

@@ -101,6 +101,34 @@ def test_batch_matches_oracle_per_domain(precision, oracle_mod, geosgs_lib):
 
 
 @pytest.mark.gpu
+def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
+    """A domain whose kriging weights amplify FP32 rounding (a nugget-free
+    Gaussian variogram, sum |w| ~ 100) makes the batch keep FP64 values,
+    read through the packed tables; every domain stays within 1e-6."""
+    bw = workloads.c5_small("fp32", ndomains=5, seed=63)
+    gau = geosgs.GaussianProcess(geosgs.GaussianVariogram(range=6.0, sill=1.0, nugget=0.0), 0.2)
+    grid = geosgs.CartesianGrid((20, 20))
+    bw.items.append(workloads.Workload("gau", gau, grid, None,
+                                       geosgs.GPUSEQSIM(path=geosgs.LinearPath(), maxneighbors=16, precision="fp32"),
+                                       bw.nreals))
+    probs = problems_of(bw, "fp32")
+    B = geosgs.Batch(probs).prepare()
+    info = B.info()
+    assert info.values_fp64 == 1 and info.weight_l1_max > 10.0
+    R = bw.nreals
+    zs = [np.random.default_rng(200 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
+    vals = B.simulate(R, z=zs)
+    seeded = B.simulate(R, seed=3)
+    zall = oracle_mod.normals(3, B.nnodes, R)
+    for d, (p, keep) in enumerate(probs):
+        O = oracle_mod.OraclePlan(p, keep).prepare()
+        assert rel_err(vals[d], O.simulate(R, zs[d])) <= VALUE_TOL, d
+        f, n = int(B.first[d]), int(B.sizes[d])
+        assert rel_err(seeded[d], O.simulate(R, zall[:, f:f + n])) <= VALUE_TOL, d
+    B.close()
+
+
+@pytest.mark.gpu
 def test_batch_graph_replay_and_seeded_draws(oracle_mod, geosgs_lib):
     """Replayed graphs give identical results; seeded draws are Philox keyed
     by the global node id, so the oracle fed those normals agrees."""
@@ -140,8 +168,8 @@ def test_batch_device_values_and_autotuner(oracle_mod, geosgs_lib):
     pinned = torch.empty(R * B.nnodes, dtype=torch.float64, pin_memory=True)
     B._check(B.lib.sgs_batch_simulate(B.h, R, None, C.c_uint64(5), C.cast(pinned.data_ptr(), C.POINTER(C.c_double))))
     np.testing.assert_array_equal(pinned.numpy(), np.concatenate([h.reshape(-1) for h in host]))
-    V = torch.empty((B.nnodes, R), dtype=torch.float32, device="cuda")
-    B.simulate_device(R, 5, V.data_ptr())
+    V = torch.empty((B.nnodes, R), dtype=torch.float64 if B.values_fp64() else torch.float32, device="cuda")
+    B.simulate_device(R, 5, V)
     info = B.info()
     assert info.ms_sweep > 0
     Vh = V.cpu().numpy().astype(np.float64)

@@ -38,7 +38,7 @@ def test_device_ensemble_statistics(precision, geosgs_lib):
     p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
     G = geosgs.Plan(p, keep).prepare()
     R, Rp = 37, 40
-    dt = torch.float32 if precision == "fp32" else torch.float64
+    dt = torch.float64 if G.values_fp64() else torch.float32
     V = torch.empty((G.N, Rp), dtype=dt, device="cuda")
     # the sweep and the statistics on one stream (a NULL stream handle, as
     # torch's default stream has, would select the plan's own stream)
@@ -47,7 +47,7 @@ def test_device_ensemble_statistics(precision, geosgs_lib):
     xs = [-1.0, 0.0, 0.75, 2.5]
     ps = [0.0, 0.1, 0.5, 0.9, 1.0]
     with torch.cuda.stream(st):
-        G.simulate_device(R, None, 3, V.data_ptr(), st.cuda_stream)
+        G.simulate_device(R, None, 3, V, st.cuda_stream)
         m, v = ensemble.mean_var(V, R, Rp, offset=mu)
         c = ensemble.cdf(V, R, xs, Rp, offset=mu)
         cc = ensemble.cdf(V, R, xs, Rp, offset=mu, complement=True)
