@@ -1,0 +1,107 @@
+// peaks.cu — two device throughput probes used by the benchmark as roofline
+// denominators that no driver-side measurement provides: the FP32 FFMA rate
+// (the bound of the kriging solve, which runs on the CUDA cores) and the rate
+// at which kernels write page-locked host memory (the bound of the FP64
+// output that sgs_plan_simulate writes straight into the caller's buffer).
+// Built as its own library (libgeosgs_peaks.so); not part of the C ABI.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace {
+
+// NR independent FFMA chains per thread; the result is stored so that the
+// chains are not removed
+template <int NR>
+__global__ void ffma_chains_kernel(float* out, int iters, float a) {
+    float r[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) r[j] = threadIdx.x * 1e-3f + j;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) r[j] = __fmaf_rn(r[j], a, 0.5f);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) s += r[j];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// streaming 16-byte writes of n2 double2 values
+__global__ void write_stream_kernel(double2* out, int64_t n2, double v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = make_double2(v, v + 1.0);
+}
+
+int sms() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return n;
+}
+
+}  // namespace
+
+// Best of three timed launches of 32 FFMA chains per thread, 8 blocks of 256
+// threads per SM; *tflops = 2 x FFMA lanes per second / 1e12.  0 on success.
+extern "C" int geosgs_peak_fp32(double* tflops) {
+    const int nsm = sms();
+    if (!tflops || nsm <= 0) return 1;
+    const int blocks = nsm * 8, threads = 256, iters = 20000;
+    float* out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)) != cudaSuccess) return 2;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        ffma_chains_kernel<32><<<blocks, threads>>>(out, iters, 0.999f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // the first launch warms up
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess || best <= 0.f) return 3;
+    *tflops = 2.0 * (double)blocks * threads * iters * 32 / (best * 1e-3) / 1e12;
+    return 0;
+}
+
+// Best of three timed kernels writing `bytes` (rounded down to 16) into
+// page-locked host memory through its device address; *gbs = bytes / s / 1e9.
+extern "C" int geosgs_peak_host_write(int64_t bytes, double* gbs) {
+    const int nsm = sms();
+    if (!gbs || nsm <= 0 || bytes < 16) return 1;
+    const int64_t n2 = bytes / 16;
+    void* h = nullptr;
+    if (cudaHostAlloc(&h, (size_t)n2 * 16, cudaHostAllocMapped) != cudaSuccess) return 2;
+    void* hd = nullptr;
+    if (cudaHostGetDevicePointer(&hd, h, 0) != cudaSuccess) {
+        cudaFreeHost(h);
+        return 2;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        write_stream_kernel<<<nsm * 8, 256>>>(static_cast<double2*>(hd), n2, 1.0);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeHost(h);
+    if (err != cudaSuccess || best <= 0.f) return 3;
+    *gbs = (double)n2 * 16 / (best * 1e-3) / 1e9;
+    return 0;
+}

@@ -30,6 +30,18 @@ def test_library_loads_and_exports_every_header_symbol():
     _abi.load_library()
 
 
+def test_peak_probe_library_builds_and_exports():
+    """The benchmark's throughput probes live in their own library, outside
+    the C ABI of include/geosgs.h."""
+    from geosgs import _build
+
+    _build.build()
+    lib = C.CDLL(_build.PEAKS_PATH)
+    for name in ("geosgs_peak_fp32", "geosgs_peak_host_write"):
+        assert hasattr(lib, name), name
+    assert not any(n.startswith("geosgs_peak") for n in header_symbols())
+
+
 def test_create_without_gpu_fails_cleanly():
     try:
         import torch
