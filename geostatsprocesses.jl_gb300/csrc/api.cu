@@ -231,6 +231,46 @@ void sgs::set_thread_error(const char* msg) { g_create_err = msg; }
 
 extern "C" const char* sgs_version(void) { return "geosgs 0.1.0 (sm_103a)"; }
 
+// Diagnostic (exported, not part of the C ABI in include/geosgs.h): runs the
+// dataflow sweep's bounded wait on a flag that nothing sets, with a limit of
+// wait_ns.  *timed_out = 1 when the wait gave up and said so; *elapsed_ns =
+// the launch's duration.  Returns 0, or a negative SGS_ERR_* code when the
+// launch itself failed.
+extern "C" int sgs_selftest_bounded_wait(int64_t wait_ns, int32_t* timed_out, int64_t* elapsed_ns) {
+    if (!timed_out || !elapsed_ns || wait_ns <= 0) return SGS_ERR_ARG;
+    *timed_out = 0;
+    *elapsed_ns = 0;
+    int32_t* d = nullptr;  // [0] the flag, [1] the error word, [2] the neighbour index (0)
+    if (cudaMalloc(&d, 3 * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return SGS_ERR_CUDA;
+    }
+    int rc = SGS_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FlowArgs f{};
+    f.done = d;
+    f.err = d + 1;
+    f.epoch = 1;
+    f.wait_ns = (uint64_t)wait_ns;
+    int32_t herr = 0;
+    float ms = 0.f;
+    if (cudaMemset(d, 0, 3 * sizeof(int32_t)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess || cudaEventRecord(e0) != cudaSuccess ||
+        launch_flow_wait_selftest(d + 2, f, 0) != cudaSuccess || cudaEventRecord(e1) != cudaSuccess ||
+        cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaMemcpy(&herr, d + 1, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        cudaGetLastError();
+        rc = SGS_ERR_CUDA;
+    }
+    *timed_out = herr;
+    *elapsed_ns = (int64_t)(ms * 1e6);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return rc;
+}
+
 extern "C" const char* sgs_last_error(const sgs_plan* plan) {
     return plan ? plan->err.c_str() : g_create_err.c_str();
 }

@@ -277,6 +277,7 @@ cudaError_t launch_sweep_all_fp64(const SweepTables<double>& t, int k, const int
 // per slice of the neighbour list and G chunks of 4 realizations per lane,
 // as returned by flow_layout, which also gives the pieces per row
 int flow_layout(int Rp, int& W, int& G);
+cudaError_t launch_flow_wait_selftest(const int32_t* idx, const FlowArgs& f, cudaStream_t s);
 cudaError_t launch_sweep_flow_fp32(const SweepTables<float>& t, int k, int Rp, int W, int G, const float* z,
                                    uint64_t seed, float* V, const FlowArgs& f, int nsm, cudaStream_t s);
 cudaError_t launch_sweep_flow_fp64(const SweepTables<double>& t, int k, int Rp, int W, int G, const double* z,

@@ -112,7 +112,8 @@ __device__ __forceinline__ uint64_t now_ns() {
 // bounded wait for the barrier phase with the given parity
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
     uint64_t t0 = 0;
-    for (;;) {
+    // bounded by 2 s of elapsed time and by a count of polls
+    for (uint32_t polls = 0; polls < (1u << 26); ++polls) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -126,6 +127,7 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
         if (t0 == 0) t0 = t;
         if (t - t0 > 2000000000ull) return false;
     }
+    return false;
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

@@ -520,13 +520,17 @@ __device__ __forceinline__ uint64_t global_ns() {
 __device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m, const int32_t* done_q,
                                           const FlowArgs& f, int lane) {
     bool ok = true;
+    // bounded by elapsed time and, should the timer stall, by a count of
+    // polls (each takes at least the 64 ns back-off, so the count bound is
+    // reached no earlier than the time bound)
+    const uint64_t max_polls = f.wait_ns / 32 + 1024;
     for (int j = lane; j < m; j += 32) {
         const int32_t* flag = done_q + idx[j];
-        uint64_t t0 = 0;
+        uint64_t t0 = 0, polls = 0;
         while (ld_flag_acquire(flag) != f.epoch) {
             const uint64_t now = global_ns();
             if (t0 == 0) t0 = now;
-            if (now - t0 > f.wait_ns) {
+            if (now - t0 > f.wait_ns || ++polls > max_polls) {
                 ok = false;
                 break;
             }
@@ -705,6 +709,20 @@ __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables
             if (lane == 0) st_flag(done_q + g, f.epoch);
         }
     }
+}
+
+// Self-test of the dataflow wait: one warp waits, with the sweep's own
+// flow_wait, on a flag that nothing sets; the wait must give up after
+// f.wait_ns and report it in *f.err, leaving the context usable.
+__global__ void flow_wait_selftest_kernel(const int32_t* __restrict__ idx, const FlowArgs f) {
+    const int lane = threadIdx.x & 31;
+    const bool ok = flow_wait(idx, 1, f.done, f, lane);
+    if (!ok && lane == 0) atomicExch(f.err, 1);
+}
+
+cudaError_t launch_flow_wait_selftest(const int32_t* idx, const FlowArgs& f, cudaStream_t s) {
+    flow_wait_selftest_kernel<<<1, 32, 0, s>>>(idx, f);
+    return cudaGetLastError();
 }
 
 // Flags of the positions [p0, p1) swept by per-level launches before a

@@ -196,6 +196,25 @@ def test_simulate_into_pinned_host_memory(geosgs_lib):
         G.close()
 
 
+def test_bounded_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
+    """The dataflow sweep's dependency wait, run on a flag that nothing sets
+    (sgs_selftest_bounded_wait), gives up after its limit and reports it; the
+    same process then simulates normally (no fault, no hang)."""
+    import ctypes as C
+
+    lib = C.CDLL(_abi.LIB_PATH)
+    lib.sgs_selftest_bounded_wait.argtypes = [C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    timed_out, elapsed = C.c_int32(0), C.c_int64(0)
+    assert lib.sgs_selftest_bounded_wait(50_000_000, C.byref(timed_out), C.byref(elapsed)) == 0
+    assert timed_out.value == 1
+    assert 50_000_000 <= elapsed.value < 5_000_000_000
+    wl = workloads.small(n=30, k=10, ndata=10, nreals=8, precision="fp32")
+    G, O = both(wl, oracle_mod, "fp32")
+    z = np.random.default_rng(8).standard_normal((8, O.N))
+    assert rel_err(G.simulate(8, z), O.simulate(8, z)) <= VALUE_TOL
+    G.close()
+
+
 def test_error_codes(geosgs_lib):
     from geosgs import _abi
 

@@ -30,6 +30,17 @@ def test_library_loads_and_exports_every_header_symbol():
     _abi.load_library()
 
 
+def test_diagnostic_exports_outside_the_header():
+    """The bounded-wait self-test is exported for the GPU tests but is not
+    part of the C ABI the header declares."""
+    from geosgs import _build
+
+    _build.build()
+    lib = C.CDLL(_abi.LIB_PATH)
+    assert hasattr(lib, "sgs_selftest_bounded_wait")
+    assert "sgs_selftest_bounded_wait" not in header_symbols()
+
+
 def test_peak_probe_library_builds_and_exports():
     """The benchmark's throughput probes live in their own library, outside
     the C ABI of include/geosgs.h."""
