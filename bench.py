@@ -48,9 +48,12 @@ def measure_peaks() -> dict:
         return out
     lib.geosgs_peak_fp32.argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.geosgs_peak_host_write.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+    lib.geosgs_peak_gj_pattern.argtypes = [ctypes.POINTER(ctypes.c_double)]
     v = ctypes.c_double(0.0)
     if lib.geosgs_peak_fp32(ctypes.byref(v)) == 0:
         out["fp32_tflops"] = v.value
+    if lib.geosgs_peak_gj_pattern(ctypes.byref(v)) == 0:
+        out["gj_pattern_tflops"] = v.value
     if lib.geosgs_peak_host_write(ctypes.c_int64(1 << 30), ctypes.byref(v)) == 0:
         out["host_write_gbs"] = v.value
     return out
@@ -684,6 +687,7 @@ def main():
                   "bound": "fp32", "achieved": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12,
                   "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": fp32_src, "nominal_peak": fp32_nominal,
                   "frac": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12 / fp32_peak,
+                  "gj_pattern_peak": probes.get("gj_pattern_tflops"),
                   "algorithmic_flops": solve_flops, "systems": int(sz.sum()),
                   "mean_system_size": float(np.sum(sz * nn) / max(1, sz.sum())), "ms": fast["ms_solve"]}
 

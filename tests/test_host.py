@@ -48,7 +48,7 @@ def test_peak_probe_library_builds_and_exports():
 
     _build.build()
     lib = C.CDLL(_build.PEAKS_PATH)
-    for name in ("geosgs_peak_fp32", "geosgs_peak_host_write"):
+    for name in ("geosgs_peak_fp32", "geosgs_peak_gj_pattern", "geosgs_peak_host_write"):
         assert hasattr(lib, name), name
     assert not any(n.startswith("geosgs_peak") for n in header_symbols())
 
