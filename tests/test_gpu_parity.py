@@ -149,6 +149,35 @@ def test_c3_sampled_neighbours_and_prefix_values(oracle_mod, geosgs_lib):
     assert rel_err(vg[:, first], vo[:, first]) <= VALUE_TOL
 
 
+def test_c4_sampled_neighbours_and_prefix_values(oracle_mod, geosgs_lib):
+    """Full 256^3 grid (16.8 M nodes), unconditional, rotated ellipsoid, k=32,
+    both precisions: neighbours of every 4,001st path rank and of the first
+    3,000 ranks bit-exact, and the values of the first 3,000 path nodes (which
+    depend only on earlier ones) within 1e-6."""
+    for precision in ("fp32", "fp64"):
+        wl = workloads.c4(precision=precision, nreals=4)
+        p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+        G = gpu_plan(p, keep)
+        O = oracle_mod.OraclePlan(p, keep)
+        T = 3000
+        O.search(oracle_mod.TEMPLATE, stride=4001)
+        O.search(oracle_mod.TEMPLATE, t1=T)
+        O.solve(t1=T)
+        path = wl.method.path.permutation(O.N)
+        ranks = np.unique(np.concatenate([np.arange(0, O.N, 4001), np.arange(T)]))
+        nodes = path[ranks]
+        ig, cg = G.neighbors()
+        io, co = O.neighbors()
+        np.testing.assert_array_equal(cg[nodes], co[nodes])
+        np.testing.assert_array_equal(ig[nodes], io[nodes])
+        first = path[:T]
+        z = np.random.default_rng(6).standard_normal((wl.nreals, O.N))
+        vg = G.simulate(wl.nreals, z)
+        vo = O.simulate(wl.nreals, z, t_end=T)
+        assert rel_err(vg[:, first], vo[:, first]) <= VALUE_TOL, precision
+        G.close()
+
+
 def test_levels_schedule_is_valid(geosgs_lib):
     wl = workloads.small(n=50, k=16, ndata=30, precision="fp32")
     p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)

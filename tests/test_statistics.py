@@ -1,0 +1,64 @@
+"""Statistical reproduction: realizations of an unconditional simulation
+reproduce the model's mean (0), variance (the sill) and semivariogram, and
+their pooled values are standard normal.  The reference's own tests pin no
+statistics (test/field.jl checks types and one datum); these checks follow
+the method's definition: SGS draws from the Gaussian process the variogram
+defines, up to the limited neighbourhood, which flattens the semivariogram
+a little near the range.
+
+Setup: a 100 x 100 unit grid, range 15, sill 1, 24 neighbours, one random
+path, 200 seeded realizations.  Empirical semivariogram along x and y at lags
+1..12 (0.5 mean of squared differences over all pairs and realizations)
+within 0.06 of the model; mean within 0.02; variance within 0.05 of the
+sill; pooled 5/25/50/75/95 % quantiles within 0.06 of N(0, 1)'s.  The FP64
+oracle meets the bars with margin (largest semivariogram gap 0.034)."""
+import numpy as np
+import pytest
+
+import geosgs
+
+NORMAL_Q = {0.05: -1.6449, 0.25: -0.6745, 0.5: 0.0, 0.75: 0.6745, 0.95: 1.6449}
+VARIOS = {
+    "sph": (geosgs.SphericalVariogram, 0.0),
+    "exp": (geosgs.ExponentialVariogram, 0.0),
+    "gau": (geosgs.GaussianVariogram, 0.01),
+}
+
+
+def setup(name, precision):
+    cls, nugget = VARIOS[name]
+    grid = geosgs.CartesianGrid((100, 100))
+    proc = geosgs.GaussianProcess(cls(range=15.0, sill=1.0, nugget=nugget), 0.0)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(5), maxneighbors=24, precision=precision)
+    return proc, geosgs.build_problem(proc, grid, None, method)
+
+
+def check_statistics(v, model):
+    """v: realizations x 100 x 100 (node id = x + 100 y)."""
+    hs = np.arange(1, 13)
+    gm = np.asarray(model(hs.astype(float) / 15.0))
+    gx = np.array([0.5 * np.mean((v[:, :, h:] - v[:, :, :-h]) ** 2) for h in hs])
+    gy = np.array([0.5 * np.mean((v[:, h:, :] - v[:, :-h, :]) ** 2) for h in hs])
+    assert np.abs(gx - gm).max() < 0.06, (gx, gm)
+    assert np.abs(gy - gm).max() < 0.06, (gy, gm)
+    assert abs(v.mean()) < 0.02
+    assert abs(v.var() - 1.0) < 0.05
+    q = np.quantile(v.ravel(), list(NORMAL_Q))
+    assert np.abs(q - np.array(list(NORMAL_Q.values()))).max() < 0.06, q
+
+
+@pytest.mark.parametrize("name", sorted(VARIOS))
+def test_oracle_reproduces_the_model(name, oracle_mod):
+    proc, (p, keep) = setup(name, "fp64")
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    check_statistics(O.simulate(200, seed=3).reshape(200, 100, 100), proc.func)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("name", sorted(VARIOS))
+def test_gpu_reproduces_the_model(name, precision, geosgs_lib):
+    proc, (p, keep) = setup(name, precision)
+    G = geosgs.Plan(p, keep).prepare()
+    check_statistics(G.simulate(200, seed=3).reshape(200, 100, 100), proc.func)
+    G.close()
