@@ -129,6 +129,39 @@ def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
 
 
 @pytest.mark.gpu
+def test_batch_of_full_size_c5_domains_sampled(oracle_mod, geosgs_lib):
+    """The first 10 domains of the C5 batch at full size (3.4 M nodes; 2D and
+    3D, sides up to 243, k 8-48, up to 474 data, :range balls up to 37 cells):
+    per domain the oracle searches every ~N/600-th path rank and searches and
+    solves the first 500 ranks; neighbours of those nodes are bit-exact and
+    the values of the first 500 path nodes are within 1e-6."""
+    bw = workloads.c5(ndomains=10)
+    probs = problems_of(bw, "fp32")
+    B = geosgs.Batch(probs).prepare()
+    R = 4
+    zs = [np.random.default_rng(300 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
+    vals = B.simulate(R, z=zs)
+    T = 500
+    for d, (p, keep) in enumerate(probs):
+        O = oracle_mod.OraclePlan(p, keep)
+        N = O.N
+        stride = max(1, N // 600)
+        O.search(oracle_mod.TEMPLATE, stride=stride)
+        O.search(oracle_mod.TEMPLATE, t1=T)
+        O.solve(t1=T)
+        path = bw.items[d].method.path.permutation(N)
+        nodes = path[np.unique(np.concatenate([np.arange(0, N, stride), np.arange(T)]))]
+        ig, cg = B.neighbors(d)
+        io, co = O.neighbors()
+        np.testing.assert_array_equal(cg[nodes], co[nodes], err_msg=f"domain {d}")
+        np.testing.assert_array_equal(ig[nodes], io[nodes], err_msg=f"domain {d}")
+        first = path[:T]
+        vo = O.simulate(R, zs[d], t_end=T)
+        assert rel_err(vals[d][:, first], vo[:, first]) <= VALUE_TOL, d
+    B.close()
+
+
+@pytest.mark.gpu
 def test_batch_graph_replay_and_seeded_draws(oracle_mod, geosgs_lib):
     """Replayed graphs give identical results; seeded draws are Philox keyed
     by the global node id, so the oracle fed those normals agrees."""
