@@ -22,6 +22,7 @@
 namespace sgs {
 
 constexpr int SEARCH_WARPS = 8;
+constexpr int SCAN_STEPS = 4;  // template steps of 32 entries loaded per pass
 constexpr int DCAP = 256;  // data candidate buffer per warp
 
 // Squared distances are non-negative doubles, whose IEEE bit patterns order
@@ -85,29 +86,46 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
         cell_of(G, g, i0, i1, i2);
 
         // ---- grid candidates from the sorted template ----
+        // SCAN_STEPS steps of 32 entries per pass: the template entries and
+        // rank gathers of all are issued before the first is used, and each
+        // later step is taken only if the earlier ones left the row short
+        // (the entries are processed in the same order as one step at a time)
         int ng = 0;
         const int T = a.data_only ? 0 : a.T;
-        for (int base = 0; base < T && ng < k; base += 32) {
-            const int j = base + lane;
-            bool ok = false;
-            int c = 0;
-            if (j < T) {
-                const TmplEntry e = a.tmpl[j];
-                const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
-                if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {
-                    c = g + e.dlin;
-                    ok = a.rank[c] < t;
+        for (int base = 0; base < T && ng < k; base += 32 * SCAN_STEPS) {
+            int c[SCAN_STEPS];
+            bool in[SCAN_STEPS];
+#pragma unroll
+            for (int h = 0; h < SCAN_STEPS; ++h) {
+                c[h] = 0;
+                in[h] = false;
+                const int j = base + 32 * h + lane;
+                if (j < T) {
+                    const TmplEntry e = a.tmpl[j];
+                    const int c0 = i0 + e.dx, c1 = i1 + e.dy, c2 = i2 + e.dz;
+                    if (c0 >= 0 && c0 < G.n[0] && c1 >= 0 && c1 < G.n[1] && c2 >= 0 && c2 < G.n[2]) {
+                        c[h] = g + e.dlin;
+                        in[h] = true;
+                    }
                 }
             }
-            const unsigned b = __ballot_sync(FULL_MASK, ok);
-            if (ok) {
-                const int p = ng + __popc(b & lt);
-                if (p < k) {
-                    gidx[p] = c;
-                    gd2[p] = tkey[j];
+            int rk[SCAN_STEPS];
+#pragma unroll
+            for (int h = 0; h < SCAN_STEPS; ++h) rk[h] = in[h] ? a.rank[c[h]] : 0;
+#pragma unroll
+            for (int h = 0; h < SCAN_STEPS; ++h) {
+                if (ng >= k) break;  // warp-uniform
+                const bool ok = in[h] && rk[h] < t;
+                const unsigned b = __ballot_sync(FULL_MASK, ok);
+                if (ok) {
+                    const int p = ng + __popc(b & lt);
+                    if (p < k) {
+                        gidx[p] = c[h];
+                        gd2[p] = tkey[base + 32 * h + lane];
+                    }
                 }
+                ng += __popc(b);
             }
-            ng += __popc(b);
         }
         ng = min(ng, k);
         __syncwarp();
