@@ -164,6 +164,12 @@ def dist_setup(args):
     return ws, rank, local
 
 
+def replica_seed(seed: int) -> int:
+    """Seed of this rank's realizations: replicas draw disjoint Philox
+    streams, so N ranks produce N x R distinct realizations."""
+    return seed + int(os.environ.get("RANK", "0")) * 1_000_003
+
+
 def barrier(ws):
     if ws > 1:
         import torch.distributed as dist
@@ -282,7 +288,7 @@ def time_device(wl, args, torch, ws, network=None):
 
     def step(i):
         plan.prepare()
-        plan.simulate_device(R, None, 1000 + i, V, stream)
+        plan.simulate_device(R, None, replica_seed(1000 + i), V, stream)
 
     if args.sweep_config:
         plan.set_sweep(**json.loads(args.sweep_config))
@@ -348,7 +354,7 @@ def time_e2e(wl, args, torch, ws, steps, sweep=None):
         t1 = time.perf_counter()
         plan.prepare()
         t2 = time.perf_counter()
-        plan._check(plan.lib.sgs_plan_simulate(plan.h, R, None, 77 + i,
+        plan._check(plan.lib.sgs_plan_simulate(plan.h, R, None, replica_seed(77 + i),
                                                out.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))))
         t3 = time.perf_counter()
         inf = plan.info()
@@ -397,7 +403,7 @@ def time_batch(bw, args, torch, ws, precision):
 
     def step(i):
         B.prepare()
-        B.simulate_device(R, 1000 + i, V, stream)
+        B.simulate_device(R, replica_seed(1000 + i), V, stream)
 
     for i in range(args.warmup):
         step(i)
@@ -484,7 +490,7 @@ def main_batch(args, torch, ws, rank, uuid):
         def e2e_step(i):
             B = geosgs.Batch(probs)
             B.prepare()
-            B._check(B.lib.sgs_batch_simulate(B.h, R, None, 77 + i, out.ctypes.data_as(C.POINTER(C.c_double))))
+            B._check(B.lib.sgs_batch_simulate(B.h, R, None, replica_seed(77 + i), out.ctypes.data_as(C.POINTER(C.c_double))))
             inf = B.info()
             B.close()
             return inf
