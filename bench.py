@@ -481,7 +481,7 @@ def main_batch(args, torch, ws, rank, uuid):
         a64.warmup = max(1, min(args.warmup, 2))
         fp64, _ = time_batch(workloads.c5("fp64", nreals=R, ndomains=args.ndomains), a64, torch, ws, "fp64")
     e2e = None
-    if not args.no_e2e and N * R * 8 <= (8 << 30):
+    if not args.no_e2e and N * R * 8 <= (32 << 30):
         import geosgs
 
         out = torch.empty(N * R, dtype=torch.float64, pin_memory=True).numpy()
