@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <memory>
 #include <thread>
 #include <vector>
 
@@ -455,12 +456,34 @@ void bfree(sgs_batch* b, void* p) {
 }
 
 template <typename T>
-int bupload(sgs_batch* b, T** d, const std::vector<T>& h) {
-    int rc = balloc(b, d, h.size());
+int bupload_raw(sgs_batch* b, T** d, const T* h, size_t count) {
+    int rc = balloc(b, d, count);
     if (rc) return rc;
-    if (!h.empty()) BCK(b, cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream));
-    b->info.h2d_bytes += (int64_t)(h.size() * sizeof(T));
+    if (count) BCK(b, cudaMemcpyAsync(*d, h, count * sizeof(T), cudaMemcpyHostToDevice, b->stream));
+    b->info.h2d_bytes += (int64_t)(count * sizeof(T));
     return SGS_OK;
+}
+
+template <typename T>
+int bupload(sgs_batch* b, T** d, const std::vector<T>& h) {
+    return bupload_raw(b, d, h.data(), h.size());
+}
+
+// A host arena that is not zero-filled on construction: the threads that
+// fill it touch its pages first.
+template <typename T>
+struct HostArena {
+    std::unique_ptr<T[]> p;
+    size_t n = 0;
+    explicit HostArena(size_t count) : p(new T[count ? count : 1]), n(count) {}
+    T* data() { return p.get(); }
+    const T* data() const { return p.get(); }
+    size_t size() const { return n; }
+};
+
+template <typename T>
+int bupload(sgs_batch* b, T** d, const HostArena<T>& h) {
+    return bupload_raw(b, d, h.data(), h.size());
 }
 
 // 0 when the pair cannot be timed (the error is cleared, not left pending)
@@ -578,22 +601,32 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
     BCK(B, cudaMallocHost(&B->h_seed, sizeof(uint64_t)));
 
     // arenas
-    std::vector<int32_t> path(B->Ntot), rank(B->Ntot), did(B->Dtot), bstart(boff[nd]);
-    std::vector<TmplEntry> tmpl(toff[nd]);
-    std::vector<double> td2(toff[nd]), xyz(3 * B->Dtot), val(B->Dtot), xyzb(3 * B->Dtot);
-    std::vector<float4> xf(B->Dtot);
-    for (int d = 0; d < nd; ++d) {
-        const HostDomain& h = H[d];
-        std::copy(h.path.begin(), h.path.end(), path.begin() + B->noff[d]);
-        std::copy(h.rank.begin(), h.rank.end(), rank.begin() + B->noff[d]);
-        std::copy(h.tmpl.begin(), h.tmpl.end(), tmpl.begin() + toff[d]);
-        std::copy(h.tmpl_d2.begin(), h.tmpl_d2.end(), td2.begin() + toff[d]);
-        std::copy(h.xyz.begin(), h.xyz.end(), xyz.begin() + 3 * doff[d]);
-        std::copy(h.val.begin(), h.val.end(), val.begin() + doff[d]);
-        std::copy(h.xyz_b.begin(), h.xyz_b.end(), xyzb.begin() + 3 * doff[d]);
-        std::copy(h.did.begin(), h.did.end(), did.begin() + doff[d]);
-        std::copy(h.xf.begin(), h.xf.end(), xf.begin() + doff[d]);
-        std::copy(h.bstart.begin(), h.bstart.end(), bstart.begin() + boff[d]);
+    HostArena<int32_t> path(B->Ntot), rank(B->Ntot), did(B->Dtot), bstart(boff[nd]);
+    HostArena<TmplEntry> tmpl(toff[nd]);
+    HostArena<double> td2(toff[nd]), xyz(3 * B->Dtot), val(B->Dtot), xyzb(3 * B->Dtot);
+    HostArena<float4> xf(B->Dtot);
+    {
+        // the arenas (GBs of paths, ranks and templates) are filled by all
+        // host threads, each domain's slices by one thread
+        const int nt = std::max(1, std::min<int>(nd, (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back([&, t]() {
+                for (int d = t; d < nd; d += nt) {
+                    const HostDomain& h = H[d];
+                    std::copy(h.path.begin(), h.path.end(), path.data() + B->noff[d]);
+                    std::copy(h.rank.begin(), h.rank.end(), rank.data() + B->noff[d]);
+                    std::copy(h.tmpl.begin(), h.tmpl.end(), tmpl.data() + toff[d]);
+                    std::copy(h.tmpl_d2.begin(), h.tmpl_d2.end(), td2.data() + toff[d]);
+                    std::copy(h.xyz.begin(), h.xyz.end(), xyz.data() + 3 * doff[d]);
+                    std::copy(h.val.begin(), h.val.end(), val.data() + doff[d]);
+                    std::copy(h.xyz_b.begin(), h.xyz_b.end(), xyzb.data() + 3 * doff[d]);
+                    std::copy(h.did.begin(), h.did.end(), did.data() + doff[d]);
+                    std::copy(h.xf.begin(), h.xf.end(), xf.data() + doff[d]);
+                    std::copy(h.bstart.begin(), h.bstart.end(), bstart.data() + boff[d]);
+                }
+            });
+        for (auto& x : th) x.join();
     }
     int rc;
     int32_t *d_rank, *d_did, *d_bstart;
