@@ -248,8 +248,8 @@ class CartesianGrid:
         self.dims = tuple(int(x) for x in dims)
         self.origin = tuple(float(x) for x in origin)
         self.spacing = tuple(float(x) for x in spacing)
-        if len(self.dims) not in (2, 3) or len(self.origin) != len(self.dims) or len(self.spacing) != len(self.dims):
-            raise ArgumentError("the GPU path supports 2D and 3D grids")
+        if len(self.dims) not in (1, 2, 3) or len(self.origin) != len(self.dims) or len(self.spacing) != len(self.dims):
+            raise ArgumentError("the GPU path supports 1D, 2D and 3D grids")
 
     @property
     def dim(self) -> int:

@@ -40,9 +40,15 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         raise ArgumentError("the GPU SEQSIM path simulates GaussianProcess and IndicatorProcess")
     if not isinstance(domain, CartesianGrid):
         raise ArgumentError("the GPU SEQSIM path simulates on a CartesianGrid")
+    # A 1D grid of n cells runs as the n x 1 grid with unit spacing across and
+    # the data on the row's centre line (second coordinate 0.5, the cells'
+    # centroid): every lag's second component is exactly 0, so distances,
+    # neighbour order and covariances are those of the 1D problem.
     dim = domain.dim
+    flat = dim == 1
+    cdim = 2 if flat else dim
     p = _abi.SgsProblem()
-    p.dim = dim
+    p.dim = cdim
     for j in range(3):
         p.dims[j] = domain.dims[j] if j < dim else 1
         p.origin[j] = domain.origin[j] if j < dim else 0.0
@@ -54,6 +60,8 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         if len(data.values) != 1:
             raise ArgumentError("the GPU path simulates one variable")
         xy = np.ascontiguousarray(data.coords, dtype=np.float64)
+        if flat:
+            xy = np.ascontiguousarray(np.column_stack([xy[:, 0], np.full(xy.shape[0], 0.5)]))
         if isinstance(process, IndicatorProcess):
             val = np.ascontiguousarray(indicator_levels(process, data)[1], dtype=np.float64)
         else:
@@ -64,7 +72,7 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         p.data_values = val.ctypes.data_as(C.POINTER(C.c_double))
     else:
         p.ndata = 0
-    p.variogram = (process.corr if isinstance(process, IndicatorProcess) else process.func).to_c(dim)
+    p.variogram = (process.corr if isinstance(process, IndicatorProcess) else process.func).to_c(cdim)
     p.mean = process.mean
     p.minneighbors = int(method.minneighbors)
     p.maxneighbors = int(method.maxneighbors)
@@ -75,7 +83,7 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         p.search = _abi.SGS_SEARCH_NEAREST
     elif isinstance(nb, MetricBall):
         p.search = _abi.SGS_SEARCH_BALL
-        for j, r in enumerate(nb.padded_radii(dim)):
+        for j, r in enumerate(nb.padded_radii(cdim)):
             p.ball.radii[j] = r
         for i in range(3):
             for j in range(3):

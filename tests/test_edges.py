@@ -1,6 +1,6 @@
 """Edge cases of the plan path against the FP64 oracle: the largest and
 smallest neighbour counts, maxneighbors clamped to the grid size, a one-node
-grid, degenerate axes, duplicate data locations (colliding data make the
+grid, degenerate axes, a 1D grid (run as n x 1), duplicate data locations (colliding data make the
 kriging system singular where both are neighbours), data outside the grid,
 minneighbors equal to maxneighbors, a single realization, non-unit and
 unequal spacings with an offset origin.  Bars as in the parity suite:
@@ -53,6 +53,7 @@ CASES = {
                            rng_=12.0, vario=geosgs.SphericalVariogram),
     "gaussian_linear_path": case((20, 20), 16, ndata=15, seed=11, vario=geosgs.GaussianVariogram, nugget=0.0,
                                  path="linear"),
+    "line_1d": case((300,), 8, ndata=6, seed=12, rng_=12.0),
 }
 
 

@@ -62,3 +62,21 @@ def test_gpu_reproduces_the_model(name, precision, geosgs_lib):
     G = geosgs.Plan(p, keep).prepare()
     check_statistics(G.simulate(200, seed=3).reshape(200, 100, 100), proc.func)
     G.close()
+
+
+def test_oracle_1d_grid_reproduces_data_and_model(oracle_mod):
+    """A 1D grid (run as the n x 1 grid with the data on its centre line):
+    data at cell centres are reproduced exactly (nugget 0), and unconditional
+    realizations reproduce the 1D semivariogram."""
+    grid = geosgs.CartesianGrid(400)
+    proc = geosgs.GaussianProcess(geosgs.ExponentialVariogram(range=15.0), 0.0)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(2), maxneighbors=12, precision="fp64")
+    data = geosgs.georef({"Z": [1.5, -0.5]}, [40.5, 250.5])
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    out = oracle_mod.OraclePlan(p, keep).prepare().simulate(20, seed=1)
+    assert np.all(out[:, 40] == 1.5) and np.all(out[:, 250] == -0.5)
+    p, keep = geosgs.build_problem(proc, grid, None, method)
+    v = oracle_mod.OraclePlan(p, keep).prepare().simulate(400, seed=2)
+    hs = np.arange(1, 13)
+    g = np.array([0.5 * np.mean((v[:, h:] - v[:, :-h]) ** 2) for h in hs])
+    assert np.abs(g - proc.func(hs / 15.0)).max() < 0.06
