@@ -111,6 +111,10 @@ vtype(::GaussianVariogram) = Int32(3)
 vtype(f) = throw(ArgumentError("GPUSEQSIM supports spherical, exponential and gaussian variograms"))
 
 pad3(t, fill) = ntuple(i -> i <= length(t) ? Float64(t[i]) : fill, 3)
+# radii of a ball; a 1D problem runs as the n x 1 grid, whose second axis
+# then takes the same radius (every lag's second component is 0)
+radii3(b, dim) = dim == 1 ? (Float64(ustrip(first(radii(b)))), Float64(ustrip(first(radii(b)))), 1.0) :
+                            pad3(ustrip.(radii(b)), 1.0)
 
 function rot9(R, dim)
   M = Matrix{Float64}(I(3))
@@ -122,17 +126,18 @@ function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSI
   domain isa CartesianGrid || throw(ArgumentError("GPUSEQSIM simulates on a CartesianGrid"))
   f = process.func
   dim = embeddim(domain)
+  cdim = dim == 1 ? 2 : dim  # 1D: the n x 1 grid with the data on the row's centre line (y = 0.5)
   dims = size(domain)
   orig = ustrip.(to(minimum(domain)))
   spac = ustrip.(spacing(domain))
   ball = f.ball
   vg = SgsVariogram(vtype(f), 0, ustrip(sill(f)), ustrip(nugget(f)),
-                    pad3(ustrip.(radii(ball)), 1.0), rot9(rotation(ball), dim))
+                    radii3(ball, dim), rot9(rotation(ball), dim))
   nb = method.neighborhood
   search, sball = if nb === :range
     SGS_SEARCH_RANGE, SgsBall((1.0, 1.0, 1.0), rot9(I(3), dim))
   elseif nb isa MetricBall
-    SGS_SEARCH_BALL, SgsBall(pad3(ustrip.(radii(nb)), 1.0), rot9(rotation(nb), dim))
+    SGS_SEARCH_BALL, SgsBall(radii3(nb, dim), rot9(rotation(nb), dim))
   else
     SGS_SEARCH_NEAREST, SgsBall((1.0, 1.0, 1.0), rot9(I(3), dim))
   end
@@ -143,14 +148,15 @@ function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSI
   if !isnothing(data)
     var = first(propertynames(values(data)))
     for i in 1:nrow(data)
-      append!(xy, ustrip.(to(centroid(domain(data), i))))
+      c = ustrip.(to(centroid(domain(data), i)))
+      append!(xy, dim == 1 ? (c[1], 0.5) : c)
     end
     vals = Float64.(ustrip.(getproperty(values(data), var)))
   end
   path = Int32.(collect(traverse(domain, method.path)) .- 1)  # one path for all realizations
   planref = Ref{Ptr{Cvoid}}(C_NULL)
   GC.@preserve xy vals path begin
-    prob = SgsProblem(Int32(dim), pad3(dims, 1.0) .|> Int32, pad3(orig, 0.0), pad3(spac, 1.0),
+    prob = SgsProblem(Int32(cdim), pad3(dims, 1.0) .|> Int32, pad3(orig, 0.0), pad3(spac, 1.0),
                       length(vals), pointer(xy), pointer(vals), vg, Float64(ustrip(process.mean)),
                       method.minneighbors, method.maxneighbors, search,
                       method.precision === :fp64 ? Int32(0) : Int32(1), sball, pointer(path),
