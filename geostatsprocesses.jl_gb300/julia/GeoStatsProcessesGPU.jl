@@ -17,6 +17,7 @@
 module GeoStatsProcessesGPU
 
 using Random
+using LinearAlgebra: I
 using Distributed: myid
 using Meshes
 using GeoTables
@@ -122,17 +123,15 @@ function rot9(R, dim)
   ntuple(k -> M[(k - 1) % 3 + 1, (k - 1) ÷ 3 + 1], 9)  # column-major, leading dimension 3
 end
 
-function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, init, domain, data)
-  domain isa CartesianGrid || throw(ArgumentError("GPUSEQSIM simulates on a CartesianGrid"))
-  f = process.func
-  dim = embeddim(domain)
+# Geometry, neighbourhood, data and path of a problem -> a created plan; the
+# `before_prepare` hook runs between sgs_plan_create and sgs_plan_prepare.
+function _plan(vg::SgsVariogram, mean, method::GPUSEQSIM, grid, data, datavals; before_prepare=identity)
+  grid isa CartesianGrid || throw(ArgumentError("GPUSEQSIM simulates on a CartesianGrid"))
+  dim = embeddim(grid)
   cdim = dim == 1 ? 2 : dim  # 1D: the n x 1 grid with the data on the row's centre line (y = 0.5)
-  dims = size(domain)
-  orig = ustrip.(to(minimum(domain)))
-  spac = ustrip.(spacing(domain))
-  ball = f.ball
-  vg = SgsVariogram(vtype(f), 0, ustrip(sill(f)), ustrip(nugget(f)),
-                    radii3(ball, dim), rot9(rotation(ball), dim))
+  dims = size(grid)
+  orig = ustrip.(to(minimum(grid)))
+  spac = ustrip.(spacing(grid))
   nb = method.neighborhood
   search, sball = if nb === :range
     SGS_SEARCH_RANGE, SgsBall((1.0, 1.0, 1.0), rot9(I(3), dim))
@@ -143,28 +142,36 @@ function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSI
   end
   # data appended after the grid nodes, as SEQSIM's ExplicitInit (seqsim.jl:211-218,267-271)
   xy = Float64[]
-  vals = Float64[]
-  var = :field
+  vals = Float64.(datavals)
   if !isnothing(data)
-    var = first(propertynames(values(data)))
     for i in 1:nrow(data)
-      c = ustrip.(to(centroid(domain(data), i)))
+      c = ustrip.(to(centroid(GeoTables.domain(data), i)))
       append!(xy, dim == 1 ? (c[1], 0.5) : c)
     end
-    vals = Float64.(ustrip.(getproperty(values(data), var)))
   end
-  path = Int32.(collect(traverse(domain, method.path)) .- 1)  # one path for all realizations
+  path = Int32.(collect(traverse(grid, method.path)) .- 1)  # one path for all realizations
   planref = Ref{Ptr{Cvoid}}(C_NULL)
   GC.@preserve xy vals path begin
     prob = SgsProblem(Int32(cdim), pad3(dims, 1.0) .|> Int32, pad3(orig, 0.0), pad3(spac, 1.0),
-                      length(vals), pointer(xy), pointer(vals), vg, Float64(ustrip(process.mean)),
+                      length(vals), pointer(xy), pointer(vals), vg, Float64(mean),
                       method.minneighbors, method.maxneighbors, search,
                       method.precision === :fp64 ? Int32(0) : Int32(1), sball, pointer(path),
                       method.refine_steps, 0, method.device, 0)
     check(ccall((:sgs_plan_create, libgeosgs), Cint, (Ref{SgsProblem}, Ref{Ptr{Cvoid}}), prob, planref), C_NULL)
   end
   plan = GPUPlan(planref[])
+  before_prepare(plan)
   check(ccall((:sgs_plan_prepare, libgeosgs), Cint, (Ptr{Cvoid},), plan.ptr), plan.ptr)
+  plan
+end
+
+function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, init, domain, data)
+  f = process.func
+  dim = embeddim(domain)
+  vg = SgsVariogram(vtype(f), 0, ustrip(sill(f)), ustrip(nugget(f)), radii3(f.ball, dim), rot9(rotation(f.ball), dim))
+  var = isnothing(data) ? :field : first(propertynames(values(data)))
+  vals = isnothing(data) ? Float64[] : Float64.(ustrip.(getproperty(values(data), var)))
+  plan = _plan(vg, ustrip(process.mean), method, domain, data, vals)
   (; plan, var, nelm=nelements(domain), block=Ref(Matrix{Float64}(undef, 0, 0)), cursor=Ref(0))
 end
 
@@ -182,6 +189,50 @@ function randsingle(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSI
   end
   cursor[] += 1
   (; var => block[][:, cursor[]])
+end
+
+# ---- sequential indicator simulation (seqsim.jl:247-261, 292-310, 342-347) ----
+# For proportional transiograms t_ab(h) = p_b + (delta_ab - p_b) rho(h) every
+# category's simple cokriging weights are rho's simple kriging weights, so the
+# plan solves with rho (the transiogram's family, its range, sill 1, nugget 0)
+# and sgs_plan_simulate_indicator draws the categories.
+ctype(::SphericalTransiogram) = Int32(1)
+ctype(::ExponentialTransiogram) = Int32(2)
+ctype(::GaussianTransiogram) = Int32(3)
+ctype(f) = throw(ArgumentError("GPUSEQSIM simulates proportional spherical, exponential and gaussian transiograms"))
+
+function preprocess(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQSIM, init, domain, data)
+  f = process.func
+  prob = Float64.(collect(process.prob))
+  2 <= length(prob) <= 8 || throw(ArgumentError("GPUSEQSIM simulates 2 to 8 categories"))
+  r = Float64(ustrip(range(f)))
+  rho = SgsVariogram(ctype(f), 0, 1.0, 0.0, (r, r, r), rot9(I(3), embeddim(domain)))
+  # categories: the data's sorted distinct labels (the one-hot transform), 1..L without data
+  var = isnothing(data) ? :field : first(propertynames(values(data)))
+  labels = isnothing(data) ? collect(1:length(prob)) : sort(unique(getproperty(values(data), var)))
+  isnothing(data) || length(labels) == length(prob) ||
+    throw(ArgumentError("probabilities must have $(length(labels)) components, received $(length(prob))"))
+  cats = isnothing(data) ? Int32[] : Int32.(indexin(getproperty(values(data), var), labels) .- 1)
+  setind(plan) = GC.@preserve prob cats check(ccall((:sgs_plan_set_indicator, libgeosgs), Cint,
+                                                     (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Int32}),
+                                                     plan.ptr, length(prob), prob, cats), plan.ptr)
+  plan = _plan(rho, 0.0, method, domain, data, zeros(length(cats)); before_prepare=setind)
+  (; plan, var, labels, nelm=nelements(domain), block=Ref(Matrix{Int32}(undef, 0, 0)), cursor=Ref(0))
+end
+
+function randsingle(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQSIM, domain, data, preproc)
+  (; plan, var, labels, nelm, block, cursor) = preproc
+  myid() == plan.owner || throw(ArgumentError("GPUSEQSIM realizations must run on the process that prepared them"))
+  if cursor[] == size(block[], 2)
+    B = Matrix{Int32}(undef, nelm, method.batch)  # N x batch, column = realization
+    check(ccall((:sgs_plan_simulate_indicator, libgeosgs), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Float64}, UInt64, Ptr{Int32}),
+                plan.ptr, method.batch, C_NULL, rand(rng, UInt64), B), plan.ptr)
+    block[] = B
+    cursor[] = 0
+  end
+  cursor[] += 1
+  (; var => labels[block[][:, cursor[]] .+ 1])
 end
 
 end # module
