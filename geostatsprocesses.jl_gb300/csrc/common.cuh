@@ -23,7 +23,6 @@ namespace sgs {
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
 // canonical squared distance of a lag under a search metric
 __device__ __forceinline__ double metric_d2(const MetricDev& m, int dim, double h0, double h1, double h2) {

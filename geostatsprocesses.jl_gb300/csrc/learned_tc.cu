@@ -376,8 +376,6 @@ __global__ void __launch_bounds__(THREADS) nn_predict_tc_kernel(const GridDev G,
     }
 }
 
-int nn_predict_tc_smem() { return SMEM_BYTES; }
-
 cudaError_t launch_nn_predict_tc(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,
                                  const double* data_xyz, const float* params, float* out, int32_t* err, int nsm,
                                  cudaStream_t s) {

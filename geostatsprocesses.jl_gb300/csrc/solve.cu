@@ -129,12 +129,6 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-__device__ __forceinline__ double warp_max(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL_MASK, v, o));
-    return v;
-}
-
 template <typename T>
 __host__ __device__ constexpr size_t warp_smem_bytes(int k) {
     // A (k x (k+1) of T), c and w (FP64), rhs (T), neighbour info
