@@ -162,6 +162,39 @@ def test_batch_of_full_size_c5_domains_sampled(oracle_mod, geosgs_lib):
 
 
 @pytest.mark.gpu
+def test_batch_edge_cases(oracle_mod, geosgs_lib):
+    """A batch of one domain, and a batch holding a one-node domain, a 1D
+    domain (as n x 1) and a domain whose maxneighbors exceeds its node count:
+    per domain the same neighbours and values as the oracle."""
+    def item(dims, k, nd=0, seed=0):
+        grid = geosgs.CartesianGrid(dims)
+        rng = np.random.default_rng(seed)
+        data = None
+        if nd:
+            ext = np.asarray(grid.dims, dtype=np.float64)
+            data = geosgs.georef({"Z": rng.standard_normal(nd)}, rng.uniform(0.0, 1.0, (nd, len(dims))) * ext)
+        proc = geosgs.GaussianProcess(geosgs.ExponentialVariogram(range=5.0, nugget=0.05), 0.3)
+        method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(seed), maxneighbors=k, precision="fp32")
+        return geosgs.build_problem(proc, grid, data, method)
+
+    for probs in ([item((30, 20), 12, nd=5, seed=1)],
+                  [item((1, 1), 8, nd=2, seed=2), item((200,), 6, nd=3, seed=3), item((4, 3), 40, seed=4),
+                   item((16, 12, 5), 24, nd=10, seed=5)]):
+        B = geosgs.Batch(probs).prepare()
+        R = 5
+        zs = [np.random.default_rng(400 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
+        vals = B.simulate(R, z=zs)
+        for d, (p, keep) in enumerate(probs):
+            O = oracle_mod.OraclePlan(p, keep).prepare()
+            ig, cg = B.neighbors(d)
+            io, co = O.neighbors()
+            np.testing.assert_array_equal(cg, co, err_msg=f"domain {d}")
+            np.testing.assert_array_equal(ig, io, err_msg=f"domain {d}")
+            assert rel_err(vals[d], O.simulate(R, zs[d])) <= VALUE_TOL, d
+        B.close()
+
+
+@pytest.mark.gpu
 def test_batch_graph_replay_and_seeded_draws(oracle_mod, geosgs_lib):
     """Replayed graphs give identical results; seeded draws are Philox keyed
     by the global node id, so the oracle fed those normals agrees."""
