@@ -271,6 +271,56 @@ extern "C" int sgs_selftest_bounded_wait(int64_t wait_ns, int32_t* timed_out, in
     return rc;
 }
 
+// Diagnostic (exported, not part of the C ABI in include/geosgs.h): runs the
+// dependency-level kernel on a two-node table in which each node is the
+// other's neighbour, so neither level can ever be known, with a wait limit
+// of wait_ns.  *timed_out = 1 when the kernel gave up and said so;
+// *elapsed_ns = the launch's duration.  Returns 0, or a negative SGS_ERR_*
+// code when the launch itself failed.
+extern "C" int sgs_selftest_levels_wait(int64_t wait_ns, int32_t* timed_out, int64_t* elapsed_ns) {
+    if (!timed_out || !elapsed_ns || wait_ns <= 0) return SGS_ERR_ARG;
+    *timed_out = 0;
+    *elapsed_ns = 0;
+    // [0,2) path, [2,4) neighbours, [4,6) counts, [6,8) levels, [8,12) ticket,
+    // max level, error flag, spare
+    const int32_t init[12] = {0, 1, 1, 0, 1, 1, -1, -1, 0, 0, 0, 0};
+    int32_t* d = nullptr;
+    if (cudaMalloc(&d, sizeof(init)) != cudaSuccess) {
+        cudaGetLastError();
+        return SGS_ERR_CUDA;
+    }
+    LevelArgs la{};
+    la.N = 2;
+    la.k = 1;
+    la.path = d;
+    la.nbr = d + 2;
+    la.cnt = d + 4;
+    la.level = d + 6;
+    la.ticket = d + 8;
+    la.maxlevel = d + 9;
+    la.err = d + 10;
+    la.wait_ns = (uint64_t)wait_ns;
+    int rc = SGS_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int32_t herr = 0;
+    float ms = 0.f;
+    if (cudaMemcpy(d, init, sizeof(init), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+        cudaEventRecord(e0) != cudaSuccess || launch_levels(la, 1, 0) != cudaSuccess ||
+        cudaEventRecord(e1) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaMemcpy(&herr, d + 10, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        cudaGetLastError();
+        rc = SGS_ERR_CUDA;
+    }
+    *timed_out = herr;
+    *elapsed_ns = (int64_t)(ms * 1e6);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return rc;
+}
+
 extern "C" const char* sgs_last_error(const sgs_plan* plan) {
     return plan ? plan->err.c_str() : g_create_err.c_str();
 }
@@ -762,7 +812,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     la.ticket = P->d_scratch + 1;
     la.maxlevel = P->d_scratch + 2;
     la.err = P->d_scratch + 3;
-    la.spin_limit = (int64_t)1 << 26;
+    la.wait_ns = LEVEL_WAIT_NS;
     LAUNCH(P, 1, launch_levels(la, P->nsm, st));
     int32_t hs[4] = {0, 0, 0, 0};
     CK(P, cudaMemcpyAsync(hs, P->d_scratch, sizeof(hs), cudaMemcpyDeviceToHost, st));

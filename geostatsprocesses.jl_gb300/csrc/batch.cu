@@ -49,19 +49,21 @@ struct LevelDom {
 // arena (domain after domain, path rank order inside a domain); a node's
 // neighbours are earlier nodes of its own domain, so they hold smaller
 // tickets, taken by running warps, and every wait ends.  Each wait is
-// bounded anyway (spin_limit polls, then the error flag).
+// bounded anyway (wait_level: wait_ns of wall-clock time, then the error
+// flag, after which no warp takes a new ticket).
 __global__ void __launch_bounds__(256)
 levels_batch_kernel(const LevelDom* __restrict__ doms, const int64_t* __restrict__ noff, int ndom,
                     const int32_t* __restrict__ path, const int32_t* __restrict__ nbr,
                     const int32_t* __restrict__ cnt, int32_t* level, unsigned long long* ticket, int32_t* maxlevel,
-                    int32_t* err, int64_t spin_limit) {
+                    int32_t* err, uint64_t wait_ns) {
     const int lane = threadIdx.x & 31;
     const int64_t total = noff[ndom];
     volatile int32_t* vlevel = level;
+    const volatile int32_t* verr = err;
     int wmax = 0;
     for (;;) {
         unsigned long long t = 0;
-        if (lane == 0) t = atomicAdd(ticket, 1ull);
+        if (lane == 0) t = *verr ? (unsigned long long)total : atomicAdd(ticket, 1ull);
         t = __shfl_sync(FULL_MASK, t, 0);
         if ((int64_t)t >= total) break;
         const int d = find_domain(noff, ndom, (int64_t)t);
@@ -72,20 +74,7 @@ levels_batch_kernel(const LevelDom* __restrict__ doms, const int64_t* __restrict
         int lv = 0;
         for (int q = lane; q < n; q += 32) {
             const int c = row[q];
-            if (c < D.N) {
-                int l = vlevel[D.node0 + c];
-                int64_t spins = 0;
-                while (l < 0) {
-                    if (++spins > spin_limit) {
-                        atomicExch(err, 1);
-                        l = 0;
-                        break;
-                    }
-                    __nanosleep(64);
-                    l = vlevel[D.node0 + c];
-                }
-                lv = max(lv, l + 1);
-            }
+            if (c < D.N) lv = max(lv, wait_level(vlevel, D.node0 + c, err, wait_ns) + 1);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lv = max(lv, __shfl_xor_sync(FULL_MASK, lv, o));
@@ -772,7 +761,7 @@ static int enqueue_prepare(sgs_batch* B, int64_t& launched) {
     BCK(B, cudaMemsetAsync(B->d_lfill, 0, B->lcap * sizeof(int32_t), st));
     levels_batch_kernel<<<B->nsm * 8, 256, 0, st>>>(B->d_ldom, B->d_noff, nd, B->d_path, B->d_nbr, B->d_cnt,
                                                      B->d_level, B->d_ticket, B->d_scratch, B->d_scratch + 1,
-                                                     (int64_t)1 << 26);
+                                                     LEVEL_WAIT_NS);
     BLAUNCH(B, cudaGetLastError());
     const unsigned lb = (unsigned)((N + BL_NODES - 1) / BL_NODES);
     level_count_batch_kernel<<<lb, 256, 0, st>>>(N, B->d_level, B->d_scratch, B->d_lcount);

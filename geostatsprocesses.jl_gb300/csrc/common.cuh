@@ -225,6 +225,36 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Level of node c once it is known (>= 0).  Bounded: the wait gives up after
+// wait_ns of wall-clock time (or, should the timer stall, after a count of
+// polls, each at least the 64 ns back-off, reached no earlier), and at once
+// when another warp has already raised *err.  A warp that gives up raises
+// *err; the returned level is then 0 and the caller's result is void.
+__device__ __forceinline__ int wait_level(const volatile int32_t* vlevel, int64_t c, int32_t* err,
+                                          uint64_t wait_ns) {
+    int l = vlevel[c];
+    if (l >= 0) return l;
+    const volatile int32_t* verr = err;
+    const uint64_t max_polls = wait_ns / 32 + 1024;
+    const uint64_t t0 = global_ns();
+    for (uint64_t polls = 0;; ++polls) {
+        __nanosleep(64);
+        l = vlevel[c];
+        if (l >= 0) return l;
+        if (*verr) return 0;
+        if (global_ns() - t0 > wait_ns || polls > max_polls) {
+            atomicExch(err, 1);
+            return 0;
+        }
+    }
+}
+
 // ---- batches of domains: global numbering and per-domain descriptors ----
 // Domain d owns the global ids [off[d], off[d+1]); returns d for id x
 // (0 <= x < off[nd]) by binary search over the nd + 1 offsets.

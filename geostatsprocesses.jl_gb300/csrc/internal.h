@@ -89,6 +89,13 @@ struct SearchArgs {
     int data_only;               // 1: data candidates only (kriging from the data)
 };
 
+// Longest wait of the dependency-level kernels for one neighbour's level.
+// Their waits end by construction (a neighbour's path rank is smaller, and
+// ranks are taken in increasing order by running warps), and the longest
+// level computation measured (354 M nodes in one batch) takes 0.6 s in total,
+// so a wait of 2 s only happens on a table that breaks the path order.
+constexpr uint64_t LEVEL_WAIT_NS = 2000000000ull;
+
 struct LevelArgs {
     int64_t N;
     int k;
@@ -99,7 +106,7 @@ struct LevelArgs {
     int32_t* ticket;             // 1 counter
     int32_t* maxlevel;           // 1 counter
     int32_t* err;                // 1 flag
-    int64_t spin_limit;
+    uint64_t wait_ns;            // longest wait for one neighbour's level
 };
 
 // Sweep tables, indexed by position in level order.  For T = double one

@@ -12,33 +12,94 @@
 // the library and lives until the process exits.
 //
 // Limits and rules (also stated in include/geosgs.h):
+//  * the inputs are checked on the device before they are used: path must
+//    be a permutation of 0..N-1, every count in [0, maxneighbors], and every
+//    grid neighbour (id < N) of a node must come earlier in the path than the
+//    node; anything else is rejected with SGS_ERR_ARG and nothing is read or
+//    written out of bounds;
 //  * at most SGS_NOALLOC_MAX_LEVELS dependency levels; a larger schedule is
 //    rejected with SGS_ERR_ARG before any per-level counter is touched;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
+//  * the array's device address is looked up (cudaGetSymbolAddress) on every
+//    call, with the caller's device and context current, so a device reset or
+//    another context never leaves a stale address behind;
 //  * all calls on a device share the array, and each call clears what must
 //    start at zero; calls that overlap on the GPU (other streams, other host
 //    threads) race on it and must be serialized by the caller.
+#include <algorithm>
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "../../include/geosgs.h"
-#include "internal.h"
+#include "common.cuh"
 
 namespace {
 
-constexpr int kHeader = 64;  // ticket, max level, error flag, padding
+constexpr int kHeader = 64;  // ticket, max level, wait error, input error, padding
 constexpr int kMaxLevels = SGS_NOALLOC_MAX_LEVELS;
 
-// [0] ticket, [1] max level, [2] error flag; then per-level counts and fill
-// cursors, kMaxLevels each
+// [0] ticket, [1] max level, [2] wait error flag, [3] input error code; then
+// per-level counts and fill cursors, kMaxLevels each
 static __device__ __align__(256) int32_t g_schedule_scratch[kHeader + 2 * kMaxLevels];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-int32_t* g_scratch_ptr[kMaxDevices] = {};
+// input error codes (scratch[3]); the smallest code raised is reported
+enum : int32_t {
+    kInOk = 0,
+    kInPathRange = 1,      // a path entry outside [0, N)
+    kInPathRepeat = 2,     // a node twice in the path
+    kInCount = 3,          // a count outside [0, maxneighbors]
+    kInNegNeighbour = 4,   // a negative id among a node's first count entries
+    kInLaterNeighbour = 5  // a grid neighbour that does not come earlier in the path
+};
+
+// Path ranks into rank[] (the caller's `order` buffer, all -1 on entry): a
+// path entry out of range or repeated raises its code.  With no code raised,
+// the N entries are N distinct ids in [0, N): a permutation.
+__global__ void check_path_kernel(const int32_t* __restrict__ path, int64_t N, int32_t* rank, int32_t* code) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t g = path[t];
+        if (g < 0 || g >= N) {
+            atomicMin(code, kInPathRange);
+            continue;
+        }
+        if (atomicCAS(&rank[g], -1, (int32_t)t) != -1) atomicMin(code, kInPathRepeat);
+    }
+}
+
+// Every node's count and first count neighbour ids, against the ranks (run
+// only when the path is a permutation, so every rank is set).
+__global__ void check_table_kernel(const int32_t* __restrict__ nbr, const int32_t* __restrict__ count, int64_t N,
+                                   int k, const int32_t* __restrict__ rank, int32_t* code) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t n = count[g];
+        if (n < 0 || n > k) {
+            atomicMin(code, kInCount);
+            continue;
+        }
+        const int32_t rg = rank[g];
+        for (int q = 0; q < n; ++q) {
+            const int32_t c = nbr[g * (int64_t)k + q];
+            if (c < 0) {
+                atomicMin(code, kInNegNeighbour);
+                break;
+            }
+            if (c < N && rank[c] >= rg) {
+                atomicMin(code, kInLaterNeighbour);
+                break;
+            }
+        }
+    }
+}
+
+const char* input_error_text(int32_t code) {
+    switch (code) {
+        case kInPathRange: return "path holds an entry outside [0, nnodes)";
+        case kInPathRepeat: return "path holds a node twice (it must be a permutation of 0..nnodes-1)";
+        case kInCount: return "a count is outside [0, maxneighbors]";
+        case kInNegNeighbour: return "a negative neighbour id among a node's first count entries";
+        case kInLaterNeighbour: return "a grid neighbour does not come earlier in the path than its node";
+        default: return "invalid input";
+    }
+}
 
 // the message is read back with sgs_last_error(NULL)
 int fail(int code, const std::string& msg) {
@@ -89,28 +150,40 @@ extern "C" int sgs_schedule_noalloc(const int32_t* path, const int32_t* nbr, con
     if (offsets_capacity < 2) return fail(SGS_ERR_ARG, "offsets_capacity must be at least 2");
     int dev = 0, nsm = 0;
     CKN(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(SGS_ERR_ARG, "device ordinal out of range");
+    // the array's address in the current context, looked up on every call
     int32_t* scratch = nullptr;
     {
-        // once per device, with that device current
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_schedule_scratch);
-            if (e != cudaSuccess) {
-                cudaGetLastError();
-                return fail(SGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            }
-            g_scratch_ptr[dev] = static_cast<int32_t*>(p);
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_schedule_scratch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         }
-        scratch = g_scratch_ptr[dev];
+        scratch = static_cast<int32_t*>(p);
     }
     CKN(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     cudaStream_t st = (cudaStream_t)stream;
+    const int check_blocks = (int)std::min<int64_t>((nnodes + 255) / 256, (int64_t)nsm * 16);
+
+    // inputs: path ranks into the caller's order buffer, then the table
+    CKN(cudaMemsetAsync(scratch, 0, kHeader * sizeof(int32_t), st));
+    CKN(cudaMemsetAsync(order, 0xff, (size_t)nnodes * sizeof(int32_t), st));
+    int32_t* code = scratch + 3;
+    check_path_kernel<<<check_blocks, 256, 0, st>>>(path, nnodes, order, code);
+    CKN(cudaGetLastError());
+    int32_t hcode = 0;
+    CKN(cudaMemcpyAsync(&hcode, code, sizeof(hcode), cudaMemcpyDeviceToHost, st));
+    CKN(cudaStreamSynchronize(st));
+    if (hcode == kInOk) {
+        check_table_kernel<<<check_blocks, 256, 0, st>>>(nbr, count, nnodes, maxneighbors, order, code);
+        CKN(cudaGetLastError());
+        CKN(cudaMemcpyAsync(&hcode, code, sizeof(hcode), cudaMemcpyDeviceToHost, st));
+        CKN(cudaStreamSynchronize(st));
+    }
+    if (hcode != kInOk) return fail(SGS_ERR_ARG, input_error_text(hcode));
 
     // levels: the ticket kernel of the plan path, its counters in the scratch
     CKN(cudaMemsetAsync(level, 0xff, (size_t)nnodes * sizeof(int32_t), st));
-    CKN(cudaMemsetAsync(scratch, 0, kHeader * sizeof(int32_t), st));
     sgs::LevelArgs la{};
     la.N = nnodes;
     la.k = maxneighbors;
@@ -121,7 +194,7 @@ extern "C" int sgs_schedule_noalloc(const int32_t* path, const int32_t* nbr, con
     la.ticket = scratch + 0;
     la.maxlevel = scratch + 1;
     la.err = scratch + 2;
-    la.spin_limit = (int64_t)1 << 26;
+    la.wait_ns = sgs::LEVEL_WAIT_NS;
     CKN(sgs::launch_levels(la, nsm, st));
     int32_t hdr[3] = {0, 0, 0};
     CKN(cudaMemcpyAsync(hdr, scratch, sizeof(hdr), cudaMemcpyDeviceToHost, st));

@@ -384,18 +384,20 @@ cudaError_t launch_search(const SearchArgs& a, cudaStream_t s) {
 // every wait ends.  The kernel is bound by the latency of dependency chains:
 // a warp that holds several ranks delays every chain through its later ones
 // (16 ranks per ticket measured 7x slower than one), so LEVEL_CHUNK is 1.
-// Each wait is still bounded: past `spin_limit` polls the kernel raises the
-// error flag and goes on (the host reports SGS_ERR_TIMEOUT).  The deepest
-// level is kept per warp and published once.
+// Each wait is still bounded (wait_level: a.wait_ns of wall-clock time, and
+// no longer once another warp gave up); the kernel then raises the error
+// flag, no warp takes a new ticket, and the host reports SGS_ERR_TIMEOUT.
+// The deepest level is kept per warp and published once.
 constexpr int LEVEL_CHUNK = 1;
 
 __global__ void __launch_bounds__(256) levels_kernel(const LevelArgs a) {
     const int lane = threadIdx.x & 31;
     volatile int32_t* vlevel = a.level;
+    const volatile int32_t* verr = a.err;
     int wmax = 0;
     while (true) {
         int64_t t0 = 0;
-        if (lane == 0) t0 = atomicAdd(a.ticket, LEVEL_CHUNK);
+        if (lane == 0) t0 = *verr ? a.N : atomicAdd(a.ticket, LEVEL_CHUNK);
         t0 = __shfl_sync(FULL_MASK, t0, 0);
         if (t0 >= a.N) break;
         const int64_t t1 = min(t0 + (int64_t)LEVEL_CHUNK, a.N);
@@ -405,20 +407,7 @@ __global__ void __launch_bounds__(256) levels_kernel(const LevelArgs a) {
             int lv = 0;
             for (int q = lane; q < n; q += 32) {
                 const int c = a.nbr[(int64_t)g * a.k + q];
-                if (c < a.N) {
-                    int l = vlevel[c];
-                    int64_t spins = 0;
-                    while (l < 0) {
-                        if (++spins > a.spin_limit) {
-                            atomicExch(a.err, 1);
-                            l = 0;
-                            break;
-                        }
-                        __nanosleep(64);
-                        l = vlevel[c];
-                    }
-                    lv = max(lv, l + 1);
-                }
+                if (c < a.N) lv = max(lv, wait_level(vlevel, c, a.err, a.wait_ns) + 1);
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) lv = max(lv, __shfl_xor_sync(FULL_MASK, lv, o));

@@ -506,11 +506,6 @@ __device__ __forceinline__ int ld_flag_acquire(const int32_t* p) {
 __device__ __forceinline__ void st_flag(int32_t* p, int v) {
     asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 // Wait until piece q of every grid neighbour is stored in this sweep (flags
 // of piece q: done_q); false when a wait gave up.  A legitimate wait can last

@@ -441,15 +441,19 @@ int sgs_ensemble_quantile(const void* vals, int32_t precision, int64_t nnodes, i
  * are device pointers owned by the caller: path (N), nbr (N x maxneighbors,
  * node-major, -1 padded, ids >= N are data), count (N); outputs level (N),
  * order (N, nodes grouped by level), offsets (nlevels + 1 entries, at most
- * offsets_capacity), and *nlevels on the host.  stream is a cudaStream_t
- * (NULL = default stream); the call returns when the results are complete.
- * Working memory is one file-scope device array per device (about 2 MB)
- * that stays until the process exits: schedules with more than
- * SGS_NOALLOC_MAX_LEVELS levels are rejected with SGS_ERR_ARG.  The first
- * call on a device looks up that array's address; make it before any stream
- * capture.  Calls on one device share the array: calls that overlap on the
- * GPU race and must be serialized by the caller.  Errors are reported by
- * sgs_last_error(NULL). */
+ * offsets_capacity), and *nlevels on the host.  The inputs are checked on
+ * the device first: path must be a permutation of 0..N-1, every count in
+ * [0, maxneighbors], the first count ids of a row non-negative, and every
+ * grid neighbour (id < N) of a node must come earlier in the path than the
+ * node; otherwise SGS_ERR_ARG, with nothing read or written out of bounds.
+ * stream is a cudaStream_t (NULL = default stream); the call synchronizes
+ * it and returns when the results are complete.  Working memory is one
+ * file-scope device array per device (about 2 MB) that stays until the
+ * process exits: schedules with more than SGS_NOALLOC_MAX_LEVELS levels are
+ * rejected with SGS_ERR_ARG.  Its device address is looked up on every call,
+ * in the current context.  Calls on one device share the array: calls that
+ * overlap on the GPU race and must be serialized by the caller.  Errors are
+ * reported by sgs_last_error(NULL). */
 int sgs_schedule_noalloc(const int32_t* path, const int32_t* nbr, const int32_t* count, int64_t nnodes,
                          int32_t maxneighbors, int32_t* level, int32_t* order, int32_t* offsets,
                          int32_t offsets_capacity, int32_t* nlevels, void* stream);

@@ -244,6 +244,26 @@ def test_bounded_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
     G.close()
 
 
+def test_level_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
+    """The dependency-level kernel's wait, run on two nodes that are each
+    other's neighbour (sgs_selftest_levels_wait: neither level can ever be
+    known), gives up after its wall-clock limit and reports it; the same
+    process then prepares and simulates normally."""
+    import ctypes as C
+
+    lib = C.CDLL(_abi.LIB_PATH)
+    lib.sgs_selftest_levels_wait.argtypes = [C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    timed_out, elapsed = C.c_int32(0), C.c_int64(0)
+    assert lib.sgs_selftest_levels_wait(50_000_000, C.byref(timed_out), C.byref(elapsed)) == 0
+    assert timed_out.value == 1
+    assert 50_000_000 <= elapsed.value < 5_000_000_000
+    wl = workloads.small(n=30, k=10, ndata=10, nreals=8, precision="fp32")
+    G, O = both(wl, oracle_mod, "fp32")
+    z = np.random.default_rng(9).standard_normal((8, O.N))
+    assert rel_err(G.simulate(8, z), O.simulate(8, z)) <= VALUE_TOL
+    G.close()
+
+
 def test_error_codes(geosgs_lib):
     from geosgs import _abi
 

@@ -31,14 +31,15 @@ def test_library_loads_and_exports_every_header_symbol():
 
 
 def test_diagnostic_exports_outside_the_header():
-    """The bounded-wait self-test is exported for the GPU tests but is not
-    part of the C ABI the header declares."""
+    """The bounded-wait self-tests are exported for the GPU tests but are
+    not part of the C ABI the header declares."""
     from geosgs import _build
 
     _build.build()
     lib = C.CDLL(_abi.LIB_PATH)
-    assert hasattr(lib, "sgs_selftest_bounded_wait")
-    assert "sgs_selftest_bounded_wait" not in header_symbols()
+    for name in ("sgs_selftest_bounded_wait", "sgs_selftest_levels_wait"):
+        assert hasattr(lib, name)
+        assert name not in header_symbols()
 
 
 def test_peak_probe_library_builds_and_exports():
