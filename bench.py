@@ -37,26 +37,80 @@ METRIC = "SGS nodes×reals/s on 1 GB300: learned+FP32 vs plain FP64 path at ≤1
 UNIT = "nodes*reals/s"
 
 
+PEAKS_SRC = os.path.join(ROOT, "bench_peaks.cu")
+PEAKS_PATH = os.path.join(ROOT, "_build", "libgeosgs_peaks.so")
+
+
+def build_peaks(force: bool = False) -> str:
+    """Compile the throughput probes (bench_peaks.cu) into their own library
+    with the product's nvcc flags; measurement infrastructure, outside the
+    product's C ABI."""
+    sys.path.insert(0, os.path.join(ROOT, "geostatsprocesses.jl_gb300"))
+    from geosgs import _build
+
+    if not force and os.path.exists(PEAKS_PATH) and os.path.getmtime(PEAKS_SRC) <= os.path.getmtime(PEAKS_PATH):
+        return PEAKS_PATH
+    os.makedirs(os.path.dirname(PEAKS_PATH), exist_ok=True)
+    tmp = PEAKS_PATH + ".tmp"
+    cmd = [_build._nvcc(), *_build.NVCC_FLAGS, "-shared", "-o", tmp, PEAKS_SRC]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {PEAKS_SRC}:\n{r.stderr}")
+    os.replace(tmp, PEAKS_PATH)
+    return PEAKS_PATH
+
+
 def measure_peaks() -> dict:
-    """FP32 FFMA rate and device-to-page-locked-host write rate, from the probe
-    library built beside libgeosgs.so; empty where it is missing."""
-    path = os.path.join(ROOT, "geostatsprocesses.jl_gb300", "geosgs", "lib", "libgeosgs_peaks.so")
+    """FP32 FFMA and FP64 DFMA rates, the Gauss-Jordan pattern rate and the
+    device-to-page-locked-host write rate, from the probe library; empty
+    where it cannot be built or loaded."""
     out = {}
     try:
-        lib = ctypes.CDLL(path)
-    except OSError:
+        lib = ctypes.CDLL(build_peaks())
+    except (OSError, RuntimeError):
         return out
-    lib.geosgs_peak_fp32.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    for name in ("geosgs_peak_fp32", "geosgs_peak_fp64", "geosgs_peak_gj_pattern"):
+        getattr(lib, name).argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.geosgs_peak_host_write.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
-    lib.geosgs_peak_gj_pattern.argtypes = [ctypes.POINTER(ctypes.c_double)]
     v = ctypes.c_double(0.0)
     if lib.geosgs_peak_fp32(ctypes.byref(v)) == 0:
         out["fp32_tflops"] = v.value
+    if lib.geosgs_peak_fp64(ctypes.byref(v)) == 0:
+        out["fp64_tflops"] = v.value
     if lib.geosgs_peak_gj_pattern(ctypes.byref(v)) == 0:
         out["gj_pattern_tflops"] = v.value
     if lib.geosgs_peak_host_write(ctypes.c_int64(1 << 30), ctypes.byref(v)) == 0:
         out["host_write_gbs"] = v.value
     return out
+
+
+def solve_flops(sizes, refine_steps: int) -> float:
+    """Algorithmic FLOPs of the kriging systems on the survey's basis, per
+    system of n neighbours: n(n+1)/2 covariance evaluations, n^3/3 for the
+    Cholesky factorization, 2 n^2 for the two triangular solves, per
+    refinement step 2 n^2 (residual) + 2 n^2 (correction), 2 n for the
+    variance; sizes[n] = number of systems with n neighbours."""
+    nn = np.arange(len(sizes), dtype=np.float64)
+    per = nn * (nn + 1) / 2 + nn ** 3 / 3 + 2 * nn ** 2 + refine_steps * 4 * nn ** 2 + 2 * nn
+    return float(np.sum(np.asarray(sizes, dtype=np.float64) * per))
+
+
+def config_of(wl, ws: int) -> dict:
+    """The workload's configuration, identical for every arm (GPU and
+    reference): what is simulated, not how."""
+    N, R = wl.domain.nelements(), wl.nreals
+    return {"workload": wl.name, "grid": list(wl.domain.dims), "nodes": N,
+            "ndata": 0 if wl.data is None else wl.data.nrow(), "maxneighbors": wl.method.maxneighbors,
+            "nreals": R, "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 (value array >= %.1f GB)" % (N * R * 4 / 1e9)}
+
+
+def batch_config_of(bw, ws: int) -> dict:
+    N = bw.nodes()
+    return {"workload": bw.name, "ndomains": len(bw.items), "nodes": N, "nreals": bw.nreals,
+            "ndata": int(sum(0 if w.data is None else w.data.nrow() for w in bw.items)),
+            "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 (value array >= %.1f GB)" % (N * bw.nreals * 4 / 1e9)}
 
 
 def parse():
@@ -221,50 +275,53 @@ def cpu_sample(wl, nodes: int, nthreads: int = 0):
 
 
 def run_reference(args):
+    """The reference arm: the FP64 CPU restatement of SEQSIM on the host
+    cores, each step a bounded sample of the workload (the Julia reference
+    has no toolchain on the box).  `value` is the throughput measured on the
+    sample; `ms_per_step` is the sample's own wall time; the line says that the
+    value is extrapolated from a sample and how large the sample was."""
     ws, rank, _ = dist_setup(args)
     if rank != 0:
         return
+    note = ("Julia reference not runnable on this box (no Julia toolchain); timed the FP64 C++ "
+            "restatement of SEQSIM (oracle/) instead")
     if args.workload == "c5":
         from geosgs import workloads
 
         bw = workloads.c5("fp64", nreals=args.nreals or 8, ndomains=args.ndomains)
-        vals = []
+        vals, secs = [], []
         for i in range(args.warmup + args.steps):
-            v, cores, sample = cpu_sample_batch(bw, args.cpu_nodes * 4)
+            v, cores, sample, t = cpu_sample_batch(bw, args.cpu_nodes * 4)
             if i >= args.warmup:
                 vals.append(v)
+                secs.append(t)
         value = statistics.median(vals)
-        print(json.dumps({
-            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * bw.nodes() * bw.nreals / value,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded PCG64 domains, data and paths; Philox normals)",
-            "config": {"workload": bw.name, "ndomains": len(bw.items), "nodes": bw.nodes(), "nreals": bw.nreals},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "Julia reference not runnable on this box (no Julia toolchain); timed the FP64 C++ "
-                    "restatement of SEQSIM (oracle/) instead"}))
-        return
-    wl = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
-    vals, secs = [], []
-    for i in range(args.warmup + args.steps):
-        v, cores, sample, s = cpu_sample(wl, args.cpu_nodes)
-        if i >= args.warmup:
-            vals.append(v)
-            secs.append(s)
-    value = statistics.median(vals)
+        config = batch_config_of(bw, args.gpus)
+        full_ms = 1e3 * bw.nodes() * bw.nreals / value
+    else:
+        wl = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
+        vals, secs = [], []
+        for i in range(args.warmup + args.steps):
+            v, cores, sample, t = cpu_sample(wl, args.cpu_nodes)
+            if i >= args.warmup:
+                vals.append(v)
+                secs.append(t)
+        value = statistics.median(vals)
+        config = config_of(wl, args.gpus)
+        full_ms = 1e3 * wl.domain.nelements() * wl.nreals / value
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * wl.domain.nelements() * wl.nreals / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded PCG64 grid data, path and Philox normals)",
-        "config": {"workload": wl.name, "nodes": wl.domain.nelements(), "nreals": wl.nreals,
-                   "maxneighbors": wl.method.maxneighbors},
+        "config": config,
+        "extrapolated": True,
+        "sample": sample,
+        "sample_wall_ms_per_step": 1e3 * statistics.median(secs),
+        "full_workload_ms_estimate": full_ms,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "Julia reference not runnable on this box (no Julia toolchain); timed the FP64 C++ "
-                "restatement of SEQSIM (oracle/) instead",
+        "note": note,
     }
     print(json.dumps(out))
 
@@ -334,7 +391,7 @@ def time_device(wl, args, torch, ws, network=None):
     return res
 
 
-def time_e2e(wl, args, torch, ws, steps, sweep=None):
+def time_e2e(wl, args, torch, ws, steps, sweep=None, network=None):
     """Through the public C ABI with host buffers: create (host -> device
     copies of the problem), prepare, simulate with the FP64 result copied to
     pinned host memory, destroy."""
@@ -349,6 +406,8 @@ def time_e2e(wl, args, torch, ws, steps, sweep=None):
     def step(i):
         t = time.perf_counter()
         plan = geosgs.Plan(p, keep)
+        if network is not None:
+            plan.set_network(network)
         if sweep:
             plan.set_sweep(**sweep)
         t1 = time.perf_counter()
@@ -463,7 +522,7 @@ def cpu_sample_batch(bw, budget_nodes: int):
     cores = os.cpu_count()
     sample = (f"oracle FP64 on {used} whole domains of {bw.name} ({nodes} nodes x {bw.nreals} realizations: "
               f"search, solve and draw loop); {cores} threads")
-    return nodes * bw.nreals / secs, cores, sample
+    return nodes * bw.nreals / secs, cores, sample, secs
 
 
 def main_batch(args, torch, ws, rank, uuid):
@@ -523,18 +582,17 @@ def main_batch(args, torch, ws, rank, uuid):
     achieved = alg_bytes / (ms_sweep * 1e-3) / 1e9
     cpu = None
     if not args.no_cpu:
-        v, cores, sample = cpu_sample_batch(bw, args.cpu_nodes * 4)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample, _ = cpu_sample_batch(bw, args.cpu_nodes * 4)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample, "extrapolated": True}
     value = ws * N * R / (fast["ms"] * 1e-3)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 values)" if inf.values_fp64 else "f32",
         "data": "synthetic (seeded PCG64 domains, variograms, data and paths; on-device Philox normals)",
-        "config": {"workload": bw.name, "ndomains": len(bw.items), "nodes": N, "nreals": R,
-                   "ndata": int(inf.ndata), "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
-                   "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (sweep tables %.1f GB)" % ((sum_m * 12 + N * 32) / 1e9)},
+        "config": batch_config_of(bw, ws),
+        "arm": {"precision": "FP32 solve + double-FP32 refinement, FP64 Cholesky fallback",
+                "warm_start": False, "note": "batches run without the learned warm start"},
         "phases_ms": fast["phases"], "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior),
         "n_fp64_fallback": int(inf.n_fp64_fallback), "bin_systems": [int(x) for x in inf.bin_systems],
         "device_gb": inf.device_bytes / 1e9, "s_create": round(fast["s_create"], 2),
@@ -579,23 +637,11 @@ def main():
     wl = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
     N, R = wl.domain.nelements(), wl.nreals
 
-    clocks = ClockSampler(uuid).start()
-    fast = time_device(wl, args, torch, ws)
-    clk = clocks.stop()
-
-    fp64 = None
-    if not args.no_fp64:
-        wl64 = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
-        a64 = argparse.Namespace(**vars(args))
-        a64.steps = max(2, args.steps // 2)
-        a64.warmup = max(1, min(args.warmup, 2))
-        fp64 = time_device(wl64, a64, torch, ws)
-
-    learned_res = None
+    # the learned warm start: a network trained on systems the method
+    # generates (random 3D variograms, the workload's maxneighbors), before
+    # any timed region
+    params, training = None, None
     if not args.no_learned:
-        # learned warm start: train on systems the method generates (random
-        # 3D variograms, same maxneighbors), then time the same steps with the
-        # network warm-starting every FP32 solve
         from geosgs import learned
 
         if args.learned_systems is None:
@@ -606,33 +652,41 @@ def main():
         t_gen = time.perf_counter() - t0
         t0 = time.perf_counter()
         params, hist = learned.train(feat, count, target, torch, epochs=args.learned_epochs, batch=16384, lr=3e-3)
-        t_train = time.perf_counter() - t0
-        mean_sq = float((target ** 2).mean())
+        training = {"systems": args.learned_systems, "epochs": args.learned_epochs, "final_mse": hist[-1],
+                    "mean_sq_target": float((target ** 2).mean()), "s_generate": round(t_gen, 2),
+                    "s_train": round(time.perf_counter() - t0, 2)}
         del feat, count, target
         torch.cuda.empty_cache()
-        wll = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
-        wll.method.warm_start = True
-        al = argparse.Namespace(**vars(args))
-        al.steps = max(2, args.steps // 2)
-        al.warmup = max(1, min(args.warmup, 2))
-        learned_res = time_device(wll, al, torch, ws, network=params)
-        learned_res.update(dict(train_systems=args.learned_systems, epochs=args.learned_epochs,
-                                final_loss=hist[-1], mean_sq_weight=mean_sq, s_generate=t_gen, s_train=t_train))
+
+    # every arm is timed on the same steps; the headline arm is the metric's
+    # named form (learned + FP32) when the network is trained
+    wlh = workload(args.workload, "fp32", args.nreals, args.grid, args.ndata)
+    wlh.method.warm_start = params is not None
+    clocks = ClockSampler(uuid).start()
+    head = time_device(wlh, args, torch, ws, network=params)
+    clk = clocks.stop()
+    fp32 = time_device(wl, args, torch, ws) if params is not None else None
+    fp64 = None
+    if not args.no_fp64:
+        wl64 = workload(args.workload, "fp64", args.nreals, args.grid, args.ndata)
+        fp64 = time_device(wl64, args, torch, ws)
 
     e2e = None
     if not args.no_e2e:
-        e2e_s, e2e_inf, _ = time_e2e(wl, args, torch, ws, max(1, min(3, args.steps)), sweep=fast["sweep_config"])
+        e2e_s, e2e_inf, _ = time_e2e(wlh, args, torch, ws, max(1, min(3, args.steps)), sweep=head["sweep_config"],
+                                     network=params)
         e2e = {"value": ws * N * R / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(e2e_inf.h2d_bytes), "d2h_bytes_per_step": int(e2e_inf.d2h_bytes),
                "ms_per_step": 1e3 * e2e_s,
-               "path": "sgs_plan_create + sgs_plan_prepare + sgs_plan_simulate (FP64 out to pinned host) + sgs_plan_destroy",
+               "path": ("sgs_plan_create + " + ("sgs_plan_set_network + " if params is not None else "") +
+                        "sgs_plan_prepare + sgs_plan_simulate (FP64 out to pinned host) + sgs_plan_destroy"),
                "calls_ms": getattr(time_e2e, "split_ms", None)}
 
     if rank != 0:
         return
 
     # roofline of the sweep (kernel c): algorithmic bytes of one sweep
-    inf = fast["info"]
+    inf = head["info"]
     sum_m = int(inf.sum_grid_neighbors)
     sv = 8 if inf.values_fp64 else 4
     # neighbour row reads + value writes, plus the sweep tables: per grid
@@ -645,17 +699,17 @@ def main():
         peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except Exception:
         peak, peak_src = 6800.0, "fallback"
-    achieved = alg_bytes / (fast["ms_sweep"] * 1e-3) / 1e9
-    # DRAM traffic of one sweep from the committed ncu capture (measured on a
-    # smaller grid of the same workload, scaled by the node-realizations)
+    achieved = alg_bytes / (head["ms_sweep"] * 1e-3) / 1e9
+    # DRAM traffic of one sweep from the committed ncu capture of the form
+    # this workload times (all launches of one sweep), per node-realization
     traffic, tr = None, {}
     try:
         tr = json.load(open(os.path.join(ROOT, "profiles", "sweep_traffic.json")))
-        if args.workload == "c3" and R == 256:
-            traffic = tr["dram_bytes_per_node_real"] * N * R
+        if tr.get("workload") == wl.name and int(tr.get("nreals", 0)) == R:
+            traffic = tr["dram_bytes_per_sweep"]
     except Exception:
         pass
-    sc = fast["sweep_config"]
+    sc = head["sweep_config"]
     form = {0: "sweep_flow_kernel (dataflow launches%s)" % (
                 ", levels %d-%d by per-level launches" % (sc["level_lo"], sc["level_hi"] - 1)
                 if sc["level_hi"] > sc["level_lo"] else ""),
@@ -666,9 +720,9 @@ def main():
     roofline = {"kernel": form + ": all launches of one sweep", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_src, "traffic": traffic,
-                "traffic_measured_on": (tr.get("kernel") if traffic is not None else None),
+                "traffic_measured_on": (tr.get("measured_on") if traffic is not None else None),
                 "algorithmic_bytes": alg_bytes,
-                "ms": fast["ms_sweep"]}
+                "ms": head["ms_sweep"]}
 
     probes = measure_peaks()
     if e2e is not None and probes.get("host_write_gbs"):
@@ -676,76 +730,89 @@ def main():
         e2e["host_write_gbs"] = probes["host_write_gbs"]
         e2e["d2h_floor_ms"] = e2e["d2h_bytes_per_step"] / probes["host_write_gbs"] / 1e6
 
-    # the solve (kernel b) is bound by the FP32 pipe: per kriging system of n
-    # neighbours, Gauss-Jordan inversion 2 n^3 FLOPs plus two refinement steps
-    # (residual and correction, 2 n^2 each) = 2 n^3 + 8 n^2; peak = 152 SMs x
-    # 128 FP32 lanes x 2 FLOPs x the maximum SM clock (nominal, not measured)
-    sz = fast["system_sizes"]
-    nn = np.arange(sz.size, dtype=np.float64)
-    solve_flops = float(np.sum(sz * (2 * nn ** 3 + 8 * nn ** 2)))
+    # the solve (kernel b), bound by the FP32 pipe, on the survey's FLOP
+    # basis (factorization n^3/3, not the cost of the algorithm run); the
+    # executed Gauss-Jordan count (2 n^3 + 8 n^2) is reported beside it
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_nominal = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     if probes.get("fp32_tflops"):
         fp32_peak, fp32_src = probes["fp32_tflops"], "measured in this run: independent FFMA chains on every SM"
     else:
         fp32_peak, fp32_src = fp32_nominal, "nominal (SM count x lanes x max clock)"
-    solve_roof = {"kernel": "solve_fp32_kernel<NMAX> (+ lag table, FP64 fallbacks): one solve phase",
-                  "bound": "fp32", "achieved": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12,
-                  "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": fp32_src, "nominal_peak": fp32_nominal,
-                  "frac": solve_flops / (fast["ms_solve"] * 1e-3) / 1e12 / fp32_peak,
-                  "gj_pattern_peak": probes.get("gj_pattern_tflops"),
-                  "algorithmic_flops": solve_flops, "systems": int(sz.sum()),
-                  "mean_system_size": float(np.sum(sz * nn) / max(1, sz.sum())), "ms": fast["ms_solve"]}
+
+    def solve_roof(res, steps, peak_, src, kernel, executed=True):
+        sz = res["system_sizes"]
+        nn = np.arange(sz.size, dtype=np.float64)
+        fl = solve_flops(sz, steps)
+        tf = fl / (res["ms_solve"] * 1e-3) / 1e12
+        out_ = {"kernel": kernel, "achieved": tf, "peak": peak_, "unit": "TFLOP/s", "peak_source": src,
+                "frac": tf / peak_ if peak_ else None, "algorithmic_flops": fl,
+                "flop_basis": "n(n+1)/2 + n^3/3 + 2n^2 + %d x 4n^2 + 2n per system" % steps,
+                "systems": int(sz.sum()), "mean_system_size": float(np.sum(sz * nn) / max(1, sz.sum())),
+                "ms": res["ms_solve"]}
+        if executed:
+            ex = float(np.sum(sz * (2 * nn ** 3 + 8 * nn ** 2)))
+            out_["executed_flops"] = ex
+            out_["executed_basis"] = "Gauss-Jordan inverse 2n^3 + two refinement steps 8n^2"
+            out_["executed_tflops"] = ex / (res["ms_solve"] * 1e-3) / 1e12
+        return out_
+
+    head_steps = wlh.method.refine_steps + (1 if params is not None else 0)
+    solve_roofline = solve_roof(head, head_steps, fp32_peak, fp32_src,
+                                "solve_fp32_kernel<NMAX> (+ lag table, prediction, FP64 fallbacks): one solve phase")
+    solve_roofline["nominal_peak"] = fp32_nominal
+    solve_roofline["gj_pattern_peak"] = probes.get("gj_pattern_tflops")
 
     cpu = None
     if not args.no_cpu:
         v, cores, sample, _ = cpu_sample(wl, args.cpu_nodes)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample, "extrapolated": True}
 
-    value = ws * N * R / (fast["ms"] * 1e-3)
+    def phases(res, solve_key="solve"):
+        return {"search": res["ms_search"], "levels": res["ms_levels"], solve_key: res["ms_solve"],
+                "sweep": res["ms_sweep"]}
+
+    value = ws * N * R / (head["ms"] * 1e-3)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": fast["ms"], "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 values)" if inf.values_fp64 else "f32",
         "data": "synthetic (seeded PCG64 grid data and path; on-device Philox normals)",
-        "config": {"workload": wl.name, "grid": list(wl.domain.dims), "nodes": N,
-                   "ndata": 0 if wl.data is None else wl.data.nrow(), "maxneighbors": wl.method.maxneighbors,
-                   "nreals": R, "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
-                   "warm_start": False, "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (value array %.1f GB)" % (N * R * sv / 1e9)},
-        "phases_ms": {"search": fast["ms_search"], "levels": fast["ms_levels"], "solve": fast["ms_solve"],
-                      "sweep": fast["ms_sweep"]},
+        "config": config_of(wl, ws),
+        "arm": {"form": "learned warm start + FP32" if params is not None else "FP32",
+                "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
+                "warm_start": params is not None, "refine_steps": head_steps},
+        "phases_ms": phases(head, "solve_incl_prediction" if params is not None else "solve"),
         "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior), "n_fp64_fallback": int(inf.n_fp64_fallback),
+        "warm_start_accepted": int(inf.n_warm_accepted),
         "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
         "roofline": roofline,
-        "solve_roofline": solve_roof,
+        "solve_roofline": solve_roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "gpu_launches": int(fast["launches"]),
+        "gpu_launches": int(head["launches"]) // max(1, args.steps),
         "clocks": clk,
         "sweep_config": {k: v for k, v in sc.items()},
-        "sweep_candidates_ms": [round(t["ms"], 3) for t in fast["sweep_tried"]],
+        "sweep_candidates_ms": [round(t["ms"], 3) for t in head["sweep_tried"]],
     }
+    if training:
+        out["training"] = training
+    if fp32:
+        v32 = ws * N * R / (fp32["ms"] * 1e-3)
+        out["fp32_path"] = {"value": v32, "ms_per_step": fp32["ms"], "phases_ms": phases(fp32),
+                            "solve_roofline": solve_roof(fp32, wl.method.refine_steps, fp32_peak, fp32_src,
+                                                         "solve_fp32_kernel<NMAX>: one solve phase")}
     if fp64:
         v64 = ws * N * R / (fp64["ms"] * 1e-3)
-        out["fp64_path"] = {"value": v64, "ms_per_step": fp64["ms"],
-                            "phases_ms": {"search": fp64["ms_search"], "levels": fp64["ms_levels"],
-                                          "solve": fp64["ms_solve"], "sweep": fp64["ms_sweep"]}}
+        fp64_peak = probes.get("fp64_tflops")
+        out["fp64_path"] = {"value": v64, "ms_per_step": fp64["ms"], "phases_ms": phases(fp64),
+                            "solve_roofline": solve_roof(fp64, 0, fp64_peak, "measured in this run: independent "
+                                                         "DFMA chains on every SM" if fp64_peak else None,
+                                                         "solve_kernel<double, double>: one solve phase",
+                                                         executed=False)}
         out["speedup_vs_fp64_path"] = value / v64
-    if learned_res:
-        li = learned_res["info"]
-        vl = ws * N * R / (learned_res["ms"] * 1e-3)
-        out["learned_fp32_path"] = {
-            "value": vl, "ms_per_step": learned_res["ms"],
-            "phases_ms": {"search": learned_res["ms_search"], "levels": learned_res["ms_levels"],
-                          "solve_incl_prediction": learned_res["ms_solve"], "sweep": learned_res["ms_sweep"]},
-            "warm_start_accepted": int(li.n_warm_accepted), "fp64_fallback": int(li.n_fp64_fallback),
-            "kriged_systems": int(N - li.n_prior),
-            "training": {"systems": learned_res["train_systems"], "epochs": learned_res["epochs"],
-                         "final_mse": learned_res["final_loss"], "mean_sq_target": learned_res["mean_sq_weight"],
-                         "s_generate": round(learned_res["s_generate"], 2), "s_train": round(learned_res["s_train"], 2)},
-            "speedup_vs_fp64_path": (vl / (N * R / (fp64["ms"] * 1e-3) * ws)) if fp64 else None,
-        }
+        if fp32:
+            out["fp32_path"]["speedup_vs_fp64_path"] = out["fp32_path"]["value"] / v64
     print(json.dumps(out))
 
 

@@ -1,11 +1,13 @@
-// peaks.cu — device throughput probes used by the benchmark as roofline
+// bench_peaks.cu — device throughput probes used by bench.py as roofline
 // denominators that no driver-side measurement provides: the FP32 FFMA rate
-// (the bound of the kriging solve, which runs on the CUDA cores), the FP32
-// rate of the solve's Gauss-Jordan update pattern at the solve's occupancy,
-// and the rate at which kernels write page-locked host memory (the bound of
-// the FP64 output that sgs_plan_simulate writes straight into the caller's
-// buffer).
-// Built as its own library (libgeosgs_peaks.so); not part of the C ABI.
+// (the bound of the kriging solve, which runs on the CUDA cores), the FP64
+// DFMA rate (the bound of the plain FP64 path's solve), the FP32 rate of the
+// solve's Gauss-Jordan update pattern at the solve's occupancy, and the rate
+// at which kernels write page-locked host memory (the bound of the FP64
+// output that sgs_plan_simulate writes straight into the caller's buffer).
+// Measurement infrastructure beside the benchmark, built by bench.py as its
+// own library (_build/libgeosgs_peaks.so); not part of the product or its
+// C ABI.
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -23,6 +25,22 @@ __global__ void ffma_chains_kernel(float* out, int iters, float a) {
         for (int j = 0; j < NR; ++j) r[j] = __fmaf_rn(r[j], a, 0.5f);
     }
     float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) s += r[j];
+    out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// NR independent DFMA chains per thread
+template <int NR>
+__global__ void dfma_chains_kernel(double* out, int iters, double a) {
+    double r[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) r[j] = threadIdx.x * 1e-3 + j;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) r[j] = __fma_rn(r[j], a, 0.5);
+    }
+    double s = 0.0;
 #pragma unroll
     for (int j = 0; j < NR; ++j) s += r[j];
     out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
@@ -115,6 +133,36 @@ extern "C" int geosgs_peak_fp32(double* tflops) {
     cudaFree(out);
     if (err != cudaSuccess || best <= 0.f) return 3;
     *tflops = 2.0 * (double)blocks * threads * iters * 32 / (best * 1e-3) / 1e12;
+    return 0;
+}
+
+// Best of three timed launches of 16 DFMA chains per thread, 8 blocks of 256
+// threads per SM; *tflops = 2 x DFMA lanes per second / 1e12.  0 on success.
+extern "C" int geosgs_peak_fp64(double* tflops) {
+    const int nsm = sms();
+    if (!tflops || nsm <= 0) return 1;
+    const int blocks = nsm * 8, threads = 256, iters = 1000;
+    double* out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return 2;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        dfma_chains_kernel<16><<<blocks, threads>>>(out, iters, 0.999);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // the first launch warms up
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess || best <= 0.f) return 3;
+    *tflops = 2.0 * (double)blocks * threads * iters * 16 / (best * 1e-3) / 1e12;
     return 0;
 }
 

@@ -48,7 +48,6 @@ def up_to_date() -> bool:
 
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if not force and up_to_date():
-        build_peaks()
         return LIB_PATH
     nvcc = _nvcc()
     os.makedirs(OBJ_DIR, exist_ok=True)
@@ -71,23 +70,4 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
-    build_peaks(force=force)
     return LIB_PATH
-
-
-PEAKS_SRC = os.path.join(CSRC, "peaks", "peaks.cu")
-PEAKS_PATH = os.path.join(LIB_DIR, "libgeosgs_peaks.so")
-
-
-def build_peaks(force: bool = False) -> str:
-    """The throughput probes the benchmark reports beside its rooflines
-    (csrc/peaks/peaks.cu), as their own library."""
-    if not force and os.path.exists(PEAKS_PATH) and os.path.getmtime(PEAKS_SRC) <= os.path.getmtime(PEAKS_PATH):
-        return PEAKS_PATH
-    tmp = PEAKS_PATH + ".tmp"
-    cmd = [_nvcc(), *NVCC_FLAGS, "-shared", "-o", tmp, PEAKS_SRC]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {PEAKS_SRC}:\n{r.stderr}")
-    os.replace(tmp, PEAKS_PATH)
-    return PEAKS_PATH

@@ -45,11 +45,10 @@ def test_diagnostic_exports_outside_the_header():
 def test_peak_probe_library_builds_and_exports():
     """The benchmark's throughput probes live in their own library, outside
     the C ABI of include/geosgs.h."""
-    from geosgs import _build
+    import bench
 
-    _build.build()
-    lib = C.CDLL(_build.PEAKS_PATH)
-    for name in ("geosgs_peak_fp32", "geosgs_peak_gj_pattern", "geosgs_peak_host_write"):
+    lib = C.CDLL(bench.build_peaks())
+    for name in ("geosgs_peak_fp32", "geosgs_peak_fp64", "geosgs_peak_gj_pattern", "geosgs_peak_host_write"):
         assert hasattr(lib, name), name
     assert not any(n.startswith("geosgs_peak") for n in header_symbols())
 
