@@ -41,7 +41,8 @@ constexpr int kMaxLevels = SGS_NOALLOC_MAX_LEVELS;
 // per-level counts and fill cursors, kMaxLevels each
 static __device__ __align__(256) int32_t g_schedule_scratch[kHeader + 2 * kMaxLevels];
 
-// input error codes (scratch[3]); the smallest code raised is reported
+// input error codes (scratch[3], zero on entry); the first code raised is
+// kept
 enum : int32_t {
     kInOk = 0,
     kInPathRange = 1,      // a path entry outside [0, N)
@@ -51,6 +52,8 @@ enum : int32_t {
     kInLaterNeighbour = 5  // a grid neighbour that does not come earlier in the path
 };
 
+__device__ __forceinline__ void raise_code(int32_t* code, int32_t c) { atomicCAS(code, kInOk, c); }
+
 // Path ranks into rank[] (the caller's `order` buffer, all -1 on entry): a
 // path entry out of range or repeated raises its code.  With no code raised,
 // the N entries are N distinct ids in [0, N): a permutation.
@@ -58,10 +61,10 @@ __global__ void check_path_kernel(const int32_t* __restrict__ path, int64_t N, i
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
         const int32_t g = path[t];
         if (g < 0 || g >= N) {
-            atomicMin(code, kInPathRange);
+            raise_code(code, kInPathRange);
             continue;
         }
-        if (atomicCAS(&rank[g], -1, (int32_t)t) != -1) atomicMin(code, kInPathRepeat);
+        if (atomicCAS(&rank[g], -1, (int32_t)t) != -1) raise_code(code, kInPathRepeat);
     }
 }
 
@@ -72,18 +75,18 @@ __global__ void check_table_kernel(const int32_t* __restrict__ nbr, const int32_
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
         const int32_t n = count[g];
         if (n < 0 || n > k) {
-            atomicMin(code, kInCount);
+            raise_code(code, kInCount);
             continue;
         }
         const int32_t rg = rank[g];
         for (int q = 0; q < n; ++q) {
             const int32_t c = nbr[g * (int64_t)k + q];
             if (c < 0) {
-                atomicMin(code, kInNegNeighbour);
+                raise_code(code, kInNegNeighbour);
                 break;
             }
             if (c < N && rank[c] >= rg) {
-                atomicMin(code, kInLaterNeighbour);
+                raise_code(code, kInLaterNeighbour);
                 break;
             }
         }
