@@ -370,17 +370,35 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
     for (int64_t i = 0; i < H.D; ++i)
         if (!std::isfinite(pr->data_values[i])) HERR("data values must be finite");
     const sgs_variogram& v = pr->variogram;
-    if (v.type < SGS_SPHERICAL || v.type > SGS_GAUSSIAN) HERR("unknown variogram type");
-    if (!(v.sill > 0.0) || !(v.nugget >= 0.0) || v.nugget > v.sill || !std::isfinite(v.sill))
-        HERR("invalid sill/nugget");
-    for (int j = 0; j < dim; ++j)
-        if (!(v.ranges[j] > 0.0) || !std::isfinite(v.ranges[j])) HERR("ranges must be finite and > 0");
+    if (pr->nstructures < 0 || pr->nstructures >= SGS_MAX_STRUCTURES || (pr->nstructures > 0 && !pr->structures))
+        HERR("nstructures must be in [0, SGS_MAX_STRUCTURES) with a structures array");
+    // the model: `variogram` plus the nested structures, summed
+    H.vario.ns = 1 + pr->nstructures;
+    H.vario.sill = 0.0;
+    H.vario.nugget = 0.0;
+    double rmax = 0.0;  // range(f): the largest range of any structure
+    for (int i = 0; i < H.vario.ns; ++i) {
+        const sgs_variogram& u = i == 0 ? v : pr->structures[i - 1];
+        if (u.type < SGS_SPHERICAL || u.type > SGS_GAUSSIAN) HERR("unknown variogram type");
+        if (!(u.sill > 0.0) || !(u.nugget >= 0.0) || u.nugget > u.sill || !std::isfinite(u.sill))
+            HERR("invalid sill/nugget");
+        for (int j = 0; j < dim; ++j) {
+            if (!(u.ranges[j] > 0.0) || !std::isfinite(u.ranges[j])) HERR("ranges must be finite and > 0");
+            rmax = std::max(rmax, u.ranges[j]);
+        }
+        VarioStructDev& d = H.vario.st[i];
+        d.type = u.type;
+        d.sill = u.sill;
+        d.nugget = u.nugget;
+        for (int j = 0; j < 3; ++j) d.inv_range[j] = j < dim ? 1.0 / u.ranges[j] : 1.0;
+        for (int j = 0; j < 9; ++j) d.R[j] = u.rotation[j];
+        H.vario.sill += u.sill;
+        H.vario.nugget += u.nugget;
+    }
+    H.vario.type = H.vario.st[0].type;
+    for (int j = 0; j < 3; ++j) H.vario.inv_range[j] = H.vario.st[0].inv_range[j];
+    for (int j = 0; j < 9; ++j) H.vario.R[j] = H.vario.st[0].R[j];
     if (!std::isfinite(pr->mean)) HERR("mean must be finite");
-    H.vario.type = v.type;
-    H.vario.sill = v.sill;
-    H.vario.nugget = v.nugget;
-    for (int j = 0; j < 3; ++j) H.vario.inv_range[j] = j < dim ? 1.0 / v.ranges[j] : 1.0;
-    for (int j = 0; j < 9; ++j) H.vario.R[j] = v.rotation[j];
     H.mean = pr->mean;
 
     // seqsim.jl:202-208
@@ -396,8 +414,6 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
     // neighbourhood: seqsim.jl:171-177,221-227
     static const double I9[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (pr->search == SGS_SEARCH_RANGE) {
-        double rmax = v.ranges[0];
-        for (int j = 1; j < dim; ++j) rmax = std::max(rmax, v.ranges[j]);
         double r[3] = {rmax, rmax, rmax};
         set_metric(H.metric, dim, METRIC_ISO, r, I9);
     } else if (pr->search == SGS_SEARCH_BALL) {

@@ -89,10 +89,9 @@ __device__ __forceinline__ void cell_of(const GridDev& g, int node, int& i0, int
     i2 = r / g.n[1];
 }
 
-// covariance C(h) = sill - gamma(h) in FP64 (GeoStatsFunctions conventions;
-// the nugget applies for nonzero lags only)
-__device__ __forceinline__ double cov_fp64(const VarioDev& v, int dim, double h0, double h1, double h2) {
-    if (h0 == 0.0 && h1 == 0.0 && (dim == 2 || h2 == 0.0)) return v.sill;
+// gamma(h) of one structure at a nonzero lag (GeoStatsFunctions conventions:
+// practical ranges, nugget for nonzero lags only)
+__device__ __forceinline__ double structure_gamma(const VarioStructDev& v, int dim, double h0, double h1, double h2) {
     double s = 0.0;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -108,7 +107,16 @@ __device__ __forceinline__ double cov_fp64(const VarioDev& v, int dim, double h0
     if (v.type == 1) f = hn < 1.0 ? 1.5 * hn - 0.5 * hn * hn * hn : 1.0;
     else if (v.type == 2) f = 1.0 - exp(-3.0 * hn);
     else f = 1.0 - exp(-3.0 * s);
-    return v.sill - (v.nugget + (v.sill - v.nugget) * f);
+    return v.nugget + (v.sill - v.nugget) * f;
+}
+
+// covariance C(h) = sill - gamma(h) in FP64, gamma summed over the model's
+// structures
+__device__ __forceinline__ double cov_fp64(const VarioDev& v, int dim, double h0, double h1, double h2) {
+    if (h0 == 0.0 && h1 == 0.0 && (dim == 2 || h2 == 0.0)) return v.sill;
+    double g = structure_gamma(v.st[0], dim, h0, h1, h2);
+    for (int i = 1; i < v.ns; ++i) g += structure_gamma(v.st[i], dim, h0, h1, h2);
+    return v.sill - g;
 }
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw 2011) on counter (c0..c3), key (k0,k1)

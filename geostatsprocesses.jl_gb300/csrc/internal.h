@@ -43,11 +43,25 @@ struct MetricDev {
     float dh_f;         // bound on the FP32 rounding of an origin-relative coordinate
 };
 
+// One structure of a (nested) variogram model.
+struct VarioStructDev {
+    int type;
+    double sill, nugget;
+    double inv_range[3];
+    double R[9];
+};
+
+// The process's variogram: ns structures summed (GeoStatsFunctions'
+// NestedVariogram; ns = 1 for a single variogram).  type, inv_range and R
+// repeat the first structure (the learned warm start's frame); sill and
+// nugget are the model's, the structures' summed.
 struct VarioDev {
     int type;
     double sill, nugget;
     double inv_range[3];
     double R[9];
+    int ns;
+    VarioStructDev st[SGS_MAX_STRUCTURES];
 };
 
 // Covariance lookup table over integer grid lags L in [-e, e] per axis:

@@ -193,7 +193,9 @@ __device__ __forceinline__ void features_f32(const GridDev& G, const VarioDev& v
     f[3] = hn;
     const float sill = (float)v.sill, nug = (float)v.nugget;
     float c = 1.0f;
-    if (hn > 0.f) {
+    if (v.ns > 1) {  // a nested model: its covariance summed over the structures
+        c = (float)(cov_fp64(v, G.dim, (double)h[0], (double)h[1], (double)h[2]) / v.sill);
+    } else if (hn > 0.f) {
         float fr;
         if (v.type == 1) fr = hn < 1.f ? 1.5f * hn - 0.5f * hn * hn * hn : 1.f;
         else if (v.type == 2) fr = 1.f - __expf(-3.f * hn);

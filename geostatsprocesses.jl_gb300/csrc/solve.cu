@@ -393,11 +393,17 @@ cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, 
 // 1e-3 (near-singular: the canonical 1e-10 decision needs FP64) or whose
 // refinement does not contract is queued for the FP64 kernel.
 constexpr int SOLVE32_WARPS = 2;
+// resident blocks per SM the FP32 solve is compiled for: 6 x 2 warps at up to
+// 168 registers a thread fill the register file; systems of up to 64
+// neighbours hold two rows of 64 registers and get 4 blocks (255 registers)
+constexpr int solve32_min_blocks(int nmax) { return nmax > 48 ? 4 : 6; }
 
 template <int NMAX>
 struct Smem32 {
-    static constexpr int LDK = NMAX + 1;  // odd row stride: conflict-free row reads
-    static constexpr size_t K = (size_t)NMAX * LDK * sizeof(DF);
+    // the double-FP32 LHS as its packed lower triangle (row r at r(r+1)/2):
+    // half the shared memory of the square, so that the register file, not
+    // shared memory, bounds the resident warps
+    static constexpr size_t K = (size_t)NMAX * (NMAX + 1) / 2 * sizeof(DF);
     static constexpr size_t C = (size_t)NMAX * sizeof(DF);
     static constexpr size_t W = (size_t)NMAX * sizeof(DF);
     static constexpr int CB = NMAX > 32 ? 64 : 32;  // one entry per owned row
@@ -408,6 +414,9 @@ struct Smem32 {
     static constexpr size_t bytes = K + C + W + V + COL + INFO + LIN;
     static_assert(K % 16 == 0 && bytes % 16 == 0, "16-byte aligned per-warp layout");
 };
+
+// packed lower-triangle index of entry (i, j) of a symmetric matrix
+__device__ __forceinline__ int tri(int i, int j) { return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
 // normalized double-FP32 covariance between two points of the augmented set
 __device__ __forceinline__ DF kcov2n(const SolveArgs& a, const NbInfo& p, const NbInfo& q) {
@@ -435,7 +444,6 @@ template <int NMAX>
 __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTables<float>& tab, int64_t pos, int g,
                                                unsigned char* base, int lane) {
     using S = Smem32<NMAX>;
-    constexpr int LDK = S::LDK;
     constexpr bool TWO = NMAX > 32;  // lanes own a second row
     DF* K = reinterpret_cast<DF*>(base);
     DF* c = reinterpret_cast<DF*>(base + S::K);
@@ -497,11 +505,11 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                 for (int r = 0; r < n; ++r) {
                     if (info[r].did >= 0) continue;
                     const int base = lcentre + lin[r];
+                    DF* Kr = K + r * (r + 1) / 2;
                     for (int q = lane; q <= r; q += 32) {
                         if (info[q].did < 0) {
                             const float2 v = lut2[min(max(base - lin[q], 0), ltotal - 1)];
-                            K[r * LDK + q] = {v.x, v.y};
-                            K[q * LDK + r] = {v.x, v.y};
+                            Kr[q] = {v.x, v.y};
                         }
                     }
                 }
@@ -512,11 +520,7 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     if (ir.did >= 0) continue;
                     for (int q = lane; q <= r; q += 32) {
                         const NbInfo iq = info[q];
-                        if (iq.did < 0) {
-                            const DF v = kcov2n(a, iq, ir);
-                            K[r * LDK + q] = v;
-                            K[q * LDK + r] = v;
-                        }
+                        if (iq.did < 0) K[r * (r + 1) / 2 + q] = kcov2n(a, iq, ir);
                     }
                 }
             }
@@ -527,18 +531,18 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     const int da = dl[item / n], q = item % n;
                     const NbInfo iq = info[q];
                     if (iq.did >= 0 && q > da) continue;  // data-data pair once
-                    const DF v = df_from_double(kcov(a, iq, info[da]) * a.inv_sill);
-                    K[da * LDK + q] = v;
-                    K[q * LDK + da] = v;
+                    K[tri(da, q)] = df_from_double(kcov(a, iq, info[da]) * a.inv_sill);
                 }
             }
             __syncwarp();
             // ---- rows of the FP32 LHS into registers (identity padding) ----
             float R0[NMAX], R1[TWO ? NMAX : 1];
+            const int t0 = i0 * (i0 + 1) / 2, t1 = i1 * (i1 + 1) / 2;  // own rows' starts
 #pragma unroll
             for (int j = 0; j < NMAX; ++j) {
-                R0[j] = (i0 < n && j < n) ? K[i0 * LDK + j].hi : (i0 == j ? 1.0f : 0.0f);
-                if (TWO) R1[j] = (i1 < n && j < n) ? K[i1 * LDK + j].hi : (i1 == j ? 1.0f : 0.0f);
+                R0[j] = (i0 < n && j < n) ? K[j <= i0 ? t0 + j : j * (j + 1) / 2 + i0].hi : (i0 == j ? 1.0f : 0.0f);
+                if (TWO)
+                    R1[j] = (i1 < n && j < n) ? K[j <= i1 ? t1 + j : j * (j + 1) / 2 + i1].hi : (i1 == j ? 1.0f : 0.0f);
             }
             // ---- Gauss-Jordan sweep with column rotation: R -> -K^-1 ----
             // At step kk register j holds column (kk + j) mod NMAX, so the pivot
@@ -617,27 +621,40 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                 // residual computed (it also drives the last correction)
                 DF sw0 = w0, sw1 = w1;
                 float sr0 = 0.0f, sr1 = 0.0f;
+                // largest starting weight, for the one-correction estimate below
+                float wmax = fmaxf(i0 < n ? fabsf(w0.hi) : 0.0f, TWO && i1 < n ? fabsf(w1.hi) : 0.0f);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) wmax = fmaxf(wmax, __shfl_xor_sync(FULL_MASK, wmax, o));
+                bool early = false;
                 for (int s = 0;; ++s) {
                     // residual r = c - K w in double-FP32, own rows
                     float r0 = 0.0f, r1 = 0.0f;
+                    // row i of the packed triangle: entries t_i + j for j <= i,
+                    // then down column i (j (j + 1) / 2 + i) for j > i
                     if (i0 < n) {
                         DFAcc acc;
                         acc.init(c[i0]);
-                        for (int j = 0; j < n; ++j) acc.add_prod(df_neg(K[i0 * LDK + j]), w[j]);
+                        int jt = 0;  // j (j + 1) / 2
+                        for (int j = 0; j < n; ++j) {
+                            acc.add_prod(df_neg(K[j <= i0 ? t0 + j : jt + i0]), w[j]);
+                            jt += j + 1;
+                        }
                         r0 = acc.value().hi;
                     }
                     if (TWO && i1 < n) {
                         DFAcc acc;
                         acc.init(c[i1]);
-                        for (int j = 0; j < n; ++j) acc.add_prod(df_neg(K[i1 * LDK + j]), w[j]);
+                        int jt = 0;
+                        for (int j = 0; j < n; ++j) {
+                            acc.add_prod(df_neg(K[j <= i1 ? t1 + j : jt + i1]), w[j]);
+                            jt += j + 1;
+                        }
                         r1 = acc.value().hi;
                     }
-                    if (s + 1 >= steps) {
-                        sw0 = w0;
-                        sw1 = w1;
-                        sr0 = r0;
-                        sr1 = r1;
-                    }
+                    sw0 = w0;
+                    sw1 = w1;
+                    sr0 = r0;
+                    sr1 = r1;
                     if (s == steps) break;  // steps == 0: no correction
                     __syncwarp();
                     vec[i0] = r0;
@@ -669,10 +686,29 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     last = dmax;
                     __syncwarp();
                     if (s + 1 == steps) break;  // the final weights need no residual
+                    // One correction is enough when the start was already good:
+                    // the start's error is about |d| and the contraction factor
+                    // of the FP32 inverse about |d| / |w|, so the corrected
+                    // weights are off by about |d|^2 / |w| (measured on the
+                    // 200x200x100 anisotropic systems: within a factor 4 of the
+                    // true error, which is ~1e-12 there).
+                    if (s == 0 && !a.w_init && last * last <= 1e-10f * wmax && isfinite(last)) {
+                        early = true;
+                        break;
+                    }
+                    // Later corrections: stop as soon as the contraction test
+                    // below passes (a warm start from a prediction needs two).
+                    if (s >= 1 && prev > 0.0f && last < 0.5f * prev && (last / prev) * last <= 1e-9f &&
+                        isfinite(last)) {
+                        early = true;
+                        break;
+                    }
                 }
                 // the remaining error is about the contraction factor times the
                 // last correction
-                if (a.refine_steps >= 2) {
+                if (early) {
+                    accept = true;
+                } else if (a.refine_steps >= 2) {
                     const float rho = prev > 0.0f ? last / prev : 0.0f;
                     accept = rho < 0.5f && rho * last <= 1e-9f && isfinite(last);
                 } else {
@@ -749,7 +785,7 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
 }
 
 template <int NMAX>
-__global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const SolveArgs a, const SweepTables<float> tab) {
+__global__ void __launch_bounds__(SOLVE32_WARPS * 32, solve32_min_blocks(NMAX)) solve_fp32_kernel(const SolveArgs a, const SweepTables<float> tab) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -763,7 +799,7 @@ __global__ void __launch_bounds__(SOLVE32_WARPS * 32) solve_fp32_kernel(const So
 // (systems with at most NMAX neighbours, from any domain), each solved with
 // its domain's descriptor.
 template <int NMAX>
-__global__ void __launch_bounds__(SOLVE32_WARPS * 32)
+__global__ void __launch_bounds__(SOLVE32_WARPS * 32, solve32_min_blocks(NMAX))
 solve_fp32_batch_kernel(const SolveArgs* __restrict__ doms, const int64_t* __restrict__ noff, int ndom,
                         const int32_t* __restrict__ order, const int32_t* __restrict__ list,
                         const int32_t* __restrict__ desc, const SweepTables<float> tab) {

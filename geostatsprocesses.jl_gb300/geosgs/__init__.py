@@ -20,6 +20,7 @@ from .model import (
     IndicatorProcess,
     LinearPath,
     MetricBall,
+    NestedVariogram,
     RandomPath,
     RotX,
     RotY,
@@ -37,7 +38,7 @@ __all__ = [
     "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "ExponentialTransiogram", "GaussianTransiogram", "IndicatorProcess", "SphericalTransiogram",
-    "LinearPath", "MetricBall", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
+    "LinearPath", "MetricBall", "NestedVariogram", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
     "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
     "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

@@ -58,6 +58,9 @@ class SgsBall(C.Structure):
     _fields_ = [("radii", C.c_double * 3), ("rotation", C.c_double * 9)]
 
 
+SGS_MAX_STRUCTURES = 4
+
+
 class SgsProblem(C.Structure):
     _fields_ = [
         ("dim", C.c_int32),
@@ -79,6 +82,9 @@ class SgsProblem(C.Structure):
         ("warm_start", C.c_int32),
         ("device", C.c_int32),
         ("flags", C.c_int32),
+        ("nstructures", C.c_int32),
+        ("reserved2", C.c_int32),
+        ("structures", C.POINTER(SgsVariogram)),
     ]
 
 

@@ -113,6 +113,24 @@ class _Variogram:
         h = np.asarray(h, dtype=np.float64)
         return np.where(h > 0, self.nugget + (self.sill - self.nugget) * self._f(h), 0.0)
 
+    def gamma_at(self, lag, dim: int):
+        """gamma of lag vectors (rows of `lag`, dim components): the lag is
+        normalized by the structure's ellipsoid, |diag(1/ranges) R^T lag|."""
+        lag = np.atleast_2d(np.asarray(lag, dtype=np.float64))[:, :dim]
+        R = self.ball.rotation[:dim, :dim]
+        r = np.asarray(self.ball.padded_radii(dim)[:dim])
+        return self(np.sqrt((((lag @ R) / r) ** 2).sum(axis=1)))
+
+    def structures(self) -> list:
+        """The model's structures (one for a single variogram)."""
+        return [self]
+
+    def __add__(self, other):
+        """gamma_1 + gamma_2: a nested model (GeoStatsFunctions NestedVariogram)."""
+        if not isinstance(other, _Variogram):
+            return NotImplemented
+        return NestedVariogram(self.structures() + other.structures())
+
     def to_c(self, dim: int) -> _abi.SgsVariogram:
         v = _abi.SgsVariogram()
         v.type = self.TYPE
@@ -146,6 +164,43 @@ class GaussianVariogram(_Variogram):
 
     def _f(self, h):
         return 1.0 - np.exp(-3.0 * h * h)
+
+
+class NestedVariogram(_Variogram):
+    """A sum of variogram structures, gamma(h) = gamma_1(h) + ... + gamma_m(h)
+    (GeoStatsFunctions' NestedVariogram, written `g1 + g2` there and here):
+    every structure keeps its own sill, nugget, ranges and rotation; the
+    model's sill and nugget are their sums and its range the largest
+    (`range` of a nested model).  Up to SGS_MAX_STRUCTURES structures."""
+
+    def __init__(self, structures):
+        st = []
+        for g in structures:
+            if not isinstance(g, _Variogram):
+                raise ArgumentError("a nested variogram sums variograms")
+            st += g.structures()
+        if not 1 <= len(st) <= _abi.SGS_MAX_STRUCTURES:
+            raise ArgumentError("a nested variogram takes 1 to %d structures on the GPU" % _abi.SGS_MAX_STRUCTURES)
+        self._st = st
+        self.ball = st[0].ball
+        self.sill = float(sum(g.sill for g in st))
+        self.nugget = float(sum(g.nugget for g in st))
+
+    def structures(self) -> list:
+        return list(self._st)
+
+    def range(self) -> float:
+        return max(g.range() for g in self._st)
+
+    def __call__(self, h):
+        raise ArgumentError("a nested model has one normalized lag per structure; evaluate gamma_at(lag)")
+
+    def gamma_at(self, lag, dim: int):
+        """gamma of a lag vector (rows of `lag`), summed over the structures."""
+        return sum(g.gamma_at(lag, dim) for g in self._st)
+
+    def to_c(self, dim: int) -> _abi.SgsVariogram:
+        return self._st[0].to_c(dim)
 
 
 # ------------------------------------------------------------------- process

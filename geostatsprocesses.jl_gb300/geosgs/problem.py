@@ -72,7 +72,14 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         p.data_values = val.ctypes.data_as(C.POINTER(C.c_double))
     else:
         p.ndata = 0
-    p.variogram = (process.corr if isinstance(process, IndicatorProcess) else process.func).to_c(cdim)
+    func = process.corr if isinstance(process, IndicatorProcess) else process.func
+    st = func.structures()
+    p.variogram = st[0].to_c(cdim)
+    if len(st) > 1:  # further structures of a nested model
+        more = (_abi.SgsVariogram * (len(st) - 1))(*[g.to_c(cdim) for g in st[1:]])
+        keep.append(more)
+        p.nstructures = len(st) - 1
+        p.structures = C.cast(more, C.POINTER(_abi.SgsVariogram))
     p.mean = process.mean
     p.minneighbors = int(method.minneighbors)
     p.maxneighbors = int(method.maxneighbors)

@@ -79,6 +79,13 @@ extern "C" {
 /* Variogram gamma(h) = nugget*(h>0) + (sill-nugget)*f(h) with the
  * normalized anisotropic lag h = |diag(1/ranges) * R^T * lag|;
  * covariance C = sill - gamma (src/utils.jl:50-62). */
+/* Nested models (GeoStatsFunctions' NestedVariogram, gamma = gamma_1 + ... +
+ * gamma_m) are `variogram` plus sgs_problem.structures: every structure has its
+ * own type, sill, nugget, ranges and rotation, and the model's sill, nugget
+ * and range are the sums and the largest range (seqsim.jl:52 takes any
+ * GeoStatsFunctions function as the process's func). */
+#define SGS_MAX_STRUCTURES 4
+
 typedef struct sgs_variogram {
     int32_t type;          /* SGS_SPHERICAL / SGS_EXPONENTIAL / SGS_GAUSSIAN */
     int32_t reserved;
@@ -118,6 +125,9 @@ typedef struct sgs_problem {
     int32_t warm_start;       /* 1 = learned warm start of the kriging weights */
     int32_t device;           /* CUDA device ordinal */
     int32_t flags;            /* 0 or SGS_FLAG_* */
+    int32_t nstructures;      /* further nested structures (0 .. SGS_MAX_STRUCTURES-1) */
+    int32_t reserved2;
+    const sgs_variogram* structures; /* nstructures structures added to `variogram` */
 } sgs_problem;
 
 typedef struct sgs_plan sgs_plan;

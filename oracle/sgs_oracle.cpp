@@ -114,7 +114,10 @@ struct oracle_plan {
     int64_t N, D;
     std::vector<double> dx;   // D x 3 (padded)
     std::vector<double> dval; // D
-    sgs_variogram vario;
+    sgs_variogram vario;      // first structure
+    std::vector<sgs_variogram> vs;  // every structure of the (nested) model
+    std::vector<Metric> vms;        // their normalized lag metrics
+    double sill = 1.0;        // the model's sill: the structures' sills summed
     double mean;
     int nmin, nmax;
     Metric search;
@@ -167,20 +170,25 @@ struct oracle_plan {
             for (int j = 0; j < dim; ++j) x[j] = dx[(a - N) * 3 + j];
         }
     }
+    // C(h) = sill - gamma(h), gamma = sum over the structures of
+    // nugget_s + (sill_s - nugget_s) f_s(|h|_s) for h != 0 (utils.jl:50-62)
     double cov(const double* h) const {
         bool zero = true;
         for (int j = 0; j < dim; ++j) zero = zero && (h[j] == 0.0);
-        const double s = vario.sill, ng = vario.nugget;
-        if (zero) return s;
-        double hn = std::sqrt(vmetric.d2(h));
-        double f;
-        switch (vario.type) {
-            case SGS_SPHERICAL: f = hn < 1.0 ? 1.5 * hn - 0.5 * hn * hn * hn : 1.0; break;
-            case SGS_EXPONENTIAL: f = 1.0 - std::exp(-3.0 * hn); break;
-            default: f = 1.0 - std::exp(-3.0 * hn * hn); break;
+        if (zero) return sill;
+        double gamma = 0.0;
+        for (size_t i = 0; i < vs.size(); ++i) {
+            const double s = vs[i].sill, ng = vs[i].nugget;
+            const double hn = std::sqrt(vms[i].d2(h));
+            double f;
+            switch (vs[i].type) {
+                case SGS_SPHERICAL: f = hn < 1.0 ? 1.5 * hn - 0.5 * hn * hn * hn : 1.0; break;
+                case SGS_EXPONENTIAL: f = 1.0 - std::exp(-3.0 * hn); break;
+                default: f = 1.0 - std::exp(-3.0 * hn * hn); break;
+            }
+            gamma = i == 0 ? ng + (s - ng) * f : gamma + (ng + (s - ng) * f);
         }
-        double gamma = ng + (s - ng) * f;
-        return s - gamma;
+        return sill - gamma;
     }
 };
 
@@ -245,10 +253,25 @@ extern "C" int oracle_create(const sgs_problem* p, oracle_plan** out) {
     }
     P->vario = p->variogram;
     const sgs_variogram& v = P->vario;
-    if (v.type < SGS_SPHERICAL || v.type > SGS_GAUSSIAN) { delete P; return fail(SGS_ERR_ARG, "unknown variogram type"); }
-    if (!(v.sill > 0.0) || v.nugget < 0.0 || v.nugget > v.sill) { delete P; return fail(SGS_ERR_ARG, "invalid sill/nugget"); }
-    for (int j = 0; j < P->dim; ++j)
-        if (!(v.ranges[j] > 0.0)) { delete P; return fail(SGS_ERR_ARG, "ranges must be > 0"); }
+    if (p->nstructures < 0 || p->nstructures >= SGS_MAX_STRUCTURES || (p->nstructures > 0 && !p->structures)) {
+        delete P;
+        return fail(SGS_ERR_ARG, "invalid nested structures");
+    }
+    P->vs.assign(1, v);
+    for (int i = 0; i < p->nstructures; ++i) P->vs.push_back(p->structures[i]);
+    P->sill = 0.0;
+    double rmax = 0.0;  // range(f): the largest range of any structure
+    for (const sgs_variogram& u : P->vs) {
+        if (u.type < SGS_SPHERICAL || u.type > SGS_GAUSSIAN) { delete P; return fail(SGS_ERR_ARG, "unknown variogram type"); }
+        if (!(u.sill > 0.0) || u.nugget < 0.0 || u.nugget > u.sill) { delete P; return fail(SGS_ERR_ARG, "invalid sill/nugget"); }
+        for (int j = 0; j < P->dim; ++j) {
+            if (!(u.ranges[j] > 0.0)) { delete P; return fail(SGS_ERR_ARG, "ranges must be > 0"); }
+            rmax = std::max(rmax, u.ranges[j]);
+        }
+        P->sill += u.sill;
+        P->vms.emplace_back();
+        set_metric(P->vms.back(), P->dim, 1, u.ranges, u.rotation);
+    }
     P->mean = p->mean;
     set_metric(P->vmetric, P->dim, 1, v.ranges, v.rotation);
 
@@ -261,8 +284,6 @@ extern "C" int oracle_create(const sgs_problem* p, oracle_plan** out) {
     P->nmin = (int)nmin;
 
     // search neighbourhood: seqsim.jl:171-177, 221-227
-    double rmax = v.ranges[0];
-    for (int j = 1; j < P->dim; ++j) rmax = std::max(rmax, v.ranges[j]);
     if (p->search == SGS_SEARCH_RANGE) {
         double r[3] = {rmax, rmax, rmax};
         double I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -478,7 +499,7 @@ static void solve_node(oracle_plan* P, int64_t g, std::vector<double>& K, std::v
     P->solved[g] = 1;
     if (n < P->nmin) {  // seqsim.jl:109-111
         P->status[g] = SGS_NODE_PRIOR_NMIN;
-        P->sigma[g] = std::sqrt(P->vario.sill);
+        P->sigma[g] = std::sqrt(P->sill);
         return;
     }
     K.assign((size_t)n * n, 0.0);
@@ -493,13 +514,13 @@ static void solve_node(oracle_plan* P, int64_t g, std::vector<double>& K, std::v
         }
     }
     // Cholesky (lower, row a: L[a][b] for b <= a), pivot rule
-    const double tau = kSingularTau * P->vario.sill;
+    const double tau = kSingularTau * P->sill;
     for (int j = 0; j < n; ++j) {
         double s = K[(size_t)j * n + j];
         for (int l = 0; l < j; ++l) s -= K[(size_t)j * n + l] * K[(size_t)j * n + l];
         if (!(s > tau)) {  // seqsim.jl:127-131: status false -> prior
             P->status[g] = SGS_NODE_PRIOR_SINGULAR;
-            P->sigma[g] = std::sqrt(P->vario.sill);
+            P->sigma[g] = std::sqrt(P->sill);
             return;
         }
         double ljj = std::sqrt(s);
@@ -524,7 +545,7 @@ static void solve_node(oracle_plan* P, int64_t g, std::vector<double>& K, std::v
     }
     double wc = 0.0;
     for (int a = 0; a < n; ++a) wc += w[a] * c[a];
-    double var = P->vario.sill - wc;
+    double var = P->sill - wc;
     P->sigma[g] = std::sqrt(var > 0.0 ? var : 0.0);
     P->status[g] = SGS_NODE_KRIGED;
 }
@@ -563,7 +584,7 @@ extern "C" int oracle_krige(oracle_plan* P, double* mean, double* var, int nthre
     if (P->D == 0) {
         for (int64_t g = 0; g < P->N; ++g) {
             mean[g] = P->mean;
-            if (var) var[g] = P->vario.sill;
+            if (var) var[g] = P->sill;
         }
         return SGS_OK;
     }
@@ -642,7 +663,7 @@ extern "C" int oracle_simulate(oracle_plan* P, int32_t R, const double* z, uint6
         if (!P->solved[P->path[t]]) return fail(SGS_ERR_STATE, "simulate before solve");
     const int nt = nthreads_or_all(nthreads);
     const int k = P->nmax;
-    const double mu = P->mean, ssd = std::sqrt(P->vario.sill);
+    const double mu = P->mean, ssd = std::sqrt(P->sill);
 #pragma omp parallel num_threads(nt)
     {
         std::vector<double> vals(P->N + P->D);
@@ -787,6 +808,10 @@ extern "C" double oracle_covariance(const sgs_variogram* v, int32_t dim, const d
     oracle_plan P;
     P.dim = dim;
     P.vario = *v;
+    P.vs.assign(1, *v);
+    P.vms.emplace_back();
+    set_metric(P.vms.back(), dim, 1, v->ranges, v->rotation);
+    P.sill = v->sill;
     set_metric(P.vmetric, dim, 1, v->ranges, v->rotation);
     double h[3] = {lag[0], lag[1], dim == 3 ? lag[2] : 0.0};
     return P.cov(h);

@@ -338,3 +338,27 @@ def test_sweep_autotuner_keeps_the_fastest_form(oracle_mod, geosgs_lib):
     assert chosen["ms"] == min(t["ms"] for t in tried)
     assert rel_err(G.simulate(64, z), O.simulate(64, z)) <= VALUE_TOL
     G.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_nested_variogram_parity(dim, precision, oracle_mod, geosgs_lib):
+    """A nested model (spherical + exponential + gaussian structures, each
+    with its own ranges, rotation, sill and nugget) with data: neighbours
+    bit-exact, status identical, weights and values against the oracle."""
+    from test_oracle import _nested_case
+
+    proc, grid, data, method = _nested_case(precision, dim)
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    G = gpu_plan(p, keep)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    np.testing.assert_array_equal(G.neighbors()[0], O.neighbors()[0])
+    wg, sg, stg = G.weights()
+    wo, so, sto = O.weights()
+    np.testing.assert_array_equal(stg, sto)
+    tol = 1e-9 if precision == "fp64" else 1e-6
+    np.testing.assert_allclose(wg, wo, rtol=0, atol=tol)
+    np.testing.assert_allclose(sg, so, rtol=0, atol=tol)
+    z = np.random.default_rng(12).standard_normal((6, O.N))
+    assert rel_err(G.simulate(6, z), O.simulate(6, z)) <= VALUE_TOL
+    G.close()

@@ -213,3 +213,68 @@ def test_seeded_normals_are_standard(oracle_mod):
     assert abs(z.mean()) < 0.02 and abs(z.std() - 1.0) < 0.02
     z2 = oracle_mod.normals(123, 5000, 8)
     np.testing.assert_array_equal(z, z2)
+
+
+def _nested_case(precision="fp64", dim=2):
+    """A nested model (three structures with their own ranges, rotations,
+    sills and nuggets) on a small grid with data."""
+    if dim == 2:
+        grid = geosgs.CartesianGrid((14, 12))
+        rng = np.random.default_rng(41)
+        xy = rng.uniform(0.0, 1.0, (12, 2)) * np.array([14.0, 12.0])
+    else:
+        grid = geosgs.CartesianGrid((10, 9, 6))
+        rng = np.random.default_rng(42)
+        xy = rng.uniform(0.0, 1.0, (15, 3)) * np.array([10.0, 9.0, 6.0])
+    func = (geosgs.SphericalVariogram(ranges=(7.0, 3.0, 2.0), rotation=geosgs.RotZ(35.0), sill=0.5, nugget=0.03)
+            + geosgs.ExponentialVariogram(range=9.0, sill=0.3)
+            + geosgs.GaussianVariogram(ranges=(4.0, 6.0, 3.0), rotation=geosgs.RotZ(-20.0), sill=0.2, nugget=0.01))
+    data = geosgs.georef({"Z": rng.standard_normal(len(xy))}, xy)
+    proc = geosgs.GaussianProcess(func, 0.25)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(3), maxneighbors=10, precision=precision)
+    return proc, grid, data, method
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_nested_variogram_weights_against_numpy(dim, oracle_mod):
+    """The oracle's kriging weights and variances for a nested model equal a
+    numpy solve whose covariances are the structures' summed, C(h) = sill -
+    sum_s gamma_s(h) (model.NestedVariogram.gamma_at), on the oracle's own
+    neighbours."""
+    proc, grid, data, method = _nested_case("fp64", dim)
+    func = proc.func
+    assert len(func.structures()) == 3 and abs(func.sill - 1.0) < 1e-15 and abs(func.nugget - 0.04) < 1e-15
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    idx, cnt = O.neighbors()
+    w, s, st = O.weights()
+    pts = np.concatenate([grid.centroids(), data.coords])
+    checked = 0
+    for g in range(O.N):
+        n = cnt[g]
+        if st[g] != 0 or n < 2:
+            continue
+        x = pts[idx[g, :n]]
+        lag = (x[:, None, :] - x[None, :, :]).reshape(-1, dim)
+        K = func.sill - func.gamma_at(lag, dim).reshape(n, n)
+        K[np.all(lag.reshape(n, n, dim) == 0, axis=2)] = func.sill
+        c = func.sill - func.gamma_at(x - pts[g], dim)
+        wn = np.linalg.solve(K, c)
+        np.testing.assert_allclose(w[g, :n], wn, rtol=0, atol=1e-10)
+        assert abs(s[g] - np.sqrt(max(func.sill - wn @ c, 0.0))) < 1e-10
+        checked += 1
+    assert checked > O.N // 2
+
+
+def test_nested_range_sets_the_search_radius(oracle_mod):
+    """`:range` takes the largest range of any structure (GeoStatsFunctions'
+    range of a nested model): the template is that of the longer structure."""
+    grid = geosgs.CartesianGrid((40, 40))
+    short = geosgs.SphericalVariogram(range=4.0, sill=0.5)
+    long = geosgs.ExponentialVariogram(range=11.0, sill=0.5)
+    m = geosgs.GPUSEQSIM(path=geosgs.RandomPath(1), maxneighbors=8)
+    sizes = []
+    for f in (short + long, long, short):
+        p, keep = geosgs.build_problem(geosgs.GaussianProcess(f), grid, None, m)
+        sizes.append(oracle_mod.OraclePlan(p, keep).template_size())
+    assert sizes[0] == sizes[1] > sizes[2]
