@@ -23,6 +23,7 @@ using Meshes
 using GeoTables
 using GeoStatsFunctions
 using Unitful: ustrip
+using Distances: Euclidean
 using GeoStatsProcesses
 import GeoStatsProcesses: preprocess, randsingle, FieldSimulationMethod
 
@@ -66,22 +67,29 @@ struct SgsProblem
   warm_start::Int32
   device::Int32
   flags::Int32
+  nstructures::Int32
+  reserved2::Int32
+  structures::Ptr{SgsVariogram}
 end
 
 const SGS_SEARCH_RANGE, SGS_SEARCH_BALL, SGS_SEARCH_NEAREST = Int32(0), Int32(1), Int32(2)
 
 """
-    GPUSEQSIM(; path, minneighbors, maxneighbors, neighborhood, precision, refine_steps, batch, device)
+    GPUSEQSIM(; path, minneighbors, maxneighbors, neighborhood, distance, precision, refine_steps, batch, device)
 
-SEQSIM's options (`path`, `minneighbors`, `maxneighbors`, `neighborhood`)
-plus `precision` (`:fp32` = FP32 solves with FP64 refinement, `:fp64`),
-`refine_steps`, `batch` (realizations simulated per GPU call) and `device`.
+SEQSIM's options (`path`, `minneighbors`, `maxneighbors`, `neighborhood`,
+`distance`; seqsim.jl:42-48, same defaults) plus `precision` (`:fp32` = FP32
+solves with FP64 refinement, `:fp64`), `refine_steps`, `batch`
+(realizations simulated per GPU call) and `device`.  `distance` must be the
+Euclidean distance (the GPU search computes Euclidean and ellipsoid metrics
+only); anything else is an `ArgumentError`.
 """
-Base.@kwdef struct GPUSEQSIM{P,N} <: FieldSimulationMethod
+Base.@kwdef struct GPUSEQSIM{P,N,D} <: FieldSimulationMethod
   path::P = LinearPath()
   minneighbors::Int = 1
   maxneighbors::Int = 26
   neighborhood::N = :range
+  distance::D = Euclidean()
   precision::Symbol = :fp32
   refine_steps::Int = 2
   batch::Int = 64
@@ -109,7 +117,12 @@ end
 vtype(::SphericalVariogram) = Int32(1)
 vtype(::ExponentialVariogram) = Int32(2)
 vtype(::GaussianVariogram) = Int32(3)
-vtype(f) = throw(ArgumentError("GPUSEQSIM supports spherical, exponential and gaussian variograms"))
+vtype(f) = throw(ArgumentError("GPUSEQSIM supports spherical, exponential and gaussian variograms and their sums"))
+
+# the structures of a (nested) model: a NestedVariogram c1 g1 + c2 g2 + ...
+# gives structure i the sill c_i sill(g_i) and nugget c_i nugget(g_i)
+structures(f::NestedVariogram) = [(Float64(c), g) for (c, g) in zip(f.cs, f.γs)]
+structures(f) = [(1.0, f)]
 
 pad3(t, fill) = ntuple(i -> i <= length(t) ? Float64(t[i]) : fill, 3)
 # radii of a ball; a 1D problem runs as the n x 1 grid, whose second axis
@@ -125,8 +138,11 @@ end
 
 # Geometry, neighbourhood, data and path of a problem -> a created plan; the
 # `before_prepare` hook runs between sgs_plan_create and sgs_plan_prepare.
-function _plan(vg::SgsVariogram, mean, method::GPUSEQSIM, grid, data, datavals; before_prepare=identity)
+function _plan(vgs::Vector{SgsVariogram}, mean, method::GPUSEQSIM, grid, data, datavals; before_prepare=identity)
   grid isa CartesianGrid || throw(ArgumentError("GPUSEQSIM simulates on a CartesianGrid"))
+  method.distance isa Euclidean || throw(ArgumentError("GPUSEQSIM supports the Euclidean distance only"))
+  1 <= length(vgs) <= 4 || throw(ArgumentError("GPUSEQSIM takes 1 to 4 nested structures"))
+  vg, more = vgs[1], vgs[2:end]
   dim = embeddim(grid)
   cdim = dim == 1 ? 2 : dim  # 1D: the n x 1 grid with the data on the row's centre line (y = 0.5)
   dims = size(grid)
@@ -151,12 +167,13 @@ function _plan(vg::SgsVariogram, mean, method::GPUSEQSIM, grid, data, datavals; 
   end
   path = Int32.(collect(traverse(grid, method.path)) .- 1)  # one path for all realizations
   planref = Ref{Ptr{Cvoid}}(C_NULL)
-  GC.@preserve xy vals path begin
+  GC.@preserve xy vals path more begin
     prob = SgsProblem(Int32(cdim), pad3(dims, 1.0) .|> Int32, pad3(orig, 0.0), pad3(spac, 1.0),
                       length(vals), pointer(xy), pointer(vals), vg, Float64(mean),
                       method.minneighbors, method.maxneighbors, search,
                       method.precision === :fp64 ? Int32(0) : Int32(1), sball, pointer(path),
-                      method.refine_steps, 0, method.device, 0)
+                      method.refine_steps, 0, method.device, 0,
+                      length(more), 0, isempty(more) ? Ptr{SgsVariogram}(C_NULL) : pointer(more))
     check(ccall((:sgs_plan_create, libgeosgs), Cint, (Ref{SgsProblem}, Ref{Ptr{Cvoid}}), prob, planref), C_NULL)
   end
   plan = GPUPlan(planref[])
@@ -168,10 +185,11 @@ end
 function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, init, domain, data)
   f = process.func
   dim = embeddim(domain)
-  vg = SgsVariogram(vtype(f), 0, ustrip(sill(f)), ustrip(nugget(f)), radii3(f.ball, dim), rot9(rotation(f.ball), dim))
+  vgs = [SgsVariogram(vtype(g), 0, c * ustrip(sill(g)), c * ustrip(nugget(g)), radii3(g.ball, dim),
+                      rot9(rotation(g.ball), dim)) for (c, g) in structures(f)]
   var = isnothing(data) ? :field : first(propertynames(values(data)))
   vals = isnothing(data) ? Float64[] : Float64.(ustrip.(getproperty(values(data), var)))
-  plan = _plan(vg, ustrip(process.mean), method, domain, data, vals)
+  plan = _plan(vgs, ustrip(process.mean), method, domain, data, vals)
   (; plan, var, nelm=nelements(domain), block=Ref(Matrix{Float64}(undef, 0, 0)), cursor=Ref(0))
 end
 
@@ -216,7 +234,7 @@ function preprocess(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQS
   setind(plan) = GC.@preserve prob cats check(ccall((:sgs_plan_set_indicator, libgeosgs), Cint,
                                                      (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Int32}),
                                                      plan.ptr, length(prob), prob, cats), plan.ptr)
-  plan = _plan(rho, 0.0, method, domain, data, zeros(length(cats)); before_prepare=setind)
+  plan = _plan([rho], 0.0, method, domain, data, zeros(length(cats)); before_prepare=setind)
   (; plan, var, labels, nelm=nelements(domain), block=Ref(Matrix{Int32}(undef, 0, 0)), cursor=Ref(0))
 end
 
