@@ -346,7 +346,7 @@ struct sgs_batch {
     int32_t* d_scratch = nullptr;  // [0] maxlevel [1] level-wait error
     unsigned long long* d_ticket = nullptr;  // levels ticket
     unsigned long long* d_sums = nullptr;    // [0] sum of grid neighbours (tables) [1] sum_m [2] priors
-    unsigned long long* d_flow = nullptr;    // sweep ticket, error flag
+    unsigned long long* d_flow = nullptr;    // sweep ticket, error flag, second launch's ticket
     uint64_t* d_seed = nullptr;
     uint64_t* h_seed = nullptr;    // pinned
     int32_t* d_done = nullptr;
@@ -366,15 +366,28 @@ struct sgs_batch {
     sgs_sweep_config sweep{SGS_SWEEP_FLOW, 1, 0, 1, 0, 0, 0, 0, 0, 0.f};
     bool sweep_graph_valid = false;
     bool sweep_pending = false;    // a device-resident sweep not yet checked
-    unsigned int* d_wl1 = nullptr; // largest sum of |grid weights| (FP32 bits)
-    bool promote = false;          // FP32 refinement, FP64 values (weights amplify rounding)
-    bool sweep_promote = false;    // value type the captured sweep graph was built for
+    unsigned int* d_wl1 = nullptr; // per domain: largest sum of |grid weights| (FP32 bits)
+    // FP32 refinement with FP64 values for the domains whose weights amplify
+    // the rounding of stored values (dom_fp64[d]); the value array then has
+    // FP64 rows (Rp doubles per node), and the other domains keep FP32 values
+    // in the first half of their rows, swept by a second launch (mixed)
+    bool promote = false;          // some domain keeps FP64 values
+    bool mixed = false;            // ... and some domain FP32 values
+    std::vector<uint8_t> dom_fp64;
+    uint8_t* d_cls = nullptr;      // per node: 1 = its domain keeps FP64 values
+    bool sweep_promote = false;    // value layout the captured sweep graph was built for
+    bool sweep_mixed = false;
     sgs_batch_info info{};
 };
 
 // the sweep's value type; promoted batches read the packed (hi, lo) FP32
 // tables through an FP64-typed view (FlowArgs::pairs)
 static bool values_fp64(const sgs_batch* B) { return B->precision == SGS_PREC_FP64 || B->promote; }
+// domain d's values: FP64 rows, or FP32 rows (in the first half of each FP64
+// row when the batch is mixed)
+static bool domain_fp64(const sgs_batch* B, int d) {
+    return B->precision == SGS_PREC_FP64 || (B->promote && (!B->mixed || B->dom_fp64[d]));
+}
 static SweepTables<double> sweep64(const sgs_batch* B) {
     if (!B->promote) return B->t64;
     SweepTables<double> v{};
@@ -655,9 +668,9 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
     if ((rc = balloc(B, &B->d_scratch, 4))) return rc;
     if ((rc = balloc(B, &B->d_ticket, 1))) return rc;
     if ((rc = balloc(B, &B->d_sums, 4))) return rc;
-    if ((rc = balloc(B, &B->d_flow, 2))) return rc;
+    if ((rc = balloc(B, &B->d_flow, 3))) return rc;
     if ((rc = balloc(B, &B->d_seed, 1))) return rc;
-    if ((rc = balloc(B, &B->d_wl1, 1))) return rc;
+    if ((rc = balloc(B, &B->d_wl1, nd))) return rc;
 
     // descriptors
     B->search.resize(nd);
@@ -706,7 +719,7 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
         s.fallback = B->d_fallback;
         s.nfallback = B->d_fbdesc;
         s.sum_m = B->d_sums + 1;
-        s.wl1_max = B->d_wl1;
+        s.wl1_max = B->d_wl1 + d;
         s.node0 = B->noff[d];
 
         ld[d] = LevelDom{B->noff[d], B->nbr0[d], (int32_t)h.N, h.k};
@@ -788,7 +801,7 @@ static int enqueue_prepare(sgs_batch* B, int64_t& launched) {
     // kriging systems by size class
     BCK(B, cudaMemsetAsync(B->d_fbdesc, 0, 2 * sizeof(int32_t), st));
     BCK(B, cudaMemsetAsync(B->d_sums + 1, 0, sizeof(unsigned long long), st));
-    BCK(B, cudaMemsetAsync(B->d_wl1, 0, sizeof(unsigned int), st));
+    BCK(B, cudaMemsetAsync(B->d_wl1, 0, (size_t)B->ndom * sizeof(unsigned int), st));
     for (int b = 0; b < NBIN; ++b) {
         if (B->precision == SGS_PREC_FP64)
             BLAUNCH(B, launch_solve_fp64_batch(bin_nmax(b), B->d_solve, B->d_noff, nd, B->d_order, B->d_blist,
@@ -872,21 +885,45 @@ extern "C" int sgs_batch_prepare(sgs_batch* B) {
     int32_t hs[4] = {0, 0, 0, 0};
     unsigned long long su[4] = {0, 0, 0, 0};
     int32_t hb[2 * NBIN], hf[2];
-    unsigned int wl1 = 0;
-    BCK(B, cudaMemcpyAsync(&wl1, B->d_wl1, sizeof(wl1), cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned int> wl1(B->ndom);
+    BCK(B, cudaMemcpyAsync(wl1.data(), B->d_wl1, wl1.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hs, B->d_scratch, sizeof(hs), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(su, B->d_sums, sizeof(su), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hb, B->d_bdesc, sizeof(hb), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaMemcpyAsync(hf, B->d_fbdesc, sizeof(hf), cudaMemcpyDeviceToHost, st));
     BCK(B, cudaStreamSynchronize(st));
-    B->info.d2h_bytes += sizeof(hs) + sizeof(su) + sizeof(hb) + sizeof(hf) + sizeof(wl1);
+    B->info.d2h_bytes += sizeof(hs) + sizeof(su) + sizeof(hb) + sizeof(hf) + wl1.size() * sizeof(unsigned int);
     if (hs[1]) return berr(B, SGS_ERR_TIMEOUT, "dependency-level wait exceeded its bound");
     {
-        float f;
-        std::memcpy(&f, &wl1, sizeof(f));
-        B->info.weight_l1_max = f;
-        B->promote = B->precision == SGS_PREC_FP32_REFINE && f > SGS_FP32_VALUE_L1_LIMIT;
+        // value precision per domain: FP64 values only where the domain's
+        // weights amplify the rounding of stored FP32 values
+        float fmax = 0.0f;
+        int nfp64 = 0;
+        B->dom_fp64.assign(B->ndom, 0);
+        for (int d = 0; d < B->ndom; ++d) {
+            float f;
+            std::memcpy(&f, &wl1[d], sizeof(f));
+            fmax = std::max(fmax, f);
+            if (B->precision == SGS_PREC_FP32_REFINE && f > SGS_FP32_VALUE_L1_LIMIT) {
+                B->dom_fp64[d] = 1;
+                ++nfp64;
+            }
+        }
+        B->info.weight_l1_max = fmax;
+        B->promote = nfp64 > 0;
+        B->mixed = nfp64 > 0 && nfp64 < B->ndom;
+        if (B->mixed) {
+            if (!B->d_cls) {
+                int rc = balloc(B, &B->d_cls, B->Ntot);
+                if (rc) return rc;
+            }
+            BCK(B, cudaMemsetAsync(B->d_cls, 0, (size_t)B->Ntot, st));
+            for (int d = 0; d < B->ndom; ++d)
+                if (B->dom_fp64[d])
+                    BCK(B, cudaMemsetAsync(B->d_cls + B->noff[d], 1, (size_t)(B->noff[d + 1] - B->noff[d]), st));
+        }
         B->info.values_fp64 = values_fp64(B) ? 1 : 0;
+        B->info.domains_fp64 = B->precision == SGS_PREC_FP64 ? B->ndom : nfp64;
     }
     B->info.nlevels = hs[0] + 1;
     B->info.sum_grid_neighbors = (int64_t)su[1];
@@ -910,7 +947,7 @@ static int enqueue_sweep(sgs_batch* B, int Rp, const void* z, void* V, cudaStrea
     const int64_t nflags = B->Ntot * H;
     if (nflags > B->done_cap) return berr(B, SGS_ERR_STATE, "sweep flags not allocated");
     BCK(B, cudaMemsetAsync(B->d_done, 0, nflags * sizeof(int32_t), st));
-    BCK(B, cudaMemsetAsync(B->d_flow, 0, 2 * sizeof(unsigned long long), st));
+    BCK(B, cudaMemsetAsync(B->d_flow, 0, 3 * sizeof(unsigned long long), st));
     FlowArgs f{};
     f.item0 = 0;
     f.item1 = B->Ntot * H;
@@ -926,10 +963,26 @@ static int enqueue_sweep(sgs_batch* B, int Rp, const void* z, void* V, cudaStrea
     f.wait_ns = 10000000000ull;  // 10 s: far beyond any dependency chain
     f.seed_dev = B->d_seed;
     f.pairs = B->promote ? 1 : 0;
-    if (values_fp64(B))
+    if (B->mixed) {
+        // two launches over disjoint domains: FP32 values in the first half
+        // of each FP64 row, then the FP64 domains with their own ticket
+        FlowArgs f32 = f;
+        f32.pairs = 0;
+        f32.row_stride = 2 * (int64_t)Rp;
+        f32.node_class = B->d_cls;
+        f32.cls = 0;
+        BLAUNCH(B, launch_sweep_flow_fp32(B->t32, B->kmax, Rp, W, G, (const float*)z, 0, (float*)V, f32, B->nsm, st));
+        FlowArgs f64 = f;
+        f64.ticket = B->d_flow + 2;
+        f64.node_class = B->d_cls;
+        f64.cls = 1;
+        BLAUNCH(B, launch_sweep_flow_fp64(sweep64(B), B->kmax, Rp, W, G, (const double*)z, 0, (double*)V, f64, B->nsm,
+                                          st));
+    } else if (values_fp64(B)) {
         BLAUNCH(B, launch_sweep_flow_fp64(sweep64(B), B->kmax, Rp, W, G, (const double*)z, 0, (double*)V, f, B->nsm, st));
-    else
+    } else {
         BLAUNCH(B, launch_sweep_flow_fp32(B->t32, B->kmax, Rp, W, G, (const float*)z, 0, (float*)V, f, B->nsm, st));
+    }
     return SGS_OK;
 }
 
@@ -963,7 +1016,7 @@ static int run_sweep_graph(sgs_batch* B, int Rp, uint64_t seed, void* V, cudaStr
     int rc;
     if ((rc = ensure_flags(B, Rp))) return rc;
     if (!B->sweep_exec || B->sweep_Rp != Rp || B->sweep_V != V || B->sweep_stream != st || !B->sweep_graph_valid ||
-        B->sweep_promote != B->promote) {
+        B->sweep_promote != B->promote || B->sweep_mixed != B->mixed) {
         if (B->sweep_exec) {
             BCK(B, cudaStreamSynchronize(B->sweep_stream ? B->sweep_stream : B->stream));
             cudaGraphExecDestroy(B->sweep_exec);
@@ -990,6 +1043,7 @@ static int run_sweep_graph(sgs_batch* B, int Rp, uint64_t seed, void* V, cudaStr
         B->sweep_V = V;
         B->sweep_stream = st;
         B->sweep_promote = B->promote;
+        B->sweep_mixed = B->mixed;
         B->sweep_graph_valid = true;
     }
     *B->h_seed = seed;
@@ -1047,7 +1101,8 @@ extern "C" int sgs_batch_simulate(sgs_batch* B, int32_t R, const double* z, uint
             const int64_t n0 = B->noff[d], n = B->noff[d + 1] - n0;
             BCK(B, cudaMemcpyAsync(zin, z + R * n0, (size_t)n * R * sizeof(double), cudaMemcpyHostToDevice, st));
             B->info.h2d_bytes += (int64_t)n * R * sizeof(double);
-            if (f64) BLAUNCH(B, launch_z_to_rows_fp64(zin, n, R, Rp, (double*)zr + n0 * Rp, st));
+            if (domain_fp64(B, d)) BLAUNCH(B, launch_z_to_rows_fp64(zin, n, R, Rp, (double*)zr + n0 * Rp, st));
+            else if (f64) BLAUNCH(B, launch_z_to_rows_fp32(zin, n, R, 2 * Rp, (float*)((double*)zr + n0 * Rp), st));
             else BLAUNCH(B, launch_z_to_rows_fp32(zin, n, R, Rp, (float*)zr + n0 * Rp, st));
         }
         if ((rc = ensure_flags(B, Rp))) {
@@ -1070,8 +1125,13 @@ extern "C" int sgs_batch_simulate(sgs_batch* B, int32_t R, const double* z, uint
     double* dout = pinned_device_view(out);
     for (int d = 0; dout && d < B->ndom; ++d) {
         const int64_t n0 = B->noff[d], n = B->noff[d + 1] - n0;
-        if (f64) BLAUNCH(B, launch_rows_to_out_fp64((const double*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
-        else BLAUNCH(B, launch_rows_to_out_fp32((const float*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
+        if (domain_fp64(B, d))
+            BLAUNCH(B, launch_rows_to_out_fp64((const double*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
+        else if (f64)
+            BLAUNCH(B, launch_rows_to_out_fp32((const float*)((const double*)V + n0 * Rp), n, R, 2 * Rp, B->mean[d],
+                                               dout + R * n0, st));
+        else
+            BLAUNCH(B, launch_rows_to_out_fp32((const float*)V + n0 * Rp, n, R, Rp, B->mean[d], dout + R * n0, st));
         B->info.d2h_bytes += (int64_t)n * R * sizeof(double);
     }
     double* ob = nullptr;
@@ -1086,8 +1146,13 @@ extern "C" int sgs_batch_simulate(sgs_batch* B, int32_t R, const double* z, uint
         const int64_t rchunk = std::max<int64_t>(1, std::min<int64_t>(R, ob_elems / std::max<int64_t>(1, n)));
         for (int64_t r0 = 0; r0 < R; r0 += rchunk) {
             const int rn = (int)std::min<int64_t>(rchunk, R - r0);
-            if (f64) BLAUNCH(B, launch_rows_to_out_fp64((const double*)V + n0 * Rp + r0, n, rn, Rp, B->mean[d], ob, st));
-            else BLAUNCH(B, launch_rows_to_out_fp32((const float*)V + n0 * Rp + r0, n, rn, Rp, B->mean[d], ob, st));
+            if (domain_fp64(B, d))
+                BLAUNCH(B, launch_rows_to_out_fp64((const double*)V + n0 * Rp + r0, n, rn, Rp, B->mean[d], ob, st));
+            else if (f64)
+                BLAUNCH(B, launch_rows_to_out_fp32((const float*)((const double*)V + n0 * Rp) + r0, n, rn, 2 * Rp,
+                                                   B->mean[d], ob, st));
+            else
+                BLAUNCH(B, launch_rows_to_out_fp32((const float*)V + n0 * Rp + r0, n, rn, Rp, B->mean[d], ob, st));
             BCK(B, cudaMemcpyAsync(out + R * n0 + r0 * n, ob, (size_t)n * rn * sizeof(double), cudaMemcpyDeviceToHost, st));
             B->info.d2h_bytes += (int64_t)n * rn * sizeof(double);
         }
@@ -1106,6 +1171,14 @@ extern "C" int sgs_batch_domain(const sgs_batch* B, int32_t d, int64_t* first, i
     if (d < 0 || d >= B->ndom) return berr(const_cast<sgs_batch*>(B), SGS_ERR_ARG, "domain out of range");
     if (first) *first = B->noff[d];
     if (nnodes) *nnodes = B->noff[d + 1] - B->noff[d];
+    return SGS_OK;
+}
+
+extern "C" int sgs_batch_domain_values_fp64(const sgs_batch* B, int32_t d, int32_t* fp64) {
+    if (!B) return berr(nullptr, SGS_ERR_ARG, "null batch");
+    if (!B->prepared) return berr(const_cast<sgs_batch*>(B), SGS_ERR_STATE, "values_fp64 before prepare");
+    if (d < 0 || d >= B->ndom || !fp64) return berr(const_cast<sgs_batch*>(B), SGS_ERR_ARG, "domain out of range");
+    *fp64 = domain_fp64(B, d) ? 1 : 0;
     return SGS_OK;
 }
 

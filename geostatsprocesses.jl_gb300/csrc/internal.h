@@ -161,6 +161,10 @@ struct FlowArgs {
                                  // launch; lets a captured graph take a new seed)
     int pairs;                   // FP64 values, packed tables: every 8-byte weight, b0
                                  // and sigma entry is an FP32 (hi, lo) pair
+    int64_t row_stride;          // values between consecutive nodes' rows (0: Rp)
+    const uint8_t* node_class;   // nullptr, or a class (0/1) per node: this launch
+    int cls;                     // sweeps only the nodes of class cls, and another
+                                 // launch the rest (their dependencies never cross)
 };
 
 struct SolveArgs {

@@ -541,8 +541,8 @@ __device__ __forceinline__ bool flow_wait(const int32_t* __restrict__ idx, int m
 // node, FP32 values with compensated sums.
 template <int G, bool CSR>
 __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int k, int64_t pos, int g, int m, int Rp,
-                                                int c0, int W, int lane, const float* __restrict__ z, uint64_t seed,
-                                                float* __restrict__ V) {
+                                                int64_t Rs, int c0, int W, int lane, const float* __restrict__ z,
+                                                uint64_t seed, float* __restrict__ V) {
     const int cpn = Rp >> 2;
     const int S = 32 / W, s = lane / W, cl = lane % W;
     const int64_t row = CSR ? t.off[pos] : pos * (int64_t)k;
@@ -555,7 +555,7 @@ __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int
         for (int q = 0; q < 4; ++q) a[gi][q].init(0.f, 0.f);
 #pragma unroll 4
     for (int j = s; j < m; j += S) {
-        const float4* row = reinterpret_cast<const float4*>(V + (int64_t)idx[j] * Rp);
+        const float4* row = reinterpret_cast<const float4*>(V + (int64_t)idx[j] * Rs);
         const float2 wj = w[j];
 #pragma unroll
         for (int gi = 0; gi < G; ++gi) {
@@ -584,14 +584,14 @@ __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int
             const int ch = c0 + cl + gi * W;
             if (ch < cpn) {
                 const float4 zz =
-                    z ? *reinterpret_cast<const float4*>(z + (int64_t)g * Rp + 4 * ch) : normals4(seed, g, ch);
+                    z ? *reinterpret_cast<const float4*>(z + (int64_t)g * Rs + 4 * ch) : normals4(seed, g, ch);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) dot2_merge(a[gi][q], b0.x, b0.y);
                 a[gi][0].add(sg.x, sg.y, zz.x);
                 a[gi][1].add(sg.x, sg.y, zz.y);
                 a[gi][2].add(sg.x, sg.y, zz.z);
                 a[gi][3].add(sg.x, sg.y, zz.w);
-                Vec4<float>::store(V + (int64_t)g * Rp + 4 * ch, make_float4(a[gi][0].value(), a[gi][1].value(),
+                Vec4<float>::store(V + (int64_t)g * Rs + 4 * ch, make_float4(a[gi][0].value(), a[gi][1].value(),
                                                                              a[gi][2].value(), a[gi][3].value()));
             }
         }
@@ -601,8 +601,8 @@ __device__ __forceinline__ void flow_piece_fp32(const SweepTables<float>& t, int
 // The same for FP64 values (plain FMA sums).
 template <int G, bool CSR>
 __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, int k, int64_t pos, int g, int m, int Rp,
-                                                int c0, int W, int lane, const double* __restrict__ z, uint64_t seed,
-                                                double* __restrict__ V, int pairs) {
+                                                int64_t Rs, int c0, int W, int lane, const double* __restrict__ z,
+                                                uint64_t seed, double* __restrict__ V, int pairs) {
     const int cpn = Rp >> 2;
     const int S = 32 / W, s = lane / W, cl = lane % W;
     const int64_t row = CSR ? t.off[pos] : pos * (int64_t)k;
@@ -621,7 +621,7 @@ __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, in
     for (int gi = 0; gi < G; ++gi) a[gi] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll 4
     for (int j = s; j < m; j += S) {
-        const double2* row = reinterpret_cast<const double2*>(V + (int64_t)idx[j] * Rp);
+        const double2* row = reinterpret_cast<const double2*>(V + (int64_t)idx[j] * Rs);
         const double wj = entry(w, j);
 #pragma unroll
         for (int gi = 0; gi < G; ++gi) {
@@ -652,7 +652,7 @@ __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, in
             if (ch < cpn) {
                 D4 zz;
                 if (z) {
-                    zz = load_d4(z + (int64_t)g * Rp + 4 * ch);
+                    zz = load_d4(z + (int64_t)g * Rs + 4 * ch);
                 } else {
                     const float4 f = normals4(seed, g, ch);
                     zz = {(double)f.x, (double)f.y, (double)f.z, (double)f.w};
@@ -662,7 +662,7 @@ __device__ __forceinline__ void flow_piece_fp64(const SweepTables<double>& t, in
                 r.y = fma(sg, zz.y, a[gi].y + b0);
                 r.z = fma(sg, zz.z, a[gi].z + b0);
                 r.w = fma(sg, zz.w, a[gi].w + b0);
-                store_d4(V + (int64_t)g * Rp + 4 * ch, r);
+                store_d4(V + (int64_t)g * Rs + 4 * ch, r);
             }
         }
     }
@@ -677,6 +677,7 @@ __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables
     const int lane = threadIdx.x & 31;
     const int64_t items = f.item1;
     const int P4 = W * G;
+    const int64_t Rs = f.row_stride ? f.row_stride : Rp;
     if (CSR && f.seed_dev) seed = *f.seed_dev;
     for (;;) {
         unsigned long long base = 0;
@@ -690,12 +691,15 @@ __global__ void __launch_bounds__(256, MINB) sweep_flow_kernel(const SweepTables
             const int64_t pos = it / f.H;
             const int q = (int)(it - pos * f.H);
             const int g = t.node[pos];
+            if (f.node_class && f.node_class[g] != f.cls) continue;  // the other launch's node
             const int m = t.m[pos];
             int32_t* done_q = f.done + (int64_t)q * f.N;
             const bool ok = flow_wait(t.idx + (CSR ? t.off[pos] : pos * (int64_t)k), m, done_q, f, lane);
             if (ok) {
-                if constexpr (sizeof(T) == 4) flow_piece_fp32<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V);
-                else flow_piece_fp64<G, CSR>(t, k, pos, g, m, Rp, q * P4, W, lane, z, seed, V, CSR ? f.pairs : 0);
+                if constexpr (sizeof(T) == 4)
+                    flow_piece_fp32<G, CSR>(t, k, pos, g, m, Rp, Rs, q * P4, W, lane, z, seed, V);
+                else
+                    flow_piece_fp64<G, CSR>(t, k, pos, g, m, Rp, Rs, q * P4, W, lane, z, seed, V, CSR ? f.pairs : 0);
             } else if (lane == 0) {
                 atomicExch(f.err, 1);
             }

@@ -158,7 +158,7 @@ class SgsBatchInfo(C.Structure):
         ("device_bytes", C.c_int64),
         ("weight_l1_max", C.c_double),
         ("values_fp64", C.c_int32),
-        ("reserved", C.c_int32),
+        ("domains_fp64", C.c_int32),
     ]
 
 
@@ -193,6 +193,7 @@ EXPORTS = (
     "sgs_batch_simulate",
     "sgs_batch_simulate_device",
     "sgs_batch_domain",
+    "sgs_batch_domain_values_fp64",
     "sgs_batch_neighbors",
     "sgs_batch_weights",
     "sgs_batch_set_sweep",
@@ -274,6 +275,8 @@ def _declare(lib):
     lib.sgs_batch_simulate_device.argtypes = [P, C.c_int32, C.c_uint64, P, P]
     lib.sgs_batch_simulate_device.restype = C.c_int
     lib.sgs_batch_domain.argtypes = [P, C.c_int32, i64p, i64p]
+    lib.sgs_batch_domain_values_fp64.argtypes = [P, C.c_int32, C.POINTER(C.c_int32)]
+    lib.sgs_batch_domain_values_fp64.restype = C.c_int
     lib.sgs_batch_domain.restype = C.c_int
     lib.sgs_batch_neighbors.argtypes = [P, C.c_int32, ip, ip]
     lib.sgs_batch_neighbors.restype = C.c_int

@@ -250,10 +250,19 @@ class Batch:
         """Whether the sweep keeps FP64 values (sgs_batch_info.values_fp64)."""
         return bool(self.info().values_fp64)
 
+    def domain_values_fp64(self, d: int) -> bool:
+        """Whether domain d keeps FP64 values (sgs_batch_domain_values_fp64):
+        the precision is chosen per domain from its weights."""
+        v = C.c_int32()
+        self._check(self.lib.sgs_batch_domain_values_fp64(self.h, d, C.byref(v)))
+        return bool(v.value)
+
     def simulate_device(self, nreals: int, seed: int, vals, stream: int | None = None):
         """Seeded sweep into device memory: a device pointer or a CUDA tensor
         of nnodes x (nreals rounded up to 4) values of the sweep's type
-        (values_fp64()); tensors are checked."""
+        (values_fp64()); tensors are checked.  With FP64 rows, the domains
+        that keep FP32 values (domain_values_fp64) hold their row's floats
+        in its first half."""
         ptr = _device_values(vals, self.nnodes, nreals, self.values_fp64())
         self._check(self.lib.sgs_batch_simulate_device(self.h, nreals, C.c_uint64(seed), C.c_void_p(ptr),
                                                        C.c_void_p(stream) if stream else None))

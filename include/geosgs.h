@@ -340,9 +340,14 @@ typedef struct sgs_batch_info {
     int64_t h2d_bytes, d2h_bytes;
     int64_t device_bytes;       /* device memory held by the batch                 */
     double  weight_l1_max;      /* as sgs_info: largest sum of |grid weights|       */
-    int32_t values_fp64;        /* 1: FP64 values (sgs_batch_simulate_device takes
-                                   double arrays), as sgs_info                      */
-    int32_t reserved;
+    int32_t values_fp64;        /* 1: the value array has FP64 rows (Rp doubles per
+                                   node; sgs_batch_simulate_device takes double
+                                   arrays); the rows of domains that keep FP32
+                                   values then hold Rp floats in their first half
+                                   (sgs_batch_domain_values_fp64)                  */
+    int32_t domains_fp64;       /* domains whose values are FP64: with
+                                   SGS_PREC_FP32_REFINE, only those whose weights
+                                   exceed SGS_FP32_VALUE_L1_LIMIT                   */
 } sgs_batch_info;
 
 /* Validate every problem (the first invalid one is named in the error) and
@@ -365,6 +370,12 @@ int sgs_batch_simulate(sgs_batch* batch, int32_t nreals, const double* z, uint64
 int sgs_batch_simulate_device(sgs_batch* batch, int32_t nreals, uint64_t seed, void* vals_dev, void* stream);
 /* First global node id and node count of domain d. */
 int sgs_batch_domain(const sgs_batch* batch, int32_t domain, int64_t* first, int64_t* nnodes);
+/* Value precision of domain d after prepare: *fp64 = 1 when its values are
+ * FP64 (SGS_PREC_FP64, or weights above SGS_FP32_VALUE_L1_LIMIT), 0 when they
+ * are FP32.  The precision is decided per domain, so one domain whose
+ * weights amplify rounding does not double the value traffic of the others.
+ * No counterpart in the reference (its values are always FP64). */
+int sgs_batch_domain_values_fp64(const sgs_batch* batch, int32_t d, int32_t* fp64);
 /* Neighbour rows of domain d, as sgs_plan_neighbors (N_d x maxneighbors_d,
  * local augmented ids: grid nodes 0..N_d-1, data N_d..). */
 int sgs_batch_neighbors(sgs_batch* batch, int32_t domain, int32_t* idx, int32_t* count);

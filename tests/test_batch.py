@@ -103,8 +103,10 @@ def test_batch_matches_oracle_per_domain(precision, oracle_mod, geosgs_lib):
 @pytest.mark.gpu
 def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
     """A domain whose kriging weights amplify FP32 rounding (a nugget-free
-    Gaussian variogram, sum |w| ~ 100) makes the batch keep FP64 values,
-    read through the packed tables; every domain stays within 1e-6."""
+    Gaussian variogram, sum |w| ~ 100) keeps FP64 values, read through the
+    packed tables, while the domains whose weights do not keep FP32 values
+    (the precision is chosen per domain); every domain stays within 1e-6,
+    and the device-resident values follow the documented mixed layout."""
     bw = workloads.c5_small("fp32", ndomains=5, seed=63)
     gau = geosgs.GaussianProcess(geosgs.GaussianVariogram(range=6.0, sill=1.0, nugget=0.0), 0.2)
     grid = geosgs.CartesianGrid((20, 20))
@@ -115,6 +117,8 @@ def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
     B = geosgs.Batch(probs).prepare()
     info = B.info()
     assert info.values_fp64 == 1 and info.weight_l1_max > 10.0
+    fp64 = [B.domain_values_fp64(d) for d in range(len(probs))]
+    assert fp64[-1] and not all(fp64) and info.domains_fp64 == sum(fp64)
     R = bw.nreals
     zs = [np.random.default_rng(200 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
     vals = B.simulate(R, z=zs)
@@ -125,6 +129,19 @@ def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
         assert rel_err(vals[d], O.simulate(R, zs[d])) <= VALUE_TOL, d
         f, n = int(B.first[d]), int(B.sizes[d])
         assert rel_err(seeded[d], O.simulate(R, zall[:, f:f + n])) <= VALUE_TOL, d
+    # device values: FP64 rows of Rp doubles per node, an FP32 domain's floats
+    # in the first half of each of its rows; centred (the mean subtracted)
+    torch = pytest.importorskip("torch")
+    Rp = (R + 3) // 4 * 4
+    V = torch.empty(B.nnodes * Rp, dtype=torch.float64, device="cuda")
+    B.simulate_device(R, 3, V)
+    torch.cuda.synchronize()
+    v64 = V.cpu().numpy().reshape(B.nnodes, Rp)
+    v32 = v64.view(np.float32).reshape(B.nnodes, 2 * Rp)
+    for d, (p, keep) in enumerate(probs):
+        f, n = int(B.first[d]), int(B.sizes[d])
+        rows = v64[f:f + n, :R] if fp64[d] else v32[f:f + n, :R].astype(np.float64)
+        np.testing.assert_allclose(rows.T + p.mean, seeded[d], rtol=0, atol=1e-12)
     B.close()
 
 
