@@ -89,6 +89,13 @@ struct sgs_plan {
     double ind_prob[IND_MAX_CAT] = {};
     int32_t* d_ind_cat = nullptr;
     double *d_ind_wsum = nullptr, *d_ind_dsum = nullptr;
+    // full simple cokriging of the indicators (sgs_plan_set_indicator_cokriging):
+    // coregionalization matrices per structure, per-position systems' outputs
+    bool cok = false;
+    double* d_cok_coef = nullptr;
+    double cok_tau = 0.0;
+    int32_t *d_cok_m = nullptr, *d_cok_idx = nullptr;
+    double *d_cok_w = nullptr, *d_cok_cst = nullptr;
     // FP32 refinement whose weights amplify the rounding of FP32 values: the
     // sweep keeps FP64 values, from FP64 copies of the (hi, lo) tables
     unsigned int* d_wl1 = nullptr;
@@ -766,6 +773,20 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     return SGS_OK;
 }
 
+static CokArgs cok_args(const sgs_plan* P) {
+    CokArgs c{};
+    c.ncat = P->ind_ncat;
+    for (int l = 0; l < IND_MAX_CAT; ++l) c.prob[l] = P->ind_prob[l];
+    c.coef = P->d_cok_coef;
+    c.data_cat = P->d_ind_cat;
+    c.tau = P->cok_tau;
+    c.m = P->d_cok_m;
+    c.idx = P->d_cok_idx;
+    c.w = P->d_cok_w;
+    c.cst = P->d_cok_cst;
+    return c;
+}
+
 extern "C" int sgs_plan_prepare(sgs_plan* P) {
     if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
     CK(P, cudaSetDevice(P->device));
@@ -922,6 +943,29 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
             }
             LAUNCH(P, 1, launch_tables_to_fp64(P->t32, P->t64p, N, N * (int64_t)k, st));
         }
+    }
+    if (P->cok) {
+        // cokriging systems of every position (they replace the nodes' status)
+        const int L = P->ind_ncat;
+        if (!P->d_cok_m) {
+            if ((rc = dalloc(P, &P->d_cok_m, N))) return rc;
+            if ((rc = dalloc(P, &P->d_cok_idx, (size_t)N * k))) return rc;
+            if ((rc = dalloc(P, &P->d_cok_w, (size_t)N * k * L * L))) return rc;
+            if ((rc = dalloc(P, &P->d_cok_cst, (size_t)N * L))) return rc;
+        }
+        SolveArgs s{};
+        s.grid = P->grid;
+        s.vario = P->vario;
+        s.k = P->k;
+        s.nmin = P->nmin;
+        s.P = P->N;
+        s.order = P->d_order;
+        s.nbr = P->d_nbr;
+        s.cnt = P->d_cnt;
+        s.N = P->N;
+        s.data_xyz = P->d_dxyz;
+        s.status = P->d_status;
+        LAUNCH(P, 1, launch_cok_solve(s, cok_args(P), st));
     }
     CK(P, cudaEventRecord(P->ev[4], st));
     CK(P, cudaStreamSynchronize(st));
@@ -1504,7 +1548,46 @@ extern "C" int sgs_plan_set_indicator(sgs_plan* P, int32_t ncat, const double* p
     CK(P, cudaStreamSynchronize(P->stream));
     P->ind_ncat = ncat;
     for (int l = 0; l < IND_MAX_CAT; ++l) P->ind_prob[l] = l < ncat ? prob[l] / s : 0.0;
+    P->cok = false;
     P->prepared = false;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_set_indicator_cokriging(sgs_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat,
+                                                const double* coef) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!coef) return set_err(P, SGS_ERR_ARG, "null coregionalization matrices");
+    if (ncat >= 2 && (int64_t)ncat * P->k > COK_MAX)
+        return set_err(P, SGS_ERR_ARG, "maxneighbors x categories must be at most 64 for cokriging");
+    const int S = P->vario.ns;
+    for (int i = 0; i < S * ncat * ncat && ncat >= 2 && ncat <= IND_MAX_CAT; ++i)
+        if (!std::isfinite(coef[i])) return set_err(P, SGS_ERR_ARG, "coregionalization matrices must be finite");
+    const int old_ncat = P->ind_ncat;
+    int rc = sgs_plan_set_indicator(P, ncat, prob, data_cat);
+    if (rc) return rc;
+    if (old_ncat != ncat) {  // table sizes change: reallocate at the next prepare
+        dfree(P, P->d_cok_m);
+        dfree(P, P->d_cok_idx);
+        dfree(P, P->d_cok_w);
+        dfree(P, P->d_cok_cst);
+        P->d_cok_m = P->d_cok_idx = nullptr;
+        P->d_cok_w = P->d_cok_cst = nullptr;
+    }
+    // the singular rule's scale: the largest indicator variance
+    double vmax = 0.0;
+    for (int a = 0; a < ncat; ++a) {
+        double v = 0.0;
+        for (int s = 0; s < S; ++s) v += coef[((size_t)s * ncat + a) * ncat + a] * P->vario.st[s].sill;
+        vmax = std::max(vmax, v);
+    }
+    if (!(vmax > 0.0)) return set_err(P, SGS_ERR_ARG, "the model's indicator variances must be positive");
+    dfree(P, P->d_cok_coef);
+    P->d_cok_coef = nullptr;
+    std::vector<double> cf(coef, coef + (size_t)S * ncat * ncat);
+    if ((rc = upload(P, &P->d_cok_coef, cf.data(), cf.size()))) return rc;
+    CK(P, cudaStreamSynchronize(P->stream));
+    P->cok_tau = kSingularTau * vmax;
+    P->cok = true;
     return SGS_OK;
 }
 
@@ -1545,7 +1628,8 @@ extern "C" int sgs_plan_simulate_indicator(sgs_plan* P, int32_t R, const double*
     CK(P, cudaEventRecord(P->ev[5], st));
     for (int l = 0; l < P->nlevels; ++l) {
         const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
-        cudaError_t e = P->precision == SGS_PREC_FP64
+        cudaError_t e = P->cok ? launch_cok_level(cok_args(P), P->d_order, P->k, p0, p1, Rp, ur, seed, C, st)
+                        : P->precision == SGS_PREC_FP64
                             ? launch_sis_level_fp64(P->t64, P->k, p0, p1, Rp, ia, ur, seed, C, st)
                             : launch_sis_level_fp32(P->t32, P->k, p0, p1, Rp, ia, ur, seed, C, st);
         if (e != cudaSuccess) {

@@ -23,6 +23,8 @@
 // Per-category sums are compensated FP32 sums of (hi, lo) weights (about
 // 1e-12), so the category decision equals an FP64 evaluation except at
 // exact ties.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace sgs {
@@ -151,6 +153,236 @@ cudaError_t launch_sis_level_fp32(const SweepTables<float>& t, int k, int64_t p0
 cudaError_t launch_sis_level_fp64(const SweepTables<double>& t, int k, int64_t p0, int64_t p1, int Rp,
                                   const IndArgs& ia, const double* u, uint64_t seed, uint8_t* C, cudaStream_t s) {
     return sis_level<double>(t, k, p0, p1, Rp, ia, u, seed, C, s);
+}
+
+// ---------------------------------------------------------------------------
+// Full simple cokriging (SIS with a non-separable indicator covariance, e.g.
+// structures of different ranges with their own coregionalization matrices):
+// the reference's Kriging(f, prob) with a multivariate f solves, per node,
+// one system over the n neighbours' L indicators (seqsim.jl:292-310).  LHS
+// (nL x nL) blocks C(x_i - x_j), right-hand sides (nL x L) blocks
+// C(x_i - x_0), C_ab(h) = sum_s coef[s][a][b] (sill_s - gamma_s(h)); FP64
+// Cholesky by one warp with the canonical singular rule; then
+//   p_t = prob_t + sum_i sum_a Lambda[(i, a), t] (I_a(x_i) - prob_a)
+//       = cst_t + sum_{grid nbrs j} w[j][cat_j][t],
+// the data's terms and every prob term folded into cst.
+constexpr int COK_WARPS = 2;
+
+__host__ __device__ constexpr size_t cok_smem_per_warp() {
+    return (size_t)COK_MAX * (COK_MAX + 1) * sizeof(double)  // LHS
+           + (size_t)COK_MAX * IND_MAX_CAT * sizeof(double)  // right-hand sides -> weights
+           + (size_t)COK_MAX * sizeof(double)                // one column being solved
+           + (size_t)KMAX * 4 * sizeof(int);                 // neighbour cells / data ids
+}
+
+__device__ __forceinline__ double structure_cov(const VarioStructDev& v, int dim, double h0, double h1, double h2) {
+    if (h0 == 0.0 && h1 == 0.0 && (dim == 2 || h2 == 0.0)) return v.sill;
+    return v.sill - structure_gamma(v, dim, h0, h1, h2);
+}
+
+// lag between two points of the augmented set (grid cells or data), as the
+// plain solve evaluates it
+__device__ __forceinline__ void cok_lag(const SolveArgs& a, const int* ca, const int* cb, double* h) {
+    const GridDev& G = a.grid;
+    if (ca[3] < 0 && cb[3] < 0) {
+        for (int j = 0; j < 3; ++j) h[j] = j < G.dim ? dmul((double)(cb[j] - ca[j]), G.spacing[j]) : 0.0;
+        return;
+    }
+    double xa[3], xb[3];
+    for (int j = 0; j < 3; ++j) {
+        xa[j] = ca[3] < 0 ? (j < G.dim ? centroid(G, j, ca[j]) : 0.0) : a.data_xyz[3 * (int64_t)ca[3] + j];
+        xb[j] = cb[3] < 0 ? (j < G.dim ? centroid(G, j, cb[j]) : 0.0) : a.data_xyz[3 * (int64_t)cb[3] + j];
+        h[j] = dsub(xb[j], xa[j]);
+    }
+}
+
+__global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveArgs a, const CokArgs c) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    unsigned char* base = smem + (size_t)wib * cok_smem_per_warp();
+    double* A = reinterpret_cast<double*>(base);
+    double* rhs = A + COK_MAX * (COK_MAX + 1);
+    double* col = rhs + COK_MAX * IND_MAX_CAT;
+    int* cell = reinterpret_cast<int*>(col + COK_MAX);  // [n][4]: c0, c1, c2, data id (-1: grid)
+    const GridDev& G = a.grid;
+    const int L = c.ncat, k = a.k, S = a.vario.ns;
+    const int nwarps = gridDim.x * COK_WARPS;
+    for (int64_t pos = (int64_t)blockIdx.x * COK_WARPS + wib; pos < a.P; pos += nwarps) {
+        const int g = a.order[pos];
+        const int n = a.cnt[g];
+        const int m = n * L, ld = m + 1;
+        int self[4];
+        cell_of(G, g, self[0], self[1], self[2]);
+        self[3] = -1;
+        bool kriged = n >= a.nmin;
+        if (kriged) {
+            for (int q = lane; q < n; q += 32) {
+                const int id = a.nbr[(int64_t)g * k + q];
+                int* cq = cell + 4 * q;
+                if (id < G.N) {
+                    cell_of(G, id, cq[0], cq[1], cq[2]);
+                    cq[3] = -1;
+                } else {
+                    cq[0] = cq[1] = cq[2] = 0;
+                    cq[3] = id - (int)G.N;
+                }
+            }
+            __syncwarp();
+            // lower triangle of the LHS, one neighbour pair (i >= j) per lane
+            for (int item = lane; item < n * (n + 1) / 2; item += 32) {
+                int i = (int)((sqrt(8.0 * item + 1.0) - 1.0) * 0.5);
+                while (i * (i + 1) / 2 > item) --i;
+                while ((i + 1) * (i + 2) / 2 <= item) ++i;
+                const int j = item - i * (i + 1) / 2;
+                double h[3], cs[SGS_MAX_STRUCTURES];
+                cok_lag(a, cell + 4 * j, cell + 4 * i, h);
+                for (int s = 0; s < S; ++s) cs[s] = structure_cov(a.vario.st[s], G.dim, h[0], h[1], h[2]);
+                for (int ai = 0; ai < L; ++ai)
+                    for (int b = 0; b < L; ++b) {
+                        const int r = i * L + ai, q = j * L + b;
+                        if (q > r) continue;
+                        double v = 0.0;
+                        for (int s = 0; s < S; ++s) v += c.coef[(s * L + ai) * L + b] * cs[s];
+                        A[r * ld + q] = v;
+                    }
+            }
+            for (int i = lane; i < n; i += 32) {
+                double h[3], cs[SGS_MAX_STRUCTURES];
+                cok_lag(a, self, cell + 4 * i, h);
+                for (int s = 0; s < S; ++s) cs[s] = structure_cov(a.vario.st[s], G.dim, h[0], h[1], h[2]);
+                for (int ai = 0; ai < L; ++ai)
+                    for (int t = 0; t < L; ++t) {
+                        double v = 0.0;
+                        for (int s = 0; s < S; ++s) v += c.coef[(s * L + ai) * L + t] * cs[s];
+                        rhs[(i * L + ai) * IND_MAX_CAT + t] = v;
+                    }
+            }
+            __syncwarp();
+            kriged = warp_cholesky<double>(A, ld, m, c.tau, lane);
+        }
+        if (kriged) {
+            for (int t = 0; t < L; ++t) {
+                for (int r = lane; r < m; r += 32) col[r] = rhs[r * IND_MAX_CAT + t];
+                __syncwarp();
+                warp_chol_solve<double>(A, ld, m, col, lane);
+                for (int r = lane; r < m; r += 32) rhs[r * IND_MAX_CAT + t] = col[r];  // Lambda[(i, a), t]
+                __syncwarp();
+            }
+        }
+        // outputs: grid neighbours compacted in neighbour order, prob and
+        // data terms folded into cst
+        int mg = 0;
+        double cst[IND_MAX_CAT];
+        for (int t = 0; t < IND_MAX_CAT; ++t) cst[t] = 0.0;
+        if (kriged) {
+            for (int b0 = 0; b0 < n; b0 += 32) {
+                const int i = b0 + lane;
+                const bool isgrid = i < n && cell[4 * i + 3] < 0;
+                const unsigned bal = __ballot_sync(FULL_MASK, isgrid);
+                if (i < n) {
+                    const int dcat = isgrid ? -1 : c.data_cat[cell[4 * i + 3]];
+                    for (int t = 0; t < L; ++t) {
+                        double v = 0.0;
+                        for (int ai = 0; ai < L; ++ai) {
+                            const double lam = rhs[(i * L + ai) * IND_MAX_CAT + t];
+                            v -= lam * c.prob[ai];
+                            if (ai == dcat) v += lam;
+                        }
+                        cst[t] += v;
+                    }
+                    if (isgrid) {
+                        const int jj = mg + __popc(bal & lanemask_lt());
+                        const int64_t e = pos * k + jj;
+                        c.idx[e] = a.nbr[(int64_t)g * k + i];
+                        for (int b = 0; b < L; ++b)
+                            for (int t = 0; t < L; ++t)
+                                c.w[(e * L + b) * L + t] = rhs[(i * L + b) * IND_MAX_CAT + t];
+                    }
+                }
+                mg += __popc(bal);
+            }
+        }
+        for (int t = 0; t < L; ++t) {
+            double v = cst[t];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+            if (lane == 0) c.cst[pos * L + t] = c.prob[t] + v;
+        }
+        if (lane == 0) {
+            c.m[pos] = mg;
+            a.status[g] = (int8_t)(n < a.nmin ? SGS_NODE_PRIOR_NMIN_ : (kriged ? SGS_NODE_KRIGED_ : SGS_NODE_PRIOR_SINGULAR_));
+        }
+        __syncwarp();
+    }
+}
+
+cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, cudaStream_t s) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const size_t smem = cok_smem_per_warp() * COK_WARPS;
+    cudaError_t e = cudaFuncSetAttribute(cok_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cok_solve_kernel, COK_WARPS * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t want = (a.P + COK_WARPS - 1) / COK_WARPS;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)nsm * per_sm));
+    cok_solve_kernel<<<blocks, COK_WARPS * 32, smem, s>>>(a, c);
+    return cudaGetLastError();
+}
+
+// One level: one thread per (position, 4 realizations).
+__global__ void __launch_bounds__(256) cok_level_kernel(const CokArgs c, const int32_t* __restrict__ node, int k,
+                                                        int64_t p0, int64_t p1, int Rp, const double* __restrict__ u,
+                                                        uint64_t seed, uint8_t* __restrict__ C) {
+    const int cpn = Rp >> 2, L = c.ncat;
+    IndArgs ia{};
+    ia.ncat = L;
+    for (int l = 0; l < IND_MAX_CAT; ++l) ia.prob[l] = c.prob[l];
+    const int64_t total = (p1 - p0) * cpn;
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = p0 + it / cpn;
+        const int ch = (int)(it % cpn);
+        const int g = node[pos];
+        const int m = c.m[pos];
+        double p[4][IND_MAX_CAT];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int t = 0; t < IND_MAX_CAT; ++t) p[r][t] = t < L ? c.cst[pos * L + t] : 0.0;
+        for (int j = 0; j < m; ++j) {
+            const int64_t e = pos * k + j;
+            const uint32_t cats = *reinterpret_cast<const uint32_t*>(C + (int64_t)c.idx[e] * Rp + 4 * ch);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int b = (int)((cats >> (8 * r)) & 0xffu);
+                const double* wr = c.w + (e * L + b) * L;
+#pragma unroll
+                for (int t = 0; t < IND_MAX_CAT; ++t)
+                    if (t < L) p[r][t] += wr[t];
+            }
+        }
+        const float4 uf = u ? make_float4(0.f, 0.f, 0.f, 0.f) : uniforms4(seed, g, ch);
+        const float ufa[4] = {uf.x, uf.y, uf.z, uf.w};
+        uint32_t out = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const double ur = u ? u[(int64_t)g * Rp + 4 * ch + r] : (double)ufa[r];
+            out |= (uint32_t)draw_category(ia, p[r], ur) << (8 * r);
+        }
+        *reinterpret_cast<uint32_t*>(C + (int64_t)g * Rp + 4 * ch) = out;
+    }
+}
+
+cudaError_t launch_cok_level(const CokArgs& c, const int32_t* node, int k, int64_t p0, int64_t p1, int Rp,
+                             const double* u, uint64_t seed, uint8_t* C, cudaStream_t s) {
+    if (p1 <= p0) return cudaSuccess;
+    int64_t blocks = ((p1 - p0) * (Rp / 4) + 255) / 256;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    cok_level_kernel<<<(int)blocks, 256, 0, s>>>(c, node, k, p0, p1, Rp, u, seed, C);
+    return cudaGetLastError();
 }
 
 // node-major category bytes [N][Rp] -> realization-major int32 [R][N]

@@ -220,6 +220,27 @@ cudaError_t launch_sis_level_fp64(const SweepTables<double>& t, int k, int64_t p
                                   const IndArgs& ia, const double* u, uint64_t seed, uint8_t* C, cudaStream_t s);
 cudaError_t launch_cats_to_out(const uint8_t* C, int64_t N, int R, int Rp, int32_t* out, cudaStream_t s);
 
+// Full simple cokriging of the indicators (indicator.cu) for a linear model
+// of coregionalization C_ab(h) = sum_s coef[s][a][b] C_s(h) over the
+// structures of the plan's variogram.  Unknowns per system: n x L <= COK_MAX.
+constexpr int COK_MAX = 64;
+struct CokArgs {
+    int ncat;                    // L
+    double prob[IND_MAX_CAT];    // prior probabilities (normalized)
+    const double* coef;          // [S][L][L]
+    const int32_t* data_cat;     // [D] data categories
+    double tau;                  // singular pivot threshold (absolute)
+    int32_t* m;                  // [P] grid neighbours of the position's system
+    int32_t* idx;                // [P][k] their node ids
+    double* w;                   // [P][k][L][L] weight of (grid neighbour j, its category b) for category t
+    double* cst;                 // [P][L] prior term and the data's contribution
+};
+// systems of every position (a: geometry, neighbours, order, status; the
+// status of each node is overwritten with its cokriging status)
+cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, cudaStream_t s);
+cudaError_t launch_cok_level(const CokArgs& c, const int32_t* node, int k, int64_t p0, int64_t p1, int Rp,
+                             const double* u, uint64_t seed, uint8_t* C, cudaStream_t s);
+
 // Host-side description of one problem (api.cu: host_domain): everything
 // sgs_plan_create derives on the host before uploading.
 struct HostDomain {

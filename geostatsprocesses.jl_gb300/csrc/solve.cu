@@ -82,47 +82,6 @@ __device__ __forceinline__ int collect_data(const NbInfo* info, int n, int* dl, 
     return nd;
 }
 
-// Right-looking Cholesky of the lower triangle of A (leading dimension ld)
-// by one warp.  Fails (returns false) when a pivot is not > tau.
-template <typename T>
-__device__ bool warp_cholesky(T* A, int ld, int n, T tau, int lane) {
-    for (int j = 0; j < n; ++j) {
-        const T d = A[j * ld + j];
-        if (!(d > tau)) return false;
-        const T ljj = sqrt(d);
-        const T inv = T(1) / ljj;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) A[i * ld + j] *= inv;
-        if (lane == 0) A[j * ld + j] = ljj;
-        __syncwarp();
-        for (int i = j + 1 + lane; i < n; i += 32) {
-            const T lij = A[i * ld + j];
-            for (int l = j + 1; l <= i; ++l) A[i * ld + l] -= lij * A[l * ld + j];
-        }
-        __syncwarp();
-    }
-    return true;
-}
-
-// Solve L L^T x = b in place (x overwrites b), L from warp_cholesky.
-template <typename T>
-__device__ void warp_chol_solve(const T* A, int ld, int n, T* b, int lane) {
-    for (int j = 0; j < n; ++j) {
-        const T yj = b[j] / A[j * ld + j];
-        __syncwarp();
-        if (lane == 0) b[j] = yj;
-        for (int i = j + 1 + lane; i < n; i += 32) b[i] -= A[i * ld + j] * yj;
-        __syncwarp();
-    }
-    for (int j = n - 1; j >= 0; --j) {
-        const T wj = b[j] / A[j * ld + j];
-        __syncwarp();
-        if (lane == 0) b[j] = wj;
-        for (int i = lane; i < j; i += 32) b[i] -= A[j * ld + i] * wj;
-        __syncwarp();
-    }
-}
-
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);

@@ -18,6 +18,7 @@ from .model import (
     ExponentialTransiogram,
     GaussianTransiogram,
     IndicatorProcess,
+    LinearCoregionalization,
     LinearPath,
     MetricBall,
     NestedVariogram,
@@ -38,7 +39,7 @@ __all__ = [
     "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "ExponentialTransiogram", "GaussianTransiogram", "IndicatorProcess", "SphericalTransiogram",
-    "LinearPath", "MetricBall", "NestedVariogram", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
+    "LinearCoregionalization", "LinearPath", "MetricBall", "NestedVariogram", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
     "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
     "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

@@ -203,6 +203,7 @@ EXPORTS = (
     "sgs_batch_last_error",
     "sgs_krige",
     "sgs_plan_set_indicator",
+    "sgs_plan_set_indicator_cokriging",
     "sgs_plan_simulate_indicator",
     "sgs_ensemble_stats",
     "sgs_ensemble_cdf",
@@ -295,6 +296,8 @@ def _declare(lib):
     lib.sgs_batch_last_error.restype = C.c_char_p
     lib.sgs_plan_set_indicator.argtypes = [P, C.c_int32, dp, ip]
     lib.sgs_plan_set_indicator.restype = C.c_int
+    lib.sgs_plan_set_indicator_cokriging.argtypes = [P, C.c_int32, dp, ip, dp]
+    lib.sgs_plan_set_indicator_cokriging.restype = C.c_int
     lib.sgs_plan_simulate_indicator.argtypes = [P, C.c_int32, dp, C.c_uint64, ip]
     lib.sgs_plan_simulate_indicator.restype = C.c_int
     lib.sgs_krige.argtypes = [C.POINTER(SgsProblem), dp, dp]

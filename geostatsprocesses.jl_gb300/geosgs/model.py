@@ -247,6 +247,44 @@ class GaussianTransiogram(_Transiogram):
     SHAPE = GaussianVariogram
 
 
+class LinearCoregionalization:
+    """A multivariate covariance C_ab(h) = sum_s A_s[a][b] C_s(h) (a linear model
+    of coregionalization): symmetric positive semi-definite L x L matrices A_s
+    times the covariances C_s = sill_s - gamma_s of variogram structures
+    (GeoStatsFunctions writes it `A1 * Covariance1 + A2 * Covariance2`).  As an
+    IndicatorProcess function it gives the categories' indicator
+    cross-covariances; with structures of different ranges it is not
+    separable, and the GPU path solves full simple cokriging systems."""
+
+    def __init__(self, terms):
+        terms = list(terms)
+        if not 1 <= len(terms) <= _abi.SGS_MAX_STRUCTURES:
+            raise ArgumentError("1 to %d structures" % _abi.SGS_MAX_STRUCTURES)
+        mats, sts = [], []
+        for A, g in terms:
+            A = np.asarray(A, dtype=np.float64)
+            if not isinstance(g, _Variogram) or isinstance(g, NestedVariogram):
+                raise ArgumentError("each term is a matrix times one variogram structure")
+            if A.ndim != 2 or A.shape[0] != A.shape[1] or A.shape[0] < 2 or not np.allclose(A, A.T):
+                raise ArgumentError("coefficients must be symmetric L x L matrices, L >= 2")
+            mats.append(A)
+            sts.append(g)
+        L = mats[0].shape[0]
+        if any(A.shape[0] != L for A in mats):
+            raise ArgumentError("all coefficient matrices must have the same size")
+        if L > _abi.SGS_IND_MAX_CATEGORIES:
+            raise ArgumentError("at most %d categories on the GPU" % _abi.SGS_IND_MAX_CATEGORIES)
+        self.coef = np.ascontiguousarray(np.stack(mats))
+        self.nested = NestedVariogram(sts) if len(sts) > 1 else sts[0]
+        self.nvariables = L
+
+    def structures(self) -> list:
+        return self.nested.structures()
+
+    def range(self) -> float:
+        return self.nested.range()
+
+
 class IndicatorProcess:
     """IndicatorProcess(func, prob) — src/processes/field/indicator.jl:5-45.
 
@@ -259,12 +297,19 @@ class IndicatorProcess:
         if isinstance(func, _Transiogram):
             corr = func.shape
             prob = func.proportions if prob is None else prob
+        elif isinstance(func, LinearCoregionalization):
+            corr = func.nested
+            if prob is None:
+                raise ArgumentError("an indicator process on a coregionalization model needs its probabilities")
+            if len(prob) != func.nvariables:
+                raise ArgumentError(f"probabilities must have {func.nvariables} components, received {len(prob)}")
         elif isinstance(func, _Variogram):
             corr = func
             if prob is None:
                 raise ArgumentError("an indicator process on a variogram needs its probabilities")
         else:
-            raise ArgumentError("IndicatorProcess on the GPU path takes a transiogram or a variogram")
+            raise ArgumentError("IndicatorProcess on the GPU path takes a transiogram, a variogram or a "
+                                "linear model of coregionalization")
         p = np.asarray(prob, dtype=np.float64)
         if p.ndim != 1 or len(p) < 2 or np.any(p < 0) or np.any(p > 1) or not p.sum() > 0:
             raise ArgumentError("probabilities must be in [0, 1], at least two of them")

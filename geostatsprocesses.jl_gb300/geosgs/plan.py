@@ -116,6 +116,19 @@ class Plan:
         self.prepared = False
         return self
 
+    def set_indicator_cokriging(self, prob, coef, data_cat=None):
+        """Indicator simulation by full simple cokriging: prior probabilities,
+        the coregionalization matrices (S x L x L, one per structure of the
+        plan's variogram) and the data's category indices; call before
+        prepare()."""
+        prob = np.ascontiguousarray(np.asarray(prob, dtype=np.float64))
+        coef = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+        dc = np.ascontiguousarray(np.asarray(data_cat if data_cat is not None else np.zeros(1), dtype=np.int32))
+        self._ind = (prob, dc, coef)
+        self._check(self.lib.sgs_plan_set_indicator_cokriging(self.h, len(prob), _dp(prob), _ip(dc), _dp(coef)))
+        self.prepared = False
+        return self
+
     def simulate_indicator(self, nreals: int, u=None, seed: int = 0) -> np.ndarray:
         """nreals x N realization-major category indices (int32)."""
         out = np.empty((nreals, self.N), dtype=np.int32)

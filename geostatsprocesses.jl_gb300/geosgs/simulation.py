@@ -31,6 +31,7 @@ import numpy as np
 
 from . import _abi
 from .model import (ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess, GeoTable, IndicatorProcess,
+                    LinearCoregionalization,
                     LinearPath, RandomPath)
 from .plan import Batch, Plan
 from .problem import build_problem, indicator_levels
@@ -120,7 +121,12 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
             raise ArgumentError("per-realization paths are available for GaussianProcess")
         levels, dcat = indicator_levels(process, data)
         problem, keep = build_problem(process, domain, data, method)
-        plan = Plan(problem, keep).set_indicator(process.prob, dcat).prepare()
+        plan = Plan(problem, keep)
+        if isinstance(process.func, LinearCoregionalization):  # full simple cokriging
+            plan.set_indicator_cokriging(process.prob, process.func.coef, dcat)
+        else:
+            plan.set_indicator(process.prob, dcat)
+        plan.prepare()
         pre = _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
         pre.levels = levels
         return pre

@@ -394,6 +394,21 @@ void sgs_batch_destroy(sgs_batch* batch);
  * sgs_batch_create on this thread when batch is NULL. */
 const char* sgs_batch_last_error(const sgs_batch* batch);
 
+/* Indicator simulation with full simple cokriging, for an indicator
+ * covariance given as a linear model of coregionalization:
+ * C_ab(h) = sum_s coef[s][a][b] C_s(h), C_s = sill_s - gamma_s over the
+ * S = 1 + nstructures structures of the plan's variogram (coef: S x ncat x
+ * ncat, row-major, symmetric).  Replaces Kriging(func, prob) with a
+ * multivariate func in the indicator branches of SEQSIM
+ * (src/simulation/field/seqsim.jl:292-310; IndicatorProcess(func, prob),
+ * src/processes/field/indicator.jl:30-47), where the structures' ranges
+ * differ and every category's weights are not those of one correlogram.
+ * Each node solves one (n ncat x n ncat) system in FP64: maxneighbors x
+ * ncat must be at most 64.  prob, data_cat and the draws as
+ * sgs_plan_set_indicator / sgs_plan_simulate_indicator; prepare again after
+ * setting it. */
+int sgs_plan_set_indicator_cokriging(sgs_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat,
+                                     const double* coef);
 /* ---- sequential indicator simulation ------------------------------------
  * An IndicatorProcess(func, prob) simulated with SEQSIM
  * (src/processes/field/indicator.jl, src/simulation/field/seqsim.jl:247-261

@@ -47,6 +47,7 @@ def load():
     lib.oracle_simulate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp, C.c_int64, C.c_int]
     lib.oracle_krige.argtypes = [P, dp, dp, C.c_int]
     lib.oracle_simulate_indicator.argtypes = [P, C.c_int32, dp, ip, C.c_int32, dp, C.c_uint64, ip, C.c_int]
+    lib.oracle_simulate_cokriging.argtypes = [P, C.c_int32, dp, ip, dp, C.c_int32, dp, C.c_uint64, ip, C.c_int]
     lib.oracle_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_int32, dp]
     lib.oracle_uniforms.restype = None
     lib.oracle_neighbors.argtypes = [P, ip, ip]
@@ -135,6 +136,21 @@ class OraclePlan:
             up = _dp(u)
         self._rc(self.lib.oracle_simulate_indicator(self.h, len(prob), _dp(prob), _ip(dc), nreals, up, seed,
                                                     _ip(out), nthreads))
+        return out
+
+    def simulate_cokriging(self, nreals, prob, coef, data_cat=None, u=None, seed=0, nthreads=0):
+        """nreals x N categories by full simple cokriging of the indicators
+        (linear model of coregionalization, coef: S x L x L)."""
+        prob = np.ascontiguousarray(np.asarray(prob, dtype=np.float64))
+        coef = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+        dc = np.ascontiguousarray(np.asarray(data_cat if data_cat is not None else np.zeros(1), dtype=np.int32))
+        out = np.empty((nreals, self.N), dtype=np.int32)
+        up = None
+        if u is not None:
+            u = np.ascontiguousarray(u, dtype=np.float64).reshape(nreals, self.N)
+            up = _dp(u)
+        self._rc(self.lib.oracle_simulate_cokriging(self.h, len(prob), _dp(prob), _ip(dc), _dp(coef), nreals, up,
+                                                    seed, _ip(out), nthreads))
         return out
 
     def neighbors(self):

@@ -770,6 +770,175 @@ extern "C" int oracle_simulate_indicator(oracle_plan* P, int32_t ncat, const dou
     return SGS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Sequential indicator simulation with full simple cokriging, for an
+// indicator covariance given as a linear model of coregionalization
+//   C_ab(h) = sum_s A_s[a][b] C_s(h),   C_s = sill_s - gamma_s (structure s)
+// with the structures of the plan's (nested) variogram and symmetric L x L
+// coefficient matrices A_s (coef: S x L x L, row-major).  With structures of
+// different ranges the model is not separable, and every node solves the
+// simple cokriging system of its n neighbours' L indicators (seqsim.jl:292-310,
+// Kriging(f, prob) with a multivariate f): the (nL x nL) LHS has the blocks
+// C(x_i - x_j), the L right-hand sides the blocks C(x_i - x_0); Cholesky with
+// the canonical singular rule (a pivot not > 1e-10 x the largest variance
+// sum_s A_s[a][a] sill_s); weights Lambda[(i, a), t] give
+//   p_t = prob_t + sum_i sum_a Lambda[(i, a), t] (I_a(x_i) - prob_a),
+// clamped to [0, 1], normalized and drawn from by the inverse cdf at u.
+static double structure_cov(const oracle_plan* P, size_t s, const double* h) {
+    bool zero = true;
+    for (int j = 0; j < P->dim; ++j) zero = zero && (h[j] == 0.0);
+    const sgs_variogram& v = P->vs[s];
+    if (zero) return v.sill;
+    const double hn = std::sqrt(P->vms[s].d2(h));
+    double f;
+    switch (v.type) {
+        case SGS_SPHERICAL: f = hn < 1.0 ? 1.5 * hn - 0.5 * hn * hn * hn : 1.0; break;
+        case SGS_EXPONENTIAL: f = 1.0 - std::exp(-3.0 * hn); break;
+        default: f = 1.0 - std::exp(-3.0 * hn * hn); break;
+    }
+    return v.sill - (v.nugget + (v.sill - v.nugget) * f);
+}
+
+extern "C" int oracle_simulate_cokriging(oracle_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat,
+                                         const double* coef, int32_t R, const double* u, uint64_t seed, int32_t* out,
+                                         int nthreads) {
+    if (!P || !out || R < 0 || ncat < 2 || ncat > 8 || !prob || !coef) return fail(SGS_ERR_ARG, "invalid argument");
+    const int L = ncat, k = P->nmax, S = (int)P->vs.size();
+    if (k * L > 64) return fail(SGS_ERR_ARG, "maxneighbors x categories above 64");
+    double ps = 0.0;
+    for (int l = 0; l < L; ++l) ps += prob[l];
+    std::vector<double> pr(L);
+    for (int l = 0; l < L; ++l) pr[l] = prob[l] / ps;
+    double vmax = 0.0;  // largest variance of an indicator
+    for (int a = 0; a < L; ++a) {
+        double v = 0.0;
+        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + a] * P->vs[s].sill;
+        vmax = std::max(vmax, v);
+    }
+    const double tau = kSingularTau * vmax;
+    // per node: status and Lambda (k*L x L), realization-independent
+    std::vector<int8_t> st(P->N, (int8_t)SGS_NODE_PRIOR_NMIN);
+    std::vector<double> lam((size_t)P->N * k * L * L, 0.0);
+    const int nt = nthreads_or_all(nthreads);
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<double> K, c, cs(S);
+        double h[3];
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t g = 0; g < P->N; ++g) {
+            const int n = P->cnt[g];
+            if (n < P->nmin) continue;
+            const int m = n * L;
+            const int32_t* nb = &P->nbr[(size_t)g * k];
+            K.assign((size_t)m * m, 0.0);
+            c.assign((size_t)m * L, 0.0);
+            for (int i = 0; i < n; ++i) {
+                P->lag(g, nb[i], h);
+                for (int s = 0; s < S; ++s) cs[s] = structure_cov(P, s, h);
+                for (int a = 0; a < L; ++a)
+                    for (int t = 0; t < L; ++t) {
+                        double v = 0.0;
+                        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + t] * cs[s];
+                        c[(size_t)(i * L + a) * L + t] = v;
+                    }
+                for (int j = 0; j <= i; ++j) {
+                    P->lag(nb[j], nb[i], h);
+                    for (int s = 0; s < S; ++s) cs[s] = structure_cov(P, s, h);
+                    for (int a = 0; a < L; ++a)
+                        for (int b = 0; b < L; ++b) {
+                            const int r = i * L + a, q = j * L + b;
+                            if (q > r) continue;
+                            double v = 0.0;
+                            for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + b] * cs[s];
+                            K[(size_t)r * m + q] = v;
+                        }
+                }
+            }
+            bool ok = true;
+            for (int j = 0; j < m && ok; ++j) {
+                double sj = K[(size_t)j * m + j];
+                for (int l = 0; l < j; ++l) sj -= K[(size_t)j * m + l] * K[(size_t)j * m + l];
+                if (!(sj > tau)) {
+                    ok = false;
+                    break;
+                }
+                const double ljj = std::sqrt(sj);
+                K[(size_t)j * m + j] = ljj;
+                for (int i = j + 1; i < m; ++i) {
+                    double t = K[(size_t)i * m + j];
+                    for (int l = 0; l < j; ++l) t -= K[(size_t)i * m + l] * K[(size_t)j * m + l];
+                    K[(size_t)i * m + j] = t / ljj;
+                }
+            }
+            if (!ok) {
+                st[g] = (int8_t)SGS_NODE_PRIOR_SINGULAR;
+                continue;
+            }
+            double* lg = &lam[(size_t)g * k * L * L];
+            std::vector<double> y(m);
+            for (int t = 0; t < L; ++t) {
+                for (int i = 0; i < m; ++i) {
+                    double v = c[(size_t)i * L + t];
+                    for (int l = 0; l < i; ++l) v -= K[(size_t)i * m + l] * y[l];
+                    y[i] = v / K[(size_t)i * m + i];
+                }
+                for (int i = m - 1; i >= 0; --i) {
+                    double v = y[i];
+                    for (int l = i + 1; l < m; ++l) v -= K[(size_t)l * m + i] * lg[(size_t)l * L + t];
+                    lg[(size_t)i * L + t] = v / K[(size_t)i * m + i];
+                }
+            }
+            st[g] = (int8_t)SGS_NODE_KRIGED;
+        }
+    }
+    for (int64_t g = 0; g < P->N; ++g) P->status[g] = st[g];
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<int32_t> cat(P->N + P->D);
+        std::vector<double> p(L);
+#pragma omp for schedule(dynamic, 1)
+        for (int32_t r = 0; r < R; ++r) {
+            std::fill(cat.begin(), cat.end(), -1);
+            for (int64_t i = 0; i < P->D; ++i) cat[P->N + i] = data_cat[i];  // ExplicitInit
+            for (int64_t t = 0; t < P->N; ++t) {
+                const int64_t g = P->path[t];
+                for (int l = 0; l < L; ++l) p[l] = pr[l];
+                if (st[g] == SGS_NODE_KRIGED) {
+                    const int32_t* nb = &P->nbr[(size_t)g * k];
+                    const double* lg = &lam[(size_t)g * k * L * L];
+                    for (int i = 0; i < P->cnt[g]; ++i)
+                        for (int a = 0; a < L; ++a) {
+                            const double ind = (cat[nb[i]] == a ? 1.0 : 0.0) - pr[a];
+                            for (int l = 0; l < L; ++l) p[l] += lg[(size_t)(i * L + a) * L + l] * ind;
+                        }
+                }
+                double tot = 0.0;
+                for (int l = 0; l < L; ++l) {
+                    p[l] = std::min(std::max(p[l], 0.0), 1.0);
+                    tot += p[l];
+                }
+                if (!(tot > 0.0)) {
+                    for (int l = 0; l < L; ++l) p[l] = pr[l];
+                    tot = 1.0;
+                }
+                const double uu = u ? u[(size_t)r * P->N + g] : uniform_of(seed, g, r);
+                int cc = L - 1;
+                double cum = 0.0;
+                for (int l = 0; l < L - 1; ++l) {
+                    cum += p[l] / tot;
+                    if (uu < cum) {
+                        cc = l;
+                        break;
+                    }
+                }
+                cat[g] = cc;
+            }
+            for (int64_t g = 0; g < P->N; ++g) out[(size_t)r * P->N + g] = cat[g];
+        }
+    }
+    return SGS_OK;
+}
+
 extern "C" int oracle_neighbors(const oracle_plan* P, int32_t* idx, int32_t* count) {
     if (!P) return fail(SGS_ERR_ARG, "null plan");
     if (idx) std::memcpy(idx, P->nbr.data(), P->nbr.size() * sizeof(int32_t));

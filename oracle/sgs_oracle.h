@@ -59,6 +59,14 @@ int oracle_simulate(oracle_plan* plan, int32_t nreals, const double* z, uint64_t
  * uniforms or NULL (oracle_uniforms of seed); out: nreals x N categories. */
 int oracle_simulate_indicator(oracle_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat,
                               int32_t nreals, const double* u, uint64_t seed, int32_t* out, int nthreads);
+/* Sequential indicator simulation with full simple cokriging for an
+ * indicator covariance that is a linear model of coregionalization:
+ * C_ab(h) = sum_s coef[s][a][b] C_s(h) over the structures of the plan's
+ * (nested) variogram; coef: S x ncat x ncat row-major, S = 1 + nstructures.
+ * Requires maxneighbors x ncat <= 64.  Node status is left in the plan. */
+int oracle_simulate_cokriging(oracle_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat,
+                              const double* coef, int32_t nreals, const double* u, uint64_t seed, int32_t* out,
+                              int nthreads);
 /* Uniforms of the seeded indicator draws: u[r*nnodes + g]. */
 void oracle_uniforms(uint64_t seed, int64_t nnodes, int32_t nreals, double* u);
 

@@ -104,3 +104,114 @@ def test_rand_indicator_api(geosgs_lib):
     proc3 = geosgs.IndicatorProcess(geosgs.SphericalTransiogram(range=35.0, proportions=(0.7, 0.2, 0.1)))
     ens = geosgs.rand(rng, proc3, grid, 3, data=data, method=method)
     assert len(ens) == 3 and set(ens[0]["C"].tolist()) == {"a", "b", "c"}
+
+
+# ---- full simple cokriging: linear models of coregionalization ----
+def lmc_model(L=3):
+    """A non-separable indicator covariance: a short spherical structure and a
+    longer anisotropic exponential one with different coregionalization
+    matrices (symmetric positive definite)."""
+    A1 = np.array([[0.20, -0.08, -0.05], [-0.08, 0.15, -0.03], [-0.05, -0.03, 0.10]])[:L, :L]
+    A2 = np.array([[0.05, -0.02, 0.01], [-0.02, 0.06, -0.01], [0.01, -0.01, 0.04]])[:L, :L]
+    return geosgs.LinearCoregionalization([
+        (A1, geosgs.SphericalVariogram(range=6.0)),
+        (A2, geosgs.ExponentialVariogram(ranges=(14.0, 7.0, 4.0), rotation=geosgs.RotZ(25.0))),
+    ])
+
+
+def test_oracle_cokriging_reduces_to_the_separable_path(oracle_mod):
+    """With one structure, C_ab(h) = A_ab C(h) with A nonsingular, simple
+    cokriging gives every category the simple kriging weights of C: the
+    cokriging restatement draws the same categories as the separable one
+    from the same uniforms."""
+    grid = geosgs.CartesianGrid((24, 20))
+    A = np.array([[1.0, 0.4, 0.1], [0.4, 0.8, 0.2], [0.1, 0.2, 0.6]])
+    g = geosgs.ExponentialVariogram(range=7.0)
+    prob = (0.5, 0.3, 0.2)
+    rng = np.random.default_rng(4)
+    data = geosgs.georef({"C": np.array([0, 2, 1, 1])}, rng.uniform(0.0, 1.0, (4, 2)) * [24.0, 20.0])
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(8), maxneighbors=10)
+    sep = geosgs.IndicatorProcess(g, prob=prob)
+    cok = geosgs.IndicatorProcess(geosgs.LinearCoregionalization([(A, g)]), prob=prob)
+    p, keep = geosgs.build_problem(cok, grid, data, method)
+    _, dcat = gproblem.indicator_levels(cok, data)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    u = rng.uniform(0.0, 1.0, (6, O.N))
+    np.testing.assert_array_equal(O.simulate_cokriging(6, prob, cok.func.coef, dcat, u=u),
+                                  O.simulate_indicator(6, sep.prob, dcat, u=u))
+
+
+def test_oracle_cokriging_proportions(oracle_mod):
+    """An unconditional simulation with a non-separable model reproduces the
+    prior proportions on average over realizations."""
+    grid = geosgs.CartesianGrid((40, 40))
+    prob = (0.5, 0.3, 0.2)
+    proc = geosgs.IndicatorProcess(lmc_model(3), prob=prob)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(2), maxneighbors=12)
+    p, keep = geosgs.build_problem(proc, grid, None, method)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    cats = O.simulate_cokriging(60, prob, proc.func.coef, seed=3)
+    frac = np.bincount(cats.ravel(), minlength=3) / cats.size
+    assert np.abs(frac - np.array(prob)).max() < 0.04, frac
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gpu_cokriging_matches_oracle(dim, oracle_mod, geosgs_lib):
+    """Full simple cokriging with a non-separable model (two structures of
+    different ranges and anisotropy, each with its own coregionalization
+    matrix), with data of every category: node status identical and the
+    categories equal to the oracle's, for given and for seeded uniforms.  A
+    one-structure model run through the cokriging path also equals the
+    separable path."""
+    L = 3
+    prob = (0.5, 0.3, 0.2)
+    if dim == 2:
+        grid = geosgs.CartesianGrid((36, 30))
+        k = 12
+    else:
+        grid = geosgs.CartesianGrid((18, 16, 8))
+        k = 16
+    rng = np.random.default_rng(20 + dim)
+    npts = 40
+    xy = rng.uniform(0.0, 1.0, (npts, dim)) * np.asarray(grid.dims, dtype=float)
+    labels = rng.integers(0, L, npts)
+    labels[:L] = np.arange(L)
+    data = geosgs.georef({"C": labels}, xy)
+    proc = geosgs.IndicatorProcess(lmc_model(L), prob=prob)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(4), maxneighbors=k, precision="fp64")
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    _, dcat = gproblem.indicator_levels(proc, data)
+    G = geosgs.Plan(p, keep).set_indicator_cokriging(proc.prob, proc.func.coef, dcat).prepare()
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    R = 8
+    u = rng.uniform(0.0, 1.0, (R, G.N))
+    got = G.simulate_indicator(R, u=u)
+    want = O.simulate_cokriging(R, proc.prob, proc.func.coef, dcat, u=u)
+    np.testing.assert_array_equal(G.weights()[2], O.weights()[2])  # cokriging status of every node
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(G.simulate_indicator(R, seed=5),
+                                  O.simulate_cokriging(R, proc.prob, proc.func.coef, dcat, seed=5))
+    G.close()
+    # one structure: the cokriging path equals the separable path
+    A = np.array([[1.0, 0.4, 0.1], [0.4, 0.8, 0.2], [0.1, 0.2, 0.6]])
+    g1 = geosgs.ExponentialVariogram(range=7.0)
+    cok1 = geosgs.IndicatorProcess(geosgs.LinearCoregionalization([(A, g1)]), prob=prob)
+    p, keep = geosgs.build_problem(cok1, grid, data, method)
+    Gc = geosgs.Plan(p, keep).set_indicator_cokriging(prob, cok1.func.coef, dcat).prepare()
+    Gs = geosgs.Plan(p, keep).set_indicator(prob, dcat).prepare()
+    np.testing.assert_array_equal(Gc.simulate_indicator(R, u=u), Gs.simulate_indicator(R, u=u))
+    Gc.close()
+    Gs.close()
+
+
+@pytest.mark.gpu
+def test_rand_cokriging_api(geosgs_lib):
+    """rand with an IndicatorProcess on a linear model of coregionalization
+    runs the cokriging path and returns the data's labels."""
+    grid = geosgs.CartesianGrid((40, 40))
+    data = geosgs.georef({"C": np.array(["a", "b", "c"])}, np.array([[5.5, 5.5], [20.5, 30.5], [30.5, 10.5]]))
+    proc = geosgs.IndicatorProcess(lmc_model(3), prob=(0.5, 0.3, 0.2))
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(2), maxneighbors=12)
+    ens = geosgs.rand(np.random.default_rng(1), proc, grid, 2, data=data, method=method)
+    assert len(ens) == 2 and set(ens[0]["C"].tolist()) <= {"a", "b", "c"}
