@@ -219,10 +219,31 @@ ctype(::ExponentialTransiogram) = Int32(2)
 ctype(::GaussianTransiogram) = Int32(3)
 ctype(f) = throw(ArgumentError("GPUSEQSIM simulates proportional spherical, exponential and gaussian transiograms"))
 
+# A multivariate covariance A_1 * C_1 + A_2 * C_2 + ... (GeoStatsFunctions'
+# NestedCovariance with matrix coefficients, nvariables(f) = L) is a linear
+# model of coregionalization: each node solves the full simple cokriging
+# system (sgs_plan_set_indicator_cokriging), the structures C_s passed as
+# the problem's nested variogram and the A_s as the coregionalization matrices.
+vtype(::SphericalCovariance) = Int32(1)
+vtype(::ExponentialCovariance) = Int32(2)
+vtype(::GaussianCovariance) = Int32(3)
+
+function _lmc(f::NestedCovariance, dim)
+  vgs = [SgsVariogram(vtype(g), 0, ustrip(sill(g)), ustrip(nugget(g)), radii3(g.ball, dim),
+                      rot9(rotation(g.ball), dim)) for g in f.fs]
+  coef = Float64[]
+  for A in f.cs
+    M = Matrix{Float64}(A isa Number ? fill(A, 1, 1) : A)
+    append!(coef, vec(permutedims(M)))  # row-major, as the C side reads it
+  end
+  vgs, coef
+end
+
 function preprocess(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQSIM, init, domain, data)
   f = process.func
   prob = Float64.(collect(process.prob))
   2 <= length(prob) <= 8 || throw(ArgumentError("GPUSEQSIM simulates 2 to 8 categories"))
+  f isa NestedCovariance && return _preprocess_cokriging(process, method, domain, data, prob)
   r = Float64(ustrip(range(f)))
   rho = SgsVariogram(ctype(f), 0, 1.0, 0.0, (r, r, r), rot9(I(3), embeddim(domain)))
   # categories: the data's sorted distinct labels (the one-hot transform), 1..L without data
@@ -235,6 +256,22 @@ function preprocess(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQS
                                                      (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Int32}),
                                                      plan.ptr, length(prob), prob, cats), plan.ptr)
   plan = _plan([rho], 0.0, method, domain, data, zeros(length(cats)); before_prepare=setind)
+  (; plan, var, labels, nelm=nelements(domain), block=Ref(Matrix{Int32}(undef, 0, 0)), cursor=Ref(0))
+end
+
+function _preprocess_cokriging(process, method, domain, data, prob)
+  vgs, coef = _lmc(process.func, embeddim(domain))
+  length(coef) == length(vgs) * length(prob)^2 ||
+    throw(ArgumentError("coregionalization matrices must be $(length(prob)) x $(length(prob))"))
+  var = isnothing(data) ? :field : first(propertynames(values(data)))
+  labels = isnothing(data) ? collect(1:length(prob)) : sort(unique(getproperty(values(data), var)))
+  isnothing(data) || length(labels) == length(prob) ||
+    throw(ArgumentError("probabilities must have $(length(labels)) components, received $(length(prob))"))
+  cats = isnothing(data) ? Int32[] : Int32.(indexin(getproperty(values(data), var), labels) .- 1)
+  setcok(plan) = GC.@preserve prob cats coef check(ccall((:sgs_plan_set_indicator_cokriging, libgeosgs), Cint,
+                                                         (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Int32}, Ptr{Float64}),
+                                                         plan.ptr, length(prob), prob, cats, coef), plan.ptr)
+  plan = _plan(vgs, 0.0, method, domain, data, zeros(length(cats)); before_prepare=setcok)
   (; plan, var, labels, nelm=nelements(domain), block=Ref(Matrix{Int32}(undef, 0, 0)), cursor=Ref(0))
 end
 
