@@ -101,3 +101,85 @@ def test_tensor_core_inference_matches_fp32(k, geosgs_lib):
         if n:
             np.testing.assert_allclose(b[g, :n], nn_oracle.forward(params, fh[g], n), rtol=1e-4, atol=1e-5)
     G.close()
+
+
+def _cg_iterations(K, c, x0, tol=1e-6, maxit=400):
+    """Conjugate-gradient iterations (FP32 arithmetic) from x0 until the
+    residual is below tol x |c|_inf."""
+    K = K.astype(np.float32)
+    c = c.astype(np.float32)
+    x = x0.astype(np.float32).copy()
+    r = c - K @ x
+    p = r.copy()
+    rr = float(r @ r)
+    cn = float(np.abs(c).max())
+    it = 0
+    while float(np.abs(r).max()) > tol * cn and it < maxit:
+        Ap = K @ p
+        a = rr / float(p @ Ap)
+        x += a * p
+        r -= a * Ap
+        rr2 = float(r @ r)
+        p = r + (rr2 / rr) * p
+        rr = rr2
+        it += 1
+    return it
+
+
+def test_warm_start_gain_and_crossover(oracle_mod, geosgs_lib):
+    """What the trained network gains over the method without it, on
+    held-out systems: its predictions start closer to the exact weights than
+    a zero start or an untrained network (relative L2 error of the start),
+    and the conjugate-gradient iterations to 1e-6 from each start, beside
+    those from starts of controlled accuracy (1e-1 .. 1e-4).  The curve is
+    the crossover: an iterative solve from a prediction beats the FP32
+    inverse (whose Gauss-Jordan cost is about 35 such iterations at k = 32..48)
+    only for starts better than about 1e-2."""
+    torch = pytest.importorskip("torch")
+    feat, count, target = learned.generate(150000, seed=1, torch=torch, dims=(40, 40, 24))
+    trained, _ = learned.train(feat, count, target, torch, epochs=20, batch=8192, lr=3e-3)
+    untrained = learned.init_params(0)
+    wl = workloads.small(dim=3, n=36, nz=16, k=32, vario="exp", ranges=(14.0, 7.0, 4.0),
+                         rotation=geosgs.RotZ(20.0), nugget=0.08,
+                         ball=geosgs.MetricBall((14.0, 7.0, 4.0), geosgs.RotZ(20.0)), precision="fp64", nreals=4)
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = geosgs.Plan(p, keep).prepare()
+    w, _, st = G.weights()
+    idx, cnt = G.neighbors()
+    preds = {}
+    for name, params in (("trained", trained), ("untrained", untrained)):
+        G.set_network(params)
+        out = torch.empty((G.N, G.k), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        G.predict_device(out.data_ptr(), tensor_cores=False)  # writes every entry; returns when done
+        preds[name] = out.cpu().numpy().astype(np.float64)
+    G.close()
+    kr = np.nonzero((st == 0) & (cnt >= 8))[0]
+    err = {name: np.median([np.linalg.norm(pr[g, :cnt[g]] - w[g, :cnt[g]]) / np.linalg.norm(w[g, :cnt[g]])
+                            for g in kr]) for name, pr in preds.items()}
+    err["zero"] = 1.0
+    print("median relative start error: " + ", ".join(f"{k} {v:.3f}" for k, v in err.items()))
+    assert err["trained"] < 0.9 * err["zero"] and err["trained"] < err["untrained"]
+    # CG iterations from each start on a sample of the systems
+    grid = wl.domain
+    pts = grid.centroids()
+    v = p.variogram
+    rng = np.random.default_rng(0)
+    sample = rng.choice(kr, 120, replace=False)
+    its = {"zero": [], "trained": [], "1e-1": [], "1e-2": [], "1e-3": [], "1e-4": []}
+    for g in sample:
+        n = int(cnt[g])
+        X = pts[idx[g, :n]]
+        lags = (X[:, None, :] - X[None, :, :]).reshape(-1, 3)
+        K = np.array([oracle_mod.covariance(v, 3, l) for l in lags]).reshape(n, n)
+        c = np.array([oracle_mod.covariance(v, 3, l) for l in X - pts[g]])
+        ws = np.linalg.solve(K, c)
+        its["zero"].append(_cg_iterations(K, c, np.zeros(n)))
+        its["trained"].append(_cg_iterations(K, c, preds["trained"][g, :n]))
+        for e in ("1e-1", "1e-2", "1e-3", "1e-4"):
+            x0 = ws + float(e) * np.linalg.norm(ws) * rng.standard_normal(n) / np.sqrt(n)
+            its[e].append(_cg_iterations(K, c, x0))
+    mean = {k: float(np.mean(x)) for k, x in its.items()}
+    print("mean CG iterations to 1e-6: " + ", ".join(f"{k} {v:.1f}" for k, v in mean.items()))
+    assert mean["trained"] <= mean["zero"] + 0.5
+    assert mean["1e-1"] > mean["1e-2"] > mean["1e-3"] > mean["1e-4"]
