@@ -118,10 +118,16 @@ struct oracle_plan {
     std::vector<sgs_variogram> vs;  // every structure of the (nested) model
     std::vector<Metric> vms;        // their normalized lag metrics
     double sill = 1.0;        // the model's sill: the structures' sills summed
+    // covariances of grid lags L (|L_j| <= lut_e[j]) computed once: entry
+    // (L0 + e0) + w0 ((L1 + e1) + w1 (L2 + e2)) holds cov(L * spacing), the
+    // value cov() gives for every grid pair with that lag
+    std::vector<double> lut;
+    int64_t lut_e[3] = {-1, -1, -1}, lut_w[3] = {0, 0, 0};
     double mean;
     int nmin, nmax;
     Metric search;
     Metric vmetric;           // variogram's normalized lag metric
+    int64_t tmpl_ext[3] = {0, 0, 0};  // the offset template's extent per axis (cells)
     std::vector<int32_t> path, rank;
     std::vector<Offset> tmpl;
     // data buckets
@@ -169,6 +175,25 @@ struct oracle_plan {
         } else {
             for (int j = 0; j < dim; ++j) x[j] = dx[(a - N) * 3 + j];
         }
+    }
+    // covariance of two points by their ids, given their cells (ca, cb;
+    // unused for data): grid pairs through the lag table when it covers
+    // their lag
+    double cov_pair(int64_t a, int64_t b, const int64_t* ca, const int64_t* cb) const {
+        double h[3];
+        if (a < N && b < N && !lut.empty()) {
+            int64_t off = 0, mult = 1;
+            bool inside = true;
+            for (int j = 0; j < dim; ++j) {
+                const int64_t L = cb[j] - ca[j];
+                inside = inside && L >= -lut_e[j] && L <= lut_e[j];
+                off += (L + lut_e[j]) * mult;
+                mult *= lut_w[j];
+            }
+            if (inside) return lut[(size_t)off];
+        }
+        lag(a, b, h);
+        return cov(h);
     }
     // C(h) = sill - gamma(h), gamma = sum over the structures of
     // nugget_s + (sill_s - nugget_s) f_s(|h|_s) for h != 0 (utils.jl:50-62)
@@ -319,6 +344,7 @@ extern "C" int oracle_create(const sgs_problem* p, oracle_plan** out) {
     for (int j = 0; j < P->dim; ++j) {
         if (P->search.kind == 2) e[j] = P->n[j] - 1;
         else e[j] = std::min<int64_t>(P->n[j] - 1, (int64_t)std::floor(P->search.ext[j] / P->spacing[j]) + 1);
+        P->tmpl_ext[j] = e[j];
     }
     for (int64_t c = -e[2]; c <= e[2]; ++c)
         for (int64_t b = -e[1]; b <= e[1]; ++b)
@@ -504,14 +530,20 @@ static void solve_node(oracle_plan* P, int64_t g, std::vector<double>& K, std::v
     }
     K.assign((size_t)n * n, 0.0);
     c.assign(n, 0.0);
+    int64_t cells[3 * 64 + 3];  // grid cells of the neighbours (maxneighbors <= 64 on the GPU path)
+    std::vector<int64_t> cells_big;
+    int64_t* cl = cells;
+    if (n > 64) {
+        cells_big.resize(3 * (size_t)n);
+        cl = cells_big.data();
+    }
+    for (int a = 0; a < n; ++a)
+        if (nb[a] < P->N) P->cell(nb[a], cl + 3 * a);
     double h[3];
     for (int a = 0; a < n; ++a) {
         P->lag(g, nb[a], h);
         c[a] = P->cov(h);
-        for (int b = 0; b <= a; ++b) {
-            P->lag(nb[b], nb[a], h);
-            K[(size_t)a * n + b] = P->cov(h);
-        }
+        for (int b = 0; b <= a; ++b) K[(size_t)a * n + b] = P->cov_pair(nb[b], nb[a], cl + 3 * b, cl + 3 * a);
     }
     // Cholesky (lower, row a: L[a][b] for b <= a), pivot rule
     const double tau = kSingularTau * P->sill;
@@ -550,8 +582,40 @@ static void solve_node(oracle_plan* P, int64_t g, std::vector<double>& K, std::v
     P->status[g] = SGS_NODE_KRIGED;
 }
 
+// Grid-lag covariance table, built once per plan before the first solve: lags
+// up to twice the template's extent per axis (every pair of a node's grid
+// neighbours), capped so the table stays below 2^22 entries.
+static void build_lut(oracle_plan* P) {
+    if (P->lut_e[0] >= 0) return;
+    int64_t e[3] = {0, 0, 0}, total = 1;
+    for (int j = 0; j < P->dim; ++j) e[j] = std::min<int64_t>(2 * P->tmpl_ext[j], P->n[j] - 1);
+    for (;;) {
+        total = 1;
+        for (int j = 0; j < P->dim; ++j) total *= 2 * e[j] + 1;
+        if (total <= ((int64_t)1 << 22)) break;
+        for (int j = 0; j < P->dim; ++j) e[j] = e[j] * 3 / 4;
+    }
+    for (int j = 0; j < 3; ++j) {
+        P->lut_e[j] = j < P->dim ? e[j] : 0;
+        P->lut_w[j] = 2 * P->lut_e[j] + 1;
+    }
+    P->lut.assign((size_t)total, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < total; ++i) {
+        int64_t r = i;
+        double h[3] = {0.0, 0.0, 0.0};
+        for (int j = 0; j < P->dim; ++j) {
+            const int64_t L = r % P->lut_w[j] - P->lut_e[j];
+            r /= P->lut_w[j];
+            h[j] = (double)L * P->spacing[j];  // the lag() of a grid pair
+        }
+        P->lut[(size_t)i] = P->cov(h);
+    }
+}
+
 extern "C" int oracle_solve(oracle_plan* P, int64_t t0, int64_t t1, int64_t stride, int nthreads) {
     if (!P) return fail(SGS_ERR_ARG, "null plan");
+    build_lut(P);
     if (stride < 1) stride = 1;
     t0 = std::max<int64_t>(0, t0);
     t1 = std::min<int64_t>(P->N, t1);

@@ -143,9 +143,11 @@ def test_full_depth_all_c5_domains(oracle_mod, geosgs_lib):
             zs = [np.random.default_rng(7000 + c0 + d).standard_normal((R, int(n))) for d, n in enumerate(B.sizes)]
             vals = B.simulate(R, z=zs)
             fp64 = B.values_fp64()
-            futs = [pool.submit(oracle_domain, (p, keep, zs[d])) for d, (p, keep) in enumerate(probs)]
-            for d, fut in enumerate(futs):
-                io, co, wo, so, sto, vo = fut.result()
+            # largest domains first, so the chunk does not wait on one late straggler
+            futs = {d: pool.submit(oracle_domain, (probs[d][0], probs[d][1], zs[d]))
+                    for d in sorted(range(len(probs)), key=lambda d: -int(B.sizes[d]))}
+            for d in range(len(probs)):
+                io, co, wo, so, sto, vo = futs[d].result()
                 ig, cg = B.neighbors(d)
                 assert np.array_equal(cg, co) and np.array_equal(ig, io), f"domain {c0 + d}"
                 wg, sg, stg = B.weights(d)
