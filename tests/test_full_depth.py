@@ -156,8 +156,9 @@ def test_full_depth_all_c5_domains(oracle_mod, geosgs_lib):
                 worst["sigma"] = max(worst["sigma"], float(np.max(np.abs(sg - so))))
                 worst["values"] = max(worst["values"], float(rel(vals[d], vo).max()))
                 nodes += vo.shape[1]
+            report(f"c5 domains {c0}-{c0 + len(items) - 1}", values_fp64=int(fp64),
+                   domains_fp64=int(B.info().domains_fp64), **worst)
             B.close()
-            report(f"c5 domains {c0}-{c0 + len(items) - 1}", values_fp64=int(fp64), **worst)
     report("c5_batch_1000_domains all", nodes=nodes, reals=R, seconds=time.perf_counter() - t0, **worst)
     assert nodes == bw.nodes()
     assert worst["weights"] <= WEIGHT_TOL
