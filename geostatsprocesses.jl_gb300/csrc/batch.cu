@@ -61,9 +61,10 @@ levels_batch_kernel(const LevelDom* __restrict__ doms, const int64_t* __restrict
     volatile int32_t* vlevel = level;
     const volatile int32_t* verr = err;
     int wmax = 0;
-    for (;;) {
+    for (int taken = 0;; ++taken) {
         unsigned long long t = 0;
-        if (lane == 0) t = *verr ? (unsigned long long)total : atomicAdd(ticket, 1ull);
+        // after an error no new tickets (the flag is read every 16th ticket)
+        if (lane == 0) t = ((taken & 15) == 15 && *verr) ? (unsigned long long)total : atomicAdd(ticket, 1ull);
         t = __shfl_sync(FULL_MASK, t, 0);
         if ((int64_t)t >= total) break;
         const int d = find_domain(noff, ndom, (int64_t)t);

@@ -241,24 +241,30 @@ __device__ __forceinline__ uint64_t global_ns() {
 
 // Level of node c once it is known (>= 0).  Bounded: the wait gives up after
 // wait_ns of wall-clock time (or, should the timer stall, after a count of
-// polls, each at least the 64 ns back-off, reached no earlier), and at once
-// when another warp has already raised *err.  A warp that gives up raises
-// *err; the returned level is then 0 and the caller's result is void.
+// polls, each at least the 64 ns back-off, reached no earlier), and soon after
+// another warp has raised *err.  The flag and the timer are read every 32nd
+// poll only: the flag shares its cache line with the kernel's ticket counter,
+// which every warp updates.  A warp that gives up raises *err; the returned
+// level is then 0 and the caller's result is void.
 __device__ __forceinline__ int wait_level(const volatile int32_t* vlevel, int64_t c, int32_t* err,
                                           uint64_t wait_ns) {
     int l = vlevel[c];
     if (l >= 0) return l;
     const volatile int32_t* verr = err;
     const uint64_t max_polls = wait_ns / 32 + 1024;
-    const uint64_t t0 = global_ns();
-    for (uint64_t polls = 0;; ++polls) {
+    uint64_t t0 = 0;
+    for (uint64_t polls = 1;; ++polls) {
         __nanosleep(64);
         l = vlevel[c];
         if (l >= 0) return l;
-        if (*verr) return 0;
-        if (global_ns() - t0 > wait_ns || polls > max_polls) {
-            atomicExch(err, 1);
-            return 0;
+        if ((polls & 31) == 0) {
+            if (*verr) return 0;
+            const uint64_t now = global_ns();
+            if (t0 == 0) t0 = now;
+            if (now - t0 > wait_ns || polls > max_polls) {
+                atomicExch(err, 1);
+                return 0;
+            }
         }
     }
 }

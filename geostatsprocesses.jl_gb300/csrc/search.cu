@@ -395,9 +395,10 @@ __global__ void __launch_bounds__(256) levels_kernel(const LevelArgs a) {
     volatile int32_t* vlevel = a.level;
     const volatile int32_t* verr = a.err;
     int wmax = 0;
-    while (true) {
+    for (int taken = 0;; ++taken) {
         int64_t t0 = 0;
-        if (lane == 0) t0 = *verr ? a.N : atomicAdd(a.ticket, LEVEL_CHUNK);
+        // after an error no new tickets (the flag is read every 16th ticket)
+        if (lane == 0) t0 = ((taken & 15) == 15 && *verr) ? a.N : atomicAdd(a.ticket, LEVEL_CHUNK);
         t0 = __shfl_sync(FULL_MASK, t0, 0);
         if (t0 >= a.N) break;
         const int64_t t1 = min(t0 + (int64_t)LEVEL_CHUNK, a.N);
