@@ -255,9 +255,15 @@ def test_batch_device_values_and_autotuner(oracle_mod, geosgs_lib):
     B.simulate_device(R, 5, V)
     info = B.info()
     assert info.ms_sweep > 0
-    Vh = V.cpu().numpy().astype(np.float64)
+    Vn = V.cpu().numpy()
     for d, w in enumerate(bw.items):
         f, n = int(B.first[d]), int(B.sizes[d])
-        dev = Vh[f:f + n].T + w.process.mean
+        if not B.values_fp64():
+            rows = Vn[f:f + n].astype(np.float64)
+        elif B.domain_values_fp64(d):
+            rows = Vn[f:f + n]
+        else:  # FP32 values in the first half of the domain's FP64 rows
+            rows = Vn.view(np.float32).reshape(B.nnodes, 2 * R)[f:f + n, :R].astype(np.float64)
+        dev = rows.T + w.process.mean
         assert rel_err(dev, host[d]) <= 1e-7, d
     B.close()
