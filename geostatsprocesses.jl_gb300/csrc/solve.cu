@@ -580,6 +580,8 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                 // residual computed (it also drives the last correction)
                 DF sw0 = w0, sw1 = w1;
                 float sr0 = 0.0f, sr1 = 0.0f;
+                // the correction computed from that residual (0 when none was)
+                float sd0 = 0.0f, sd1 = 0.0f;
                 // largest starting weight, for the one-correction estimate below
                 float wmax = fmaxf(i0 < n ? fabsf(w0.hi) : 0.0f, TWO && i1 < n ? fabsf(w1.hi) : 0.0f);
 #pragma unroll
@@ -614,6 +616,7 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     sw1 = w1;
                     sr0 = r0;
                     sr1 = r1;
+                    sd0 = sd1 = 0.0f;
                     if (s == steps) break;  // steps == 0: no correction
                     __syncwarp();
                     vec[i0] = r0;
@@ -627,6 +630,8 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                         if (TWO) d1 = __fmaf_rn(-R1[j], v, d1);
                     }
                     float dmax = 0.0f;
+                    sd0 = i0 < n ? d0 : 0.0f;
+                    sd1 = TWO && i1 < n ? d1 : 0.0f;
                     if (i0 < n) {
                         const DF t = df_two_sum(w0.hi, d0);
                         w0 = df_fast_two_sum(t.hi, __fadd_rn(t.lo, w0.lo));
@@ -674,15 +679,25 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     accept = isfinite(last);
                 }
                 if (accept) {
-                    // sigma^2 = sill (1 - w'c - w'r) with r = c - K w: equal to
-                    // sill - w'c at the exact weights, but stationary there
-                    // (its error is second order in the weights' error), so
-                    // it stays accurate where the variance cancels to ~0 (a
-                    // node on a datum), where sqrt would magnify any error
+                    // sigma^2 = sill S(w), S(w) = 1 - w'c - w'r with r = c - K w:
+                    // equal to 1 - w'c at the exact weights, but stationary
+                    // there (its error is (w - w*)' K (w - w*)), so it stays
+                    // accurate where the variance cancels to ~0 (a node on a
+                    // datum), where sqrt would magnify any error.  It is taken
+                    // at the final weights w + d: S(w + d) = S(w) - 2 d'r +
+                    // d' K d, and K d = r up to the inverse's error, so
+                    // S(w + d) = S(w) - d'r with an error of order
+                    // |d| |r| x that error.
                     DFAcc acc;
                     acc.init({0.0f, 0.0f});
-                    if (i0 < n) acc.add_prod(sw0, df_add(c[i0], {sr0, 0.0f}));
-                    if (TWO && i1 < n) acc.add_prod(sw1, df_add(c[i1], {sr1, 0.0f}));
+                    if (i0 < n) {
+                        acc.add_prod(sw0, df_add(c[i0], {sr0, 0.0f}));
+                        acc.add_prod({sd0, 0.0f}, {sr0, 0.0f});
+                    }
+                    if (TWO && i1 < n) {
+                        acc.add_prod(sw1, df_add(c[i1], {sr1, 0.0f}));
+                        acc.add_prod({sd1, 0.0f}, {sr1, 0.0f});
+                    }
                     const DF wc = warp_sum_df(acc.value());
                     sigma = df_mul(sd_sill, df_sqrt(df_add({1.0f, 0.0f}, df_neg(wc))));
                 }
