@@ -146,3 +146,26 @@ def test_paths():
     np.testing.assert_array_equal(p, geosgs.RandomPath(4).permutation(1000))
     with pytest.raises(geosgs.ArgumentError):
         geosgs.ExplicitPath([0, 1]).permutation(3)
+
+
+def test_reference_arm_line_shares_the_config():
+    """bench.py --impl reference times the FP64 oracle on a bounded sample and
+    prints the workload's config exactly as the GPU arm builds it (what is
+    simulated, not how), marks the value as extrapolated from the sample and
+    reports the sample's own wall time per step."""
+    import json
+    import subprocess
+    import sys
+
+    import bench
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "c1",
+                        "--steps", "1", "--warmup", "0", "--cpu-nodes", "2000"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    wl = bench.workload("c1", "fp64", None)
+    assert line["config"] == bench.config_of(wl, 1)
+    assert line["impl"] == "reference" and line["extrapolated"] is True
+    assert line["ms_per_step"] == line["sample_wall_ms_per_step"] > 0
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
