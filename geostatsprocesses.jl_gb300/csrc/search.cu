@@ -24,6 +24,12 @@ namespace sgs {
 constexpr int SEARCH_WARPS = 8;
 constexpr int SCAN_STEPS = 4;  // template steps of 32 entries loaded per pass
 constexpr int DCAP = 256;  // data candidate buffer per warp
+// Early path ranks: a node of rank t has exactly t simulated grid nodes, the
+// first t of the path.  While t is small against the template (T > 8 t, up
+// to 2048), testing those t nodes costs less than scanning the template far
+// enough to find k of them (the scan reads about k N / t entries).
+constexpr int BRUTE_MAX = 2048;
+constexpr int BRUTE_RATIO = 8;
 
 // Squared distances are non-negative doubles, whose IEEE bit patterns order
 // exactly like the values when read as int64, so the kernel compares and
@@ -92,7 +98,55 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
         // (the entries are processed in the same order as one step at a time)
         int ng = 0;
         const int T = a.data_only ? 0 : a.T;
-        for (int base = 0; base < T && ng < k; base += 32 * SCAN_STEPS) {
+        if (!a.data_only && t <= BRUTE_MAX && (int64_t)BRUTE_RATIO * t < T) {
+            // the t earlier path nodes, with the template's canonical FP64 d2
+            // (h_j = offset_j x spacing_j), inside the same neighbourhood,
+            // kept by (d2, node id): the order of the template (d2, linear
+            // offset), since for a fixed node the linear offset orders ids
+            int nbuf = 0;
+            for (int base = 0; base < t; base += 32) {
+                const int j = base + lane;
+                int c = 0, c0 = 0, c1 = 0, c2 = 0;
+                bool maybe = false;
+                if (j < t) {
+                    c = a.path[j];
+                    cell_of(G, c, c0, c1, c2);
+                    maybe = a.metric.kind == METRIC_NEAREST ||
+                            metric_maybe_within(a.metric, G.dim, (float)(c0 - i0) * a.spacing_f[0],
+                                                (float)(c1 - i1) * a.spacing_f[1],
+                                                (float)(c2 - i2) * a.spacing_f[2], a.metric.bound_f);
+                }
+                bool ok = false;
+                double d2 = 0.0;
+                if (__any_sync(FULL_MASK, maybe) && maybe) {
+                    d2 = metric_d2(a.metric, G.dim, dmul((double)(c0 - i0), G.spacing[0]),
+                                   dmul((double)(c1 - i1), G.spacing[1]),
+                                   G.dim == 3 ? dmul((double)(c2 - i2), G.spacing[2]) : 0.0);
+                    ok = metric_inside(a.metric, d2);
+                }
+                const unsigned b = __ballot_sync(FULL_MASK, ok);
+                if (ok) {
+                    const int p = nbuf + __popc(b & lt);
+                    dd2[p] = key_of(d2);
+                    didx[p] = c;
+                }
+                nbuf += __popc(b);
+                __syncwarp();
+                if (nbuf > DCAP - 32) {
+                    warp_sort_pairs(dd2, didx, nbuf, lane);
+                    nbuf = min(nbuf, k);
+                }
+            }
+            if (nbuf > 0) warp_sort_pairs(dd2, didx, nbuf, lane);
+            ng = min(nbuf, k);
+            for (int q = lane; q < ng; q += 32) {
+                gd2[q] = dd2[q];
+                gidx[q] = didx[q];
+            }
+            __syncwarp();
+        }
+        for (int base = 0; base < T && ng < k && !(t <= BRUTE_MAX && (int64_t)BRUTE_RATIO * t < T);
+             base += 32 * SCAN_STEPS) {
             int c[SCAN_STEPS];
             bool in[SCAN_STEPS];
 #pragma unroll
