@@ -452,24 +452,38 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
             if (lut2 && fits) {
                 // every pairwise lag of grid neighbours is inside the table (a
                 // plan's table spans twice the search template, so this always
-                // holds there); the clamp only keeps reads in bounds
-                for (int q = lane; q < n; q += 32) {
-                    if (info[q].did < 0) {
-                        const float2 v = lut2[min(max(lcentre - lin[q], 0), ltotal - 1)];
-                        c[q] = {v.x, v.y};
-                    } else {
-                        c[q] = kcov2n(a, info[q], self);
-                    }
+                // holds there); the clamp only keeps reads in bounds.  Lane l
+                // fills columns l and l + 32 of every row; it keeps their
+                // offsets in registers, and row r's offset and kind come by
+                // shuffle and ballot mask instead of shared-memory loads.
+                const bool gA = lane < n && info[lane].did < 0;
+                const bool gB = lane + 32 < n && info[lane + 32].did < 0;
+                const int linA = gA ? lin[lane] : 0, linB = gB ? lin[lane + 32] : 0;
+                const unsigned mA = __ballot_sync(FULL_MASK, gA), mB = __ballot_sync(FULL_MASK, gB);
+                if (gA) {
+                    const float2 v = lut2[min(max(lcentre - linA, 0), ltotal - 1)];
+                    c[lane] = {v.x, v.y};
+                } else if (lane < n) {
+                    c[lane] = kcov2n(a, info[lane], self);
+                }
+                if (gB) {
+                    const float2 v = lut2[min(max(lcentre - linB, 0), ltotal - 1)];
+                    c[lane + 32] = {v.x, v.y};
+                } else if (lane + 32 < n) {
+                    c[lane + 32] = kcov2n(a, info[lane + 32], self);
                 }
                 for (int r = 0; r < n; ++r) {
-                    if (info[r].did >= 0) continue;
-                    const int base = lcentre + lin[r];
+                    const int linr = __shfl_sync(FULL_MASK, r < 32 ? linA : linB, r & 31);
+                    if (!(((r < 32 ? mA : mB) >> (r & 31)) & 1u)) continue;  // warp-uniform: row r is a datum
+                    const int base = lcentre + linr;
                     DF* Kr = K + r * (r + 1) / 2;
-                    for (int q = lane; q <= r; q += 32) {
-                        if (info[q].did < 0) {
-                            const float2 v = lut2[min(max(base - lin[q], 0), ltotal - 1)];
-                            Kr[q] = {v.x, v.y};
-                        }
+                    if (gA && lane <= r) {
+                        const float2 v = lut2[min(max(base - linA, 0), ltotal - 1)];
+                        Kr[lane] = {v.x, v.y};
+                    }
+                    if (gB && lane + 32 <= r) {
+                        const float2 v = lut2[min(max(base - linB, 0), ltotal - 1)];
+                        Kr[lane + 32] = {v.x, v.y};
                     }
                 }
             } else {
@@ -520,7 +534,10 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     ok = false;
                     break;
                 }
-                const float inv = __frcp_rn(d);
+                // the inverse is a preconditioner only: the approximate
+                // reciprocal (pivots lie in (1e-3, 1], no denormals) is enough
+                float inv;
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(d));
                 float* cb = colb + (kk & 1) * S::CB;
                 if (own0) {
                     int p = i0 - kk - 1;
