@@ -72,6 +72,7 @@ def measure_peaks() -> dict:
     for name in ("geosgs_peak_fp32", "geosgs_peak_fp64", "geosgs_peak_gj_pattern"):
         getattr(lib, name).argtypes = [ctypes.POINTER(ctypes.c_double)]
     lib.geosgs_peak_host_write.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+    lib.geosgs_peak_d2h_copy.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
     v = ctypes.c_double(0.0)
     if lib.geosgs_peak_fp32(ctypes.byref(v)) == 0:
         out["fp32_tflops"] = v.value
@@ -81,6 +82,8 @@ def measure_peaks() -> dict:
         out["gj_pattern_tflops"] = v.value
     if lib.geosgs_peak_host_write(ctypes.c_int64(1 << 30), ctypes.byref(v)) == 0:
         out["host_write_gbs"] = v.value
+    if lib.geosgs_peak_d2h_copy(ctypes.c_int64(1 << 30), ctypes.byref(v)) == 0:
+        out["d2h_copy_gbs"] = v.value
     return out
 
 
@@ -729,6 +732,8 @@ def main():
         # the FP64 output crosses the CPU-GPU link: the floor of its transfer
         e2e["host_write_gbs"] = probes["host_write_gbs"]
         e2e["d2h_floor_ms"] = e2e["d2h_bytes_per_step"] / probes["host_write_gbs"] / 1e6
+        if probes.get("d2h_copy_gbs"):
+            e2e["d2h_copy_gbs"] = probes["d2h_copy_gbs"]
 
     # the solve (kernel b), bound by the FP32 pipe, on the survey's FLOP
     # basis (factorization n^3/3, not the cost of the algorithm run); the

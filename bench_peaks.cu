@@ -201,6 +201,41 @@ extern "C" int geosgs_peak_host_write(int64_t bytes, double* gbs) {
     return 0;
 }
 
+// Best of three device-to-page-locked-host copies (cudaMemcpyAsync, the
+// copy engines) of `bytes`; *gbs = bytes / s / 1e9.  0 on success.
+extern "C" int geosgs_peak_d2h_copy(int64_t bytes, double* gbs) {
+    if (!gbs || bytes < 16) return 1;
+    void* h = nullptr;
+    void* d = nullptr;
+    if (cudaHostAlloc(&h, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return 2;
+    if (cudaMalloc(&d, (size_t)bytes) != cudaSuccess) {
+        cudaFreeHost(h);
+        return 2;
+    }
+    cudaMemset(d, 1, (size_t)bytes);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        cudaMemcpyAsync(h, d, (size_t)bytes, cudaMemcpyDeviceToHost, 0);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    cudaFreeHost(h);
+    if (err != cudaSuccess || best <= 0.f) return 3;
+    *gbs = (double)bytes / (best * 1e-3) / 1e9;
+    return 0;
+}
+
 // FP32 rate of the Gauss-Jordan update pattern with 10 resident warps per SM
 // (the solve's occupancy): *tflops = 2 x FFMA lanes per second / 1e12.
 extern "C" int geosgs_peak_gj_pattern(double* tflops) {

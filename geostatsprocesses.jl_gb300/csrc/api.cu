@@ -614,7 +614,7 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     P->precision = pr->precision;
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
-    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32))
+    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32 | SGS_FLAG_OUTPUT_STAGED))
         return set_err(P, SGS_ERR_ARG, "unknown flags");
     if ((pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) && (pr->flags & SGS_FLAG_LEVEL_SWEEP))
         return set_err(P, SGS_ERR_ARG, "SGS_FLAG_ONE_LAUNCH_SWEEP and SGS_FLAG_LEVEL_SWEEP exclude each other");
@@ -1147,7 +1147,50 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     // straight into `out` when it is page-locked host memory the device can
     // address, else in chunks of realizations through a device buffer
     double* dout = pinned_device_view(out);
-    if (dout) {
+    if (dout && (P->flags & SGS_FLAG_OUTPUT_STAGED)) {
+        // chunks of realizations transposed on the plan's stream into two
+        // device buffers in turn, each copied out by the copy engines on a
+        // second stream while the next chunk is transposed
+        const int64_t stage_bytes = (int64_t)1 << 28;
+        const int64_t rc_n = std::max<int64_t>(1, std::min<int64_t>(R, stage_bytes / (N * (int64_t)sizeof(double))));
+        double* sb[2] = {nullptr, nullptr};
+        if ((rc = dalloc(P, &sb[0], (size_t)N * rc_n)) || (rc = dalloc(P, &sb[1], (size_t)N * rc_n))) {
+            dfree(P, sb[0]);
+            return rc;
+        }
+        cudaStream_t cs = nullptr;
+        cudaEvent_t made[2] = {nullptr, nullptr}, moved[2] = {nullptr, nullptr};
+        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+        for (int b = 0; ok && b < 2; ++b)
+            ok = cudaEventCreateWithFlags(&made[b], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&moved[b], cudaEventDisableTiming) == cudaSuccess;
+        int64_t i = 0;
+        for (int64_t r0 = 0; ok && r0 < R; r0 += rc_n, ++i) {
+            const int rn = (int)std::min<int64_t>(rc_n, R - r0);
+            const int b = (int)(i & 1);
+            if (i >= 2) ok = ok && cudaStreamWaitEvent(st, moved[b], 0) == cudaSuccess;  // buffer free again
+            const cudaError_t e = values_fp64(P)
+                ? launch_rows_to_out_fp64((const double*)V + r0, N, rn, Rp, P->mean, sb[b], st)
+                : launch_rows_to_out_fp32((const float*)V + r0, N, rn, Rp, P->mean, sb[b], st);
+            ok = ok && e == cudaSuccess && cudaEventRecord(made[b], st) == cudaSuccess &&
+                 cudaStreamWaitEvent(cs, made[b], 0) == cudaSuccess &&
+                 cudaMemcpyAsync(out + r0 * N, sb[b], (size_t)N * rn * sizeof(double), cudaMemcpyDeviceToHost, cs) ==
+                     cudaSuccess &&
+                 cudaEventRecord(moved[b], cs) == cudaSuccess;
+            P->info.launches++;
+            P->info.d2h_bytes += (int64_t)N * rn * sizeof(double);
+        }
+        ok = ok && cudaStreamSynchronize(cs) == cudaSuccess;
+        const cudaError_t err = cudaGetLastError();
+        for (int b = 0; b < 2; ++b) {
+            if (made[b]) cudaEventDestroy(made[b]);
+            if (moved[b]) cudaEventDestroy(moved[b]);
+        }
+        if (cs) cudaStreamDestroy(cs);
+        dfree(P, sb[0]);
+        dfree(P, sb[1]);
+        if (!ok) return cuda_err(P, err != cudaSuccess ? err : cudaErrorUnknown, "staged output");
+    } else if (dout) {
         if (values_fp64(P))
             LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V, N, R, Rp, P->mean, dout, st));
         else

@@ -70,6 +70,10 @@ extern "C" {
 #define SGS_FLAG_LEVEL_SWEEP      2  /* one launch per dependency level */
 #define SGS_FLAG_NN_FP32          4  /* warm-start inference in FP32 on the CUDA cores
                                         instead of BF16 on the tensor cores */
+#define SGS_FLAG_OUTPUT_STAGED    8  /* sgs_plan_simulate into page-locked memory:
+                                        transpose chunks into device buffers and
+                                        move them with the copy engines (overlapped),
+                                        instead of kernels writing host memory */
 
 /* ---- per-node solve status (sgs_plan_weights) --------------------------- */
 #define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */

@@ -206,15 +206,20 @@ def test_reference_datum_reproduction_gpu(geosgs_lib):
         assert len(ens) == 3 and ens[2]["Z"].shape == (grid.nelements(),)
 
 
-def test_simulate_into_pinned_host_memory(geosgs_lib):
+@pytest.mark.parametrize("staged", [False, True])
+def test_simulate_into_pinned_host_memory(staged, geosgs_lib):
     """A page-locked output buffer is written by the transposing kernel
-    directly; the values equal those returned through pageable memory."""
+    directly, or (SGS_FLAG_OUTPUT_STAGED) through device buffers moved by the
+    copy engines in chunks; the values equal those returned through pageable
+    memory."""
     import ctypes as C
 
     torch = pytest.importorskip("torch")
     for precision in ("fp32", "fp64"):
         wl = workloads.small(n=40, k=12, ndata=10, vario="exp", nugget=0.05, precision=precision, nreals=12)
         p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+        if staged:
+            p.flags |= _abi.SGS_FLAG_OUTPUT_STAGED
         G = gpu_plan(p, keep)
         z = np.random.default_rng(4).standard_normal((12, G.N))
         a = G.simulate(12, z)

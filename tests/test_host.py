@@ -48,7 +48,8 @@ def test_peak_probe_library_builds_and_exports():
     import bench
 
     lib = C.CDLL(bench.build_peaks())
-    for name in ("geosgs_peak_fp32", "geosgs_peak_fp64", "geosgs_peak_gj_pattern", "geosgs_peak_host_write"):
+    for name in ("geosgs_peak_fp32", "geosgs_peak_fp64", "geosgs_peak_gj_pattern", "geosgs_peak_host_write",
+                 "geosgs_peak_d2h_copy"):
         assert hasattr(lib, name), name
     assert not any(n.startswith("geosgs_peak") for n in header_symbols())
 
