@@ -278,32 +278,6 @@ extern "C" int sgs_selftest_bounded_wait(int64_t wait_ns, int32_t* timed_out, in
     return rc;
 }
 
-// Diagnostic (exported, not part of the C ABI in include/geosgs.h): the
-// plan's covariance model, divided by its sill, at n lags (host array of n
-// rows x, y, z) evaluated on the device in FP64 (cov64) and in the
-// double-FP32 arithmetic the FP32 solve uses (covdf, hi + lo as a double).
-// Returns 0 or a negative SGS_ERR_* code.
-extern "C" int sgs_selftest_cov_df(const sgs_plan* p, const double* lags, int64_t n, double* cov64, double* covdf) {
-    if (!p || !lags || !cov64 || !covdf || n <= 0) return SGS_ERR_ARG;
-    if (cudaSetDevice(p->device) != cudaSuccess) return SGS_ERR_CUDA;
-    double* d = nullptr;
-    if (cudaMalloc(&d, (size_t)n * 5 * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        return SGS_ERR_CUDA;
-    }
-    int rc = SGS_OK;
-    if (cudaMemcpy(d, lags, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-        launch_cov_df_check(p->vario, p->grid.dim, 1.0 / p->vario.sill, d, n, d + 3 * n, d + 4 * n, 0) !=
-            cudaSuccess ||
-        cudaMemcpy(cov64, d + 3 * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(covdf, d + 4 * n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        rc = SGS_ERR_CUDA;
-    }
-    cudaFree(d);
-    return rc;
-}
-
 // Diagnostic (exported, not part of the C ABI in include/geosgs.h): runs the
 // dependency-level kernel on a two-node table in which each node is the
 // other's neighbour, so neither level can ever be known, with a wait limit

@@ -217,88 +217,6 @@ __device__ __forceinline__ DF df_sqrt(DF v) {
     return df_fast_two_sum(r, __fdiv_rn(d, __fmul_rn(2.0f, r)));
 }
 
-__device__ __forceinline__ DF df_mul(DF a, DF b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    const float e = __fmaf_rn(a.hi, b.hi, -p);
-    return df_fast_two_sum(p, __fadd_rn(e, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
-}
-
-// exp(x) for x <= 0 in double-FP32 (relative error below 1e-13), from the
-// mathematics: Cody-Waite reduction x = k ln2 + r with ln2 split in three
-// floats (the first with 15 significant bits, so k * L1 is exact for
-// |k| < 2^8), r / 8 into a degree-8 Taylor polynomial (|r / 8| <= 0.0434,
-// truncation below 2e-18), squared three times, scaled by 2^k.  Results
-// below the float range (x < -87) are 0.
-__device__ __forceinline__ DF df_exp_nonpos(DF x) {
-    if (x.hi < -87.0f) return {0.0f, 0.0f};
-    const float L1 = 0.693145751953125f, L2 = 1.428606765330187e-06f, L3 = 5.497923148104107e-14f;
-    const float kf = rintf(__fmul_rn(x.hi, 1.44269504f));
-    DF r = df_two_sum(x.hi, -__fmul_rn(kf, L1));  // kf * L1 exact
-    r = df_add(r, {x.lo, 0.0f});
-    const float p2 = __fmul_rn(kf, L2);
-    r = df_add(r, {-p2, -__fmaf_rn(kf, L2, -p2)});
-    r = df_add(r, {-__fmul_rn(kf, L3), 0.0f});
-    r = {__fmul_rn(r.hi, 0.125f), __fmul_rn(r.lo, 0.125f)};
-    // 1/n!, n = 8 .. 0, as float pairs (hi, lo)
-    const float ch[9] = {2.4801587642286904e-05f, 0.00019841270113829523f, 0.0013888889225199819f,
-                         0.008333333767950535f, 0.0416666679084301f, 0.1666666716337204f, 0.5f, 1.0f, 1.0f};
-    const float cl[9] = {-3.40699609366682e-13f, -2.725596874933456e-12f, -3.3631094437103215e-11f,
-                         -4.34617203337595e-10f, -1.2417634698280722e-09f, -4.967053879312289e-09f, 0.0f, 0.0f, 0.0f};
-    DF e = {ch[0], cl[0]};
-#pragma unroll
-    for (int i = 1; i < 9; ++i) e = df_add(df_mul(e, r), {ch[i], cl[i]});
-    e = df_mul(e, e);
-    e = df_mul(e, e);
-    e = df_mul(e, e);
-    const int k = (int)kf;
-    return {ldexpf(e.hi, k), ldexpf(e.lo, k)};
-}
-
-__device__ __forceinline__ DF df_of(double v) { return df_from_double(v); }
-
-// gamma(h) of one structure at a nonzero lag in double-FP32, h given in
-// double-FP32 (the same formulas as structure_gamma, about 1e-14 relative)
-__device__ __forceinline__ DF structure_gamma_df(const VarioStructDev& v, int dim, const DF* h) {
-    DF s = {0.0f, 0.0f};
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        if (j < dim) {
-            DF u = df_add(df_mul(df_of(v.R[0 + 3 * j]), h[0]), df_mul(df_of(v.R[1 + 3 * j]), h[1]));
-            if (dim == 3) u = df_add(u, df_mul(df_of(v.R[2 + 3 * j]), h[2]));
-            const DF q = df_mul(u, df_of(v.inv_range[j]));
-            s = df_add(s, df_mul(q, q));
-        }
-    }
-    DF f;
-    if (v.type == 1) {  // 1.5 h - 0.5 h^3 below the range
-        const DF hn = df_sqrt(s);
-        if (hn.hi < 1.0f) {
-            const DF h3 = df_mul(df_mul(hn, hn), hn);
-            f = df_add(df_mul({1.5f, 0.0f}, hn), df_mul({-0.5f, 0.0f}, h3));
-        } else {
-            f = {1.0f, 0.0f};
-        }
-    } else if (v.type == 2) {  // 1 - exp(-3 h)
-        const DF hn = df_sqrt(s);
-        f = df_add({1.0f, 0.0f}, df_neg(df_exp_nonpos(df_mul({-3.0f, 0.0f}, hn))));
-    } else {  // 1 - exp(-3 h^2)
-        f = df_add({1.0f, 0.0f}, df_neg(df_exp_nonpos(df_mul({-3.0f, 0.0f}, s))));
-    }
-    const DF ng = df_of(v.nugget);
-    return df_add(ng, df_mul(df_add(df_of(v.sill), df_neg(ng)), f));
-}
-
-// covariance C(h) / sill of the model (all structures) in double-FP32; the
-// lag comes in FP64 and is split once
-__device__ __forceinline__ DF cov_df_norm(const VarioDev& v, int dim, double h0, double h1, double h2,
-                                          double inv_sill) {
-    if (h0 == 0.0 && h1 == 0.0 && (dim == 2 || h2 == 0.0)) return {1.0f, 0.0f};
-    const DF h[3] = {df_of(h0), df_of(h1), df_of(h2)};
-    DF g = structure_gamma_df(v.st[0], dim, h);
-    for (int i = 1; i < v.ns; ++i) g = df_add(g, structure_gamma_df(v.st[i], dim, h));
-    return df_mul(df_add(df_of(v.sill), df_neg(g)), df_of(inv_sill));
-}
-
 __device__ __forceinline__ DF shfl_xor_df(DF v, int o) {
     return {__shfl_xor_sync(FULL_MASK, v.hi, o), __shfl_xor_sync(FULL_MASK, v.lo, o)};
 }

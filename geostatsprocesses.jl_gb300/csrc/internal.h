@@ -341,8 +341,6 @@ cudaError_t launch_rows_to_out_fp64(const double* V, int64_t N, int R, int Rp, d
 // sigma of P positions (node, m, idx and off are shared with the source)
 cudaError_t launch_tables_to_fp64(const SweepTables<float>& src, SweepTables<double>& dst, int64_t P,
                                   int64_t entries, cudaStream_t s);
-cudaError_t launch_cov_df_check(const VarioDev& v, int dim, double inv_sill, const double* lags, int64_t n,
-                                double* c64, double* cdf, cudaStream_t s);
 cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2, cudaStream_t s);
 // learned warm start (learned.cu)
 cudaError_t launch_nn_features(const GridDev& G, const VarioDev& v, const int32_t* nbr, const int32_t* cnt, int k,

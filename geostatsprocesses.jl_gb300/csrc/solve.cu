@@ -377,23 +377,6 @@ struct Smem32 {
 // packed lower-triangle index of entry (i, j) of a symmetric matrix
 __device__ __forceinline__ int tri(int i, int j) { return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
 
-// normalized covariance between two points in double-FP32 arithmetic: the
-// lag in FP64 (exact grid and data coordinates), the model in double-FP32,
-// which keeps the FP32 solve off the narrow FP64 pipe.  Out of line: it is
-// called from several fill loops, and inlined copies of the polynomial
-// would multiply the kernel's code size
-__device__ __noinline__ DF kcov_df(const SolveArgs& a, NbInfo p, NbInfo q) {
-    const GridDev& G = a.grid;
-    if (p.did < 0 && q.did < 0)
-        return cov_df_norm(a.vario, G.dim, dmul((double)(q.c0 - p.c0), G.spacing[0]),
-                           dmul((double)(q.c1 - p.c1), G.spacing[1]),
-                           G.dim == 3 ? dmul((double)(q.c2 - p.c2), G.spacing[2]) : 0.0, a.inv_sill);
-    double xp[3], xq[3];
-    point_of(a, p, xp);
-    point_of(a, q, xq);
-    return cov_df_norm(a.vario, G.dim, dsub(xq[0], xp[0]), dsub(xq[1], xp[1]), dsub(xq[2], xp[2]), a.inv_sill);
-}
-
 // normalized double-FP32 covariance between two points of the augmented set
 __device__ __forceinline__ DF kcov2n(const SolveArgs& a, const NbInfo& p, const NbInfo& q) {
     if (p.did < 0 && q.did < 0) {
@@ -405,9 +388,14 @@ __device__ __forceinline__ DF kcov2n(const SolveArgs& a, const NbInfo& p, const 
             return {v.x, v.y};
         }
     }
-    return kcov_df(a, p, q);
+    return df_from_double(kcov(a, p, q) * a.inv_sill);
 }
 
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return df_fast_two_sum(p, __fadd_rn(e, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
+}
 
 // One system (node g, sweep-table row pos) of the problem `a` with at most
 // NMAX neighbours, in this warp's shared-memory slot `base`.
@@ -516,7 +504,7 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     const int da = dl[item / n], q = item % n;
                     const NbInfo iq = info[q];
                     if (iq.did >= 0 && q > da) continue;  // data-data pair once
-                    K[tri(da, q)] = kcov_df(a, iq, info[da]);
+                    K[tri(da, q)] = df_from_double(kcov(a, iq, info[da]) * a.inv_sill);
                 }
             }
             __syncwarp();
@@ -962,25 +950,6 @@ __global__ void fill_lut_kernel(const GridDev G, const VarioDev v, const CovLut 
             c2[i] = make_float2(hi, (float)(cn - (double)hi));
         }
     }
-}
-
-// the model's normalized covariance at n lags (x, y, z rows) in FP64 and in
-// the double-FP32 arithmetic of the FP32 solve, for a comparison of the two
-__global__ void cov_df_check_kernel(const VarioDev v, int dim, double inv_sill, const double* __restrict__ lags,
-                                    int64_t n, double* __restrict__ c64, double* __restrict__ cdf) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double h0 = lags[3 * i], h1 = lags[3 * i + 1], h2 = dim == 3 ? lags[3 * i + 2] : 0.0;
-    c64[i] = cov_fp64(v, dim, h0, h1, h2) * inv_sill;
-    const DF d = cov_df_norm(v, dim, h0, h1, h2, inv_sill);
-    cdf[i] = (double)d.hi + (double)d.lo;
-}
-
-cudaError_t launch_cov_df_check(const VarioDev& v, int dim, double inv_sill, const double* lags, int64_t n,
-                                double* c64, double* cdf, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    cov_df_check_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(v, dim, inv_sill, lags, n, c64, cdf);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_fill_cov_lut(const GridDev& g, const VarioDev& v, CovLut lut, double* c64, float2* c2,

@@ -269,47 +269,6 @@ def test_level_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
     G.close()
 
 
-@pytest.mark.parametrize("model", ["sph", "exp", "gau", "nested2d", "nested3d"])
-def test_double_fp32_covariance_matches_fp64(model, geosgs_lib):
-    """The FP32 solve evaluates covariances involving a datum (and grid lags
-    outside the lag table) in double-FP32 arithmetic with its own exp; on the
-    device, at lags from zero through far beyond the ranges, they agree with
-    the FP64 model to 1e-13 (the covariance divided by the sill, at most 1)."""
-    import ctypes as C
-
-    from test_oracle import _nested_case
-
-    if model.startswith("nested"):
-        proc, grid, data, method = _nested_case("fp32", 3 if model == "nested3d" else 2)
-        p, keep = geosgs.build_problem(proc, grid, data, method)
-        dim = 3 if model == "nested3d" else 2
-    else:
-        wl = workloads.small(dim=3, n=12, nz=6, k=8, vario=model, nugget=0.1, ranges=(9.0, 5.0, 3.0),
-                             rotation=geosgs.RotZ(30.0), precision="fp32")
-        p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
-        dim = 3
-    G = geosgs.Plan(p, keep)
-    rng = np.random.default_rng(21)
-    scale = np.concatenate([np.zeros(1), 10.0 ** rng.uniform(-6, 2.5, 20000)])
-    u = rng.standard_normal((scale.size, 3))
-    lags = u / np.linalg.norm(u, axis=1, keepdims=True) * scale[:, None]
-    if dim == 2:
-        lags[:, 2] = 0.0
-    lags = np.ascontiguousarray(lags)
-    c64, cdf = np.empty(scale.size), np.empty(scale.size)
-    lib = G.lib
-    lib.sgs_selftest_cov_df.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double),
-                                        C.POINTER(C.c_double)]
-    dp = C.POINTER(C.c_double)
-    assert lib.sgs_selftest_cov_df(G.h, lags.ctypes.data_as(dp), scale.size, c64.ctypes.data_as(dp),
-                                   cdf.ctypes.data_as(dp)) == 0
-    G.close()
-    assert c64[0] == 1.0 and cdf[0] == 1.0
-    err = np.abs(cdf - c64)
-    print(f"{model}: max |df - fp64| = {err.max():.2e}, covariances {c64.min():.2e}..{c64.max():.2e}")
-    assert err.max() <= 1e-13
-
-
 def test_error_codes(geosgs_lib):
     from geosgs import _abi
 

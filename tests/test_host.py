@@ -31,13 +31,13 @@ def test_library_loads_and_exports_every_header_symbol():
 
 
 def test_diagnostic_exports_outside_the_header():
-    """The diagnostic self-tests are exported for the GPU tests but are
+    """The bounded-wait self-tests are exported for the GPU tests but are
     not part of the C ABI the header declares."""
     from geosgs import _build
 
     _build.build()
     lib = C.CDLL(_abi.LIB_PATH)
-    for name in ("sgs_selftest_bounded_wait", "sgs_selftest_levels_wait", "sgs_selftest_cov_df"):
+    for name in ("sgs_selftest_bounded_wait", "sgs_selftest_levels_wait"):
         assert hasattr(lib, name)
         assert name not in header_symbols()
 
