@@ -342,8 +342,7 @@ cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, 
 // packed 32 per pass.  Its FP32 copy is inverted in registers by the
 // Gauss-Jordan sweep operator (Goodnight 1979; no pivoting, which is stable
 // for symmetric positive definite matrices, and whose k-th pivot is the same
-// Schur complement a Cholesky factorization would test), two pivots a step
-// with paired FP32 FMAs (fma.rn.f32x2).  Every solve is then
+// Schur complement a Cholesky factorization would test).  Every solve is then
 // a lane-parallel matrix-vector product instead of a sequential triangular
 // solve.  The weights are refined against the double-FP32 LHS: the residual
 // r = c - K w is accumulated with compensated (Dot2) FP32 arithmetic, which
@@ -356,10 +355,7 @@ constexpr int SOLVE32_WARPS = 2;
 // resident blocks per SM the FP32 solve is compiled for: 6 x 2 warps at up to
 // 168 registers a thread fill the register file; systems of up to 64
 // neighbours hold two rows of 64 registers and get 4 blocks (255 registers)
-#ifndef SGS_SOLVE32_BLOCKS
-#define SGS_SOLVE32_BLOCKS 6
-#endif
-constexpr int solve32_min_blocks(int nmax) { return nmax > 48 ? 4 : SGS_SOLVE32_BLOCKS; }
+constexpr int solve32_min_blocks(int nmax) { return nmax > 48 ? 4 : 6; }
 
 template <int NMAX>
 struct Smem32 {
@@ -371,7 +367,7 @@ struct Smem32 {
     static constexpr size_t W = (size_t)NMAX * sizeof(DF);
     static constexpr int CB = NMAX > 32 ? 64 : 32;  // one entry per owned row
     static constexpr size_t V = (size_t)CB * sizeof(float);
-    static constexpr size_t COL = 4 * (size_t)CB * sizeof(float);  // two pivot rows, double-buffered
+    static constexpr size_t COL = 2 * (size_t)CB * sizeof(float);
     static constexpr size_t INFO = (size_t)NMAX * sizeof(NbInfo);
     static constexpr size_t LIN = (size_t)NMAX * sizeof(int);
     static constexpr size_t bytes = K + C + W + V + COL + INFO + LIN;
@@ -399,79 +395,6 @@ __device__ __forceinline__ DF df_mul(DF a, DF b) {
     const float p = __fmul_rn(a.hi, b.hi);
     const float e = __fmaf_rn(a.hi, b.hi, -p);
     return df_fast_two_sum(p, __fadd_rn(e, __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi))));
-}
-
-// Two floats in one 64-bit register (x in the low half), the operand form of
-// the paired FP32 instructions; R rows stay in this form through the sweep
-typedef unsigned long long f32x2;
-
-__device__ __forceinline__ f32x2 f2_pack(float x, float y) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_unpack(f32x2 v) {
-    float2 r;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
-    return r;
-}
-
-// d = a * b + c on both halves in one paired FP32 instruction
-__device__ __forceinline__ f32x2 ffma2(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
-// Coefficients of one row for a two-pivot sweep step, as the negated pairs
-// (-cf0, -cf0) and (-cf1, -cf1) of the update R_ij - cf0 R_kk,j - cf1 R_kk+1,j.
-// A non-pivot row takes cf = u = e P^-1 (e: its entries in the pivot
-// columns), which is also its new pair in the pivot columns; the pivot rows
-// take cf = I_row - P^-1_row, which leaves P^-1 R_p, and their new pair is
-// -P^-1_row (gj2_out).
-__device__ __forceinline__ void gj2_coef(int row, int kk, float2 e, float q00, float q01, float q11, f32x2& ma,
-                                         f32x2& mb) {
-    float c0, c1;
-    if (row == kk) {
-        c0 = __fsub_rn(1.0f, q00);
-        c1 = -q01;
-    } else if (row == kk + 1) {
-        c0 = -q01;
-        c1 = __fsub_rn(1.0f, q11);
-    } else {
-        c0 = __fmaf_rn(e.x, q00, __fmul_rn(e.y, q01));
-        c1 = __fmaf_rn(e.x, q01, __fmul_rn(e.y, q11));
-    }
-    ma = f2_pack(-c0, -c0);
-    mb = f2_pack(-c1, -c1);
-}
-
-__device__ __forceinline__ f32x2 gj2_out(int row, int kk, f32x2 ma, f32x2 mb, float q00, float q01, float q11) {
-    if (row == kk) return f2_pack(-q00, -q01);
-    if (row == kk + 1) return f2_pack(-q01, -q11);
-    return f2_pack(-f2_unpack(ma).x, -f2_unpack(mb).x);
-}
-
-// x0 = -(R0 v), x1 = -(R1 v) for the register-held -K^-1 rows and the vector
-// v in shared memory (NMAX entries, 16-byte aligned), two columns a paired FMA
-template <int NMAX, bool TWO>
-__device__ __forceinline__ void matvec2(const f32x2* R0, const f32x2* R1, const float* v, float& x0, float& x1) {
-    f32x2 a0 = 0ull, a1 = 0ull;  // (0.0f, 0.0f)
-    const ulonglong2* v2 = reinterpret_cast<const ulonglong2*>(v);
-#pragma unroll
-    for (int j4 = 0; j4 < NMAX / 4; ++j4) {
-        const ulonglong2 u = v2[j4];
-        a0 = ffma2(R0[2 * j4], u.x, a0);
-        a0 = ffma2(R0[2 * j4 + 1], u.y, a0);
-        if (TWO) {
-            a1 = ffma2(R1[TWO ? 2 * j4 : 0], u.x, a1);
-            a1 = ffma2(R1[TWO ? 2 * j4 + 1 : 0], u.y, a1);
-        }
-    }
-    const float2 s0 = f2_unpack(a0), s1 = f2_unpack(a1);
-    x0 = -__fadd_rn(s0.x, s0.y);
-    x1 = TWO ? -__fadd_rn(s1.x, s1.y) : 0.0f;
 }
 
 // One system (node g, sweep-table row pos) of the problem `a` with at most
@@ -586,92 +509,64 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
             }
             __syncwarp();
             // ---- rows of the FP32 LHS into registers (identity padding) ----
-            // pair q of R0 (R1) holds columns 2q and 2q + 1 of row i0 (i1), so
-            // the sweep below updates two columns per paired FMA
-            f32x2 R0[NMAX / 2], R1[TWO ? NMAX / 2 : 1];
+            float R0[NMAX], R1[TWO ? NMAX : 1];
             const int t0 = i0 * (i0 + 1) / 2, t1 = i1 * (i1 + 1) / 2;  // own rows' starts
-            auto lhs = [&](int i, int ti, int j) {
-                return (i < n && j < n) ? K[j <= i ? ti + j : j * (j + 1) / 2 + i].hi : (i == j ? 1.0f : 0.0f);
-            };
 #pragma unroll
-            for (int q = 0; q < NMAX / 2; ++q) {
-                R0[q] = f2_pack(lhs(i0, t0, 2 * q), lhs(i0, t0, 2 * q + 1));
-                if (TWO) R1[TWO ? q : 0] = f2_pack(lhs(i1, t1, 2 * q), lhs(i1, t1, 2 * q + 1));
+            for (int j = 0; j < NMAX; ++j) {
+                R0[j] = (i0 < n && j < n) ? K[j <= i0 ? t0 + j : j * (j + 1) / 2 + i0].hi : (i0 == j ? 1.0f : 0.0f);
+                if (TWO)
+                    R1[j] = (i1 < n && j < n) ? K[j <= i1 ? t1 + j : j * (j + 1) / 2 + i1].hi : (i1 == j ? 1.0f : 0.0f);
             }
-            // ---- Gauss-Jordan sweep, two pivots a step: R -> -K^-1 ----
-            // At step kk (even) pair q holds columns (kk + 2q, kk + 2q + 1) mod
-            // NMAX, so the pivot columns kk, kk + 1 are always pair 0 and every
-            // register index is static in a rolled loop (a fully unrolled sweep
-            // overflows the instruction cache).  A step sweeps the 2x2 pivot
-            // block P at once, the block form of the sweep operator: P -> -P^-1,
-            // pivot columns R_ip -> R_ip P^-1, pivot rows R_pj -> P^-1 R_pj, the
-            // rest R_ij -> R_ij - R_ip P^-1 R_pj; its two scalar pivots, p00 and
-            // p11 - p01^2 / p00, are the ones two single steps would take and
-            // get the same test.  The pivot rows are broadcast through shared
-            // memory already rotated (slot j <- the pivot-column entries of row
-            // (kk + j + 2) mod NMAX, by symmetry the pivot rows' entries for
-            // register j + 2).  NMAX / 2 steps bring the columns back in place;
-            // padding pivots are exactly 1.
+            // ---- Gauss-Jordan sweep with column rotation: R -> -K^-1 ----
+            // At step kk register j holds column (kk + j) mod NMAX, so the pivot
+            // column is always register 0 and every register index is static
+            // in a rolled loop (a fully unrolled sweep overflows the
+            // instruction cache).  The pivot column is broadcast through shared
+            // memory already rotated (slot j <- row (kk + j + 1) mod NMAX, which
+            // by symmetry is row kk's entry for register j + 1).  NMAX steps
+            // bring the columns back in place; padding pivots are exactly 1.
             bool ok = true;
             const bool own0 = i0 < NMAX, own1 = TWO && i1 < NMAX;
 #pragma unroll 1
-            for (int kk = 0; kk < NMAX; kk += 2) {
-                float* cb0 = colb + ((kk >> 1) & 1) * 2 * S::CB;  // double-buffered
-                float* cb1 = cb0 + S::CB;
-                if (own0) {
-                    int p = i0 - kk - 2;
-                    p = p < 0 ? p + NMAX : p;
-                    const float2 e = f2_unpack(R0[0]);
-                    cb0[p] = e.x;
-                    cb1[p] = e.y;
-                }
-                if (own1) {
-                    int p = i1 - kk - 2;
-                    p = p < 0 ? p + NMAX : p;
-                    const float2 e = f2_unpack(R1[0]);
-                    cb0[p] = e.x;
-                    cb1[p] = e.y;
-                }
-                __syncwarp();
-                const float p00 = cb0[NMAX - 2], p01 = cb0[NMAX - 1], p11 = cb1[NMAX - 1];
-                if (!(p00 > 1e-3f)) {  // warp-uniform
+            for (int kk = 0; kk < NMAX; ++kk) {
+                const float d = __shfl_sync(FULL_MASK, kk < 32 ? R0[0] : R1[0], kk & 31);
+                if (!(d > 1e-3f)) {  // warp-uniform
                     ok = false;
                     break;
                 }
                 // the inverse is a preconditioner only: the approximate
                 // reciprocal (pivots lie in (1e-3, 1], no denormals) is enough
-                float i00, is;
-                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(i00) : "f"(p00));
-                const float t = __fmul_rn(p01, i00);
-                const float sc = __fmaf_rn(-t, p01, p11);
-                if (!(sc > 1e-3f)) {
-                    ok = false;
-                    break;
+                float inv;
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(d));
+                float* cb = colb + (kk & 1) * S::CB;
+                if (own0) {
+                    int p = i0 - kk - 1;
+                    cb[p < 0 ? p + NMAX : p] = R0[0];
                 }
-                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(is) : "f"(sc));
-                // P^-1 = [[q00, q01], [q01, q11]]
-                const float ts = __fmul_rn(t, is);
-                const float q00 = __fmaf_rn(ts, t, i00), q01 = -ts, q11 = is;
-                f32x2 ma0, mb0, ma1 = 0ull, mb1 = 0ull;
-                gj2_coef(i0, kk, f2_unpack(R0[0]), q00, q01, q11, ma0, mb0);
-                if (TWO) gj2_coef(i1, kk, f2_unpack(R1[0]), q00, q01, q11, ma1, mb1);
-                const ulonglong2* u2 = reinterpret_cast<const ulonglong2*>(cb0);  // 16-byte aligned
-                const ulonglong2* v2 = reinterpret_cast<const ulonglong2*>(cb1);
+                if (own1) {
+                    int p = i1 - kk - 1;
+                    cb[p < 0 ? p + NMAX : p] = R1[0];
+                }
+                __syncwarp();
+                // owner row: A[k][j] / d == A[k][j] - (1 - 1/d) A[k][j]
+                const float a0 = i0 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R0[0], inv);
+                const float a1 = TWO ? (i1 == kk ? __fsub_rn(1.0f, inv) : __fmul_rn(R1[0], inv)) : 0.0f;
+                const float4* cb4 = reinterpret_cast<const float4*>(cb);  // 16-byte aligned
 #pragma unroll
                 for (int j4 = 0; j4 < NMAX / 4; ++j4) {
-                    const ulonglong2 u = u2[j4], v = v2[j4];
-                    const int qa = 2 * j4, qb = 2 * j4 + 1;  // new pairs from slots 4 j4 .. 4 j4 + 3
-                    if (qa < NMAX / 2 - 1) {
-                        R0[qa] = ffma2(mb0, v.x, ffma2(ma0, u.x, R0[qa + 1]));
-                        if (TWO) R1[TWO ? qa : 0] = ffma2(mb1, v.x, ffma2(ma1, u.x, R1[TWO ? qa + 1 : 0]));
-                    }
-                    if (qb < NMAX / 2 - 1) {
-                        R0[qb] = ffma2(mb0, v.y, ffma2(ma0, u.y, R0[qb + 1]));
-                        if (TWO) R1[TWO ? qb : 0] = ffma2(mb1, v.y, ffma2(ma1, u.y, R1[TWO ? qb + 1 : 0]));
+                    const float4 v = cb4[j4];
+                    const float akv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int j = 4 * j4 + t;
+                        if (j < NMAX - 1) {
+                            R0[j] = __fmaf_rn(-a0, akv[t], R0[j + 1]);
+                            if (TWO) R1[TWO ? j : 0] = __fmaf_rn(-a1, akv[t], R1[TWO ? j + 1 : 0]);
+                        }
                     }
                 }
-                R0[NMAX / 2 - 1] = gj2_out(i0, kk, ma0, mb0, q00, q01, q11);
-                if (TWO) R1[TWO ? NMAX / 2 - 1 : 0] = gj2_out(i1, kk, ma1, mb1, q00, q01, q11);
+                R0[NMAX - 1] = i0 == kk ? -inv : a0;
+                if (TWO) R1[TWO ? NMAX - 1 : 0] = i1 == kk ? -inv : a1;
             }
             bool accept = ok;
             if (accept) {
@@ -685,7 +580,12 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     // w = K^-1 c = -R c
                     for (int q = lane; q < S::CB; q += 32) vec[q] = q < n ? c[q].hi : 0.0f;
                     __syncwarp();
-                    matvec2<NMAX, TWO>(R0, R1, vec, s0, s1);
+#pragma unroll
+                    for (int j = 0; j < NMAX; ++j) {
+                        const float v = vec[j];
+                        s0 = __fmaf_rn(-R0[j], v, s0);
+                        if (TWO) s1 = __fmaf_rn(-R1[j], v, s1);
+                    }
                 }
                 DF w0 = {s0, 0.0f}, w1 = {s1, 0.0f};
                 if (i0 < n) w[i0] = w0;
@@ -739,8 +639,13 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                     vec[i0] = r0;
                     if (TWO) vec[i1] = r1;
                     __syncwarp();
-                    float d0, d1;
-                    matvec2<NMAX, TWO>(R0, R1, vec, d0, d1);
+                    float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < NMAX; ++j) {
+                        const float v = vec[j];
+                        d0 = __fmaf_rn(-R0[j], v, d0);
+                        if (TWO) d1 = __fmaf_rn(-R1[j], v, d1);
+                    }
                     float dmax = 0.0f;
                     sd0 = i0 < n ? d0 : 0.0f;
                     sd1 = TWO && i1 < n ? d1 : 0.0f;
