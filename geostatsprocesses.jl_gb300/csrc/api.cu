@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -141,10 +142,10 @@ int dalloc(sgs_plan* p, T** out, size_t count) {
     *out = nullptr;
     if (count == 0) count = 1;
     void* ptr = nullptr;
-    cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+    cudaError_t e = pool_alloc(&ptr, count * sizeof(T), p->device);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return set_err(p, SGS_ERR_OOM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) + " bytes failed");
+        return set_err(p, SGS_ERR_OOM, std::string("allocation of ") + std::to_string(count * sizeof(T)) + " bytes failed");
     }
     p->bufs.push_back({ptr, count * sizeof(T)});
     *out = static_cast<T*>(ptr);
@@ -155,7 +156,7 @@ void dfree(sgs_plan* p, void* ptr) {
     if (!ptr) return;
     for (size_t i = 0; i < p->bufs.size(); ++i)
         if (p->bufs[i].p == ptr) {
-            cudaFree(ptr);
+            pool_free(ptr, p->stream);
             p->bufs.erase(p->bufs.begin() + i);
             return;
         }
@@ -234,6 +235,91 @@ int upload(sgs_plan* p, T** d, const T* h, size_t count) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// device memory pool (one per device, created on first use)
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+cudaStream_t g_alloc_stream[kMaxDevices] = {};
+
+cudaError_t device_pool(int device, cudaMemPool_t* pool, cudaStream_t* as) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pool[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t mp = nullptr;
+        cudaError_t e = cudaMemPoolCreate(&mp, &props);
+        if (e != cudaSuccess) return e;
+        // keep freed memory for the next plan (a plan's buffers are GBs, and
+        // mapping them anew each time costs milliseconds)
+        uint64_t keep = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+        cudaStream_t st = nullptr;
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(mp);
+            return e;
+        }
+        g_pool[device] = mp;
+        g_alloc_stream[device] = st;
+    }
+    *pool = g_pool[device];
+    *as = g_alloc_stream[device];
+    return cudaSuccess;
+}
+}  // namespace
+
+// Allocations run on a stream of their own that never carries kernels, and
+// are waited for, so the memory is usable on any stream on return.  One
+// retry after returning the pool's idle memory to the device.
+cudaError_t sgs::pool_alloc(void** ptr, size_t bytes, int device) {
+    *ptr = nullptr;
+    cudaMemPool_t mp;
+    cudaStream_t as;
+    cudaError_t e = device_pool(device, &mp, &as);
+    if (e != cudaSuccess) return e;
+    e = cudaMallocFromPoolAsync(ptr, bytes, mp, as);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        cudaStreamSynchronize(as);
+        cudaMemPoolTrimTo(mp, 0);
+        e = cudaMallocFromPoolAsync(ptr, bytes, mp, as);
+    }
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return e;
+    }
+    e = cudaStreamSynchronize(as);
+    if (e != cudaSuccess) *ptr = nullptr;
+    return e;
+}
+
+cudaError_t sgs::pool_free(void* ptr, cudaStream_t stream) {
+    return ptr ? cudaFreeAsync(ptr, stream) : cudaSuccess;
+}
+
+extern "C" int sgs_trim_memory(int32_t device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return SGS_ERR_CUDA;
+    }
+    if (device >= n || device >= kMaxDevices) return SGS_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (int d = device < 0 ? 0 : device; d < (device < 0 ? std::min(n, kMaxDevices) : device + 1); ++d) {
+        if (!g_pool[d]) continue;
+        if (cudaSetDevice(d) != cudaSuccess || cudaStreamSynchronize(g_alloc_stream[d]) != cudaSuccess ||
+            cudaMemPoolTrimTo(g_pool[d], 0) != cudaSuccess) {
+            cudaGetLastError();
+            return SGS_ERR_CUDA;
+        }
+    }
+    return SGS_OK;
+}
+
 void sgs::set_thread_error(const char* msg) { g_create_err = msg; }
 
 extern "C" const char* sgs_version(void) { return "geosgs 0.1.0 (sm_103a)"; }
@@ -335,8 +421,12 @@ extern "C" const char* sgs_last_error(const sgs_plan* plan) {
 extern "C" void sgs_plan_destroy(sgs_plan* p) {
     if (!p) return;
     cudaSetDevice(p->device);
+    // the plan's buffers may still be read by work the caller queued on its
+    // own streams (the device-pointer entry points): wait for the device, as
+    // a synchronous free would
+    cudaDeviceSynchronize();
+    for (auto& b : p->bufs) pool_free(b.p, p->stream);
     if (p->stream) cudaStreamSynchronize(p->stream);
-    for (auto& b : p->bufs) cudaFree(b.p);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
     if (p->stream) cudaStreamDestroy(p->stream);

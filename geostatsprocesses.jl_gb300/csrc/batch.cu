@@ -433,12 +433,12 @@ int balloc(sgs_batch* b, T** out, size_t count) {
     *out = nullptr;
     if (count == 0) count = 1;
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e = pool_alloc(&p, count * sizeof(T), b->device);
     if (e != cudaSuccess) {
         cudaGetLastError();
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
-        return berr(b, SGS_ERR_OOM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed (" +
+        return berr(b, SGS_ERR_OOM, "allocation of " + std::to_string(count * sizeof(T)) + " bytes failed (" +
                                         std::to_string(fr) + " bytes free): split the batch");
     }
     b->bufs.push_back({p, count * sizeof(T)});
@@ -451,7 +451,7 @@ void bfree(sgs_batch* b, void* p) {
     if (!p) return;
     for (size_t i = 0; i < b->bufs.size(); ++i)
         if (b->bufs[i].p == p) {
-            cudaFree(p);
+            pool_free(p, b->stream);
             b->info.device_bytes -= (int64_t)b->bufs[i].bytes;
             b->bufs.erase(b->bufs.begin() + i);
             return;
@@ -525,10 +525,14 @@ extern "C" const char* sgs_batch_last_error(const sgs_batch* b) {
 extern "C" void sgs_batch_destroy(sgs_batch* b) {
     if (!b) return;
     cudaSetDevice(b->device);
-    if (b->stream) cudaStreamSynchronize(b->stream);
+    // buffers may still be read by work queued on the caller's streams (the
+    // device-pointer entry points): wait for the device, as a synchronous
+    // free would
+    cudaDeviceSynchronize();
     if (b->prep_exec) cudaGraphExecDestroy(b->prep_exec);
     if (b->sweep_exec) cudaGraphExecDestroy(b->sweep_exec);
-    for (auto& x : b->bufs) cudaFree(x.p);
+    for (auto& x : b->bufs) pool_free(x.p, b->stream);
+    if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->h_seed) cudaFreeHost(b->h_seed);
     for (auto& e : b->ev)
         if (e) cudaEventDestroy(e);

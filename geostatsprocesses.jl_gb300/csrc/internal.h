@@ -280,6 +280,13 @@ inline double* pinned_device_view(double* host) {
 }
 
 // Message returned by sgs_last_error(NULL) on this host thread.
+// Device memory of plans and batches comes from one stream-ordered pool per
+// device that keeps freed memory for the next plan instead of returning it
+// (sgs_trim_memory returns it).  pool_alloc: usable on every stream when it
+// returns; pool_free: ordered after the work already queued on `stream`.
+cudaError_t pool_alloc(void** ptr, size_t bytes, int device);
+cudaError_t pool_free(void* ptr, cudaStream_t stream);
+
 void set_thread_error(const char* msg);
 inline void set_thread_error(const std::string& msg) { set_thread_error(msg.c_str()); }
 

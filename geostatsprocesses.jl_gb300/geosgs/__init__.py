@@ -6,7 +6,7 @@ Import with the package folder on sys.path:
     sys.path.insert(0, "<repo>/geostatsprocesses.jl_gb300")
     import geosgs
 """
-from ._abi import GeoSGSError, load_library
+from ._abi import GeoSGSError, load_library, trim_memory
 from .model import (
     ArgumentError,
     CartesianGrid,
@@ -40,6 +40,6 @@ __all__ = [
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "ExponentialTransiogram", "GaussianTransiogram", "IndicatorProcess", "SphericalTransiogram",
     "LinearCoregionalization", "LinearPath", "MetricBall", "NestedVariogram", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
-    "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library",
+    "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library", "trim_memory",
     "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

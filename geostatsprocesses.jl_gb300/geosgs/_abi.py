@@ -178,6 +178,7 @@ EXPORTS = (
     "sgs_plan_levels",
     "sgs_plan_info",
     "sgs_plan_destroy",
+    "sgs_trim_memory",
     "sgs_last_error",
     "sgs_version",
     "sgs_plan_features_device",
@@ -214,6 +215,14 @@ EXPORTS = (
 _lib = None
 
 
+def trim_memory(device: int = -1) -> None:
+    """Return the device memory the library keeps for reuse (freed by
+    destroyed plans and batches) to the device; device < 0: every device."""
+    rc = load_library().sgs_trim_memory(int(device))
+    if rc != 0:
+        raise GeoSGSError(rc, "sgs_trim_memory failed")
+
+
 class GeoSGSError(RuntimeError):
     """A libgeosgs call returned a negative status."""
 
@@ -244,6 +253,8 @@ def _declare(lib):
     lib.sgs_plan_info.restype = C.c_int
     lib.sgs_plan_destroy.argtypes = [P]
     lib.sgs_plan_destroy.restype = None
+    lib.sgs_trim_memory.argtypes = [C.c_int32]
+    lib.sgs_trim_memory.restype = C.c_int
     lib.sgs_last_error.argtypes = [P]
     lib.sgs_last_error.restype = C.c_char_p
     lib.sgs_version.argtypes = []

@@ -217,8 +217,16 @@ int sgs_plan_levels(sgs_plan* plan, int32_t* level, int32_t* nlevels);
 /* Plan statistics and last device timings. */
 int sgs_plan_info(const sgs_plan* plan, sgs_info* info);
 
-/* Release all device memory of the plan.  NULL is ignored. */
+/* Release all device memory of the plan (waits for the device first, as a
+ * synchronous free does).  NULL is ignored.  The memory returns to the
+ * library's pool for the device, where the next plan or batch reuses it;
+ * sgs_trim_memory hands it back to the device. */
 void sgs_plan_destroy(sgs_plan* plan);
+
+/* Return the device memory the library keeps for reuse (freed by destroyed
+ * plans and batches, or between simulate calls) to `device`, or to every
+ * device when device < 0.  Memory of live plans is not touched. */
+int sgs_trim_memory(int32_t device);
 
 /* Message of the last failure on this plan, or of the last failed
  * sgs_plan_create on this thread when plan is NULL. */

@@ -269,6 +269,33 @@ def test_level_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
     G.close()
 
 
+def test_device_memory_pool_reuse_and_trim(geosgs_lib):
+    """Plans draw device memory from the library's pool: a destroyed plan's
+    memory stays with the pool (device free memory does not come back), the
+    next plan of the same size reuses it (free memory does not drop again),
+    values are unchanged, and sgs_trim_memory returns it to the device."""
+    torch = pytest.importorskip("torch")
+    wl = workloads.c3("fp32", nreals=16, dims=(80, 80, 40), ndata=400)
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    geosgs.trim_memory(-1)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    outs, frees = [], []
+    for _ in range(2):
+        G = geosgs.Plan(p, keep).prepare()
+        outs.append(G.simulate(16, seed=5))
+        G.close()
+        torch.cuda.synchronize()
+        frees.append(torch.cuda.mem_get_info()[0])
+    np.testing.assert_array_equal(outs[0], outs[1])
+    MB = 1 << 20
+    assert frees[0] < free0 - 64 * MB  # kept by the pool
+    assert abs(frees[1] - frees[0]) <= 64 * MB  # reused, not mapped again
+    geosgs.trim_memory(0)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free0 - 64 * MB
+
+
 def test_error_codes(geosgs_lib):
     from geosgs import _abi
 
