@@ -768,6 +768,23 @@ def main():
     solve_roofline["nominal_peak"] = fp32_nominal
     solve_roofline["gj_pattern_peak"] = probes.get("gj_pattern_tflops")
 
+    # the search (kernel a) on the survey's byte basis: a path-rank read (4 B)
+    # per grid candidate examined (earlier path nodes tested by the first
+    # ranks, template offsets inside the grid), the FP32 coordinates (16 B) of
+    # every datum screened, and the row written (k int32 slots, count and
+    # grid count); the candidates are counted by the kernel
+    kk = int(inf.maxneighbors)
+    s_bytes = (4 * int(inf.search_grid_candidates) + 16 * int(inf.search_data_candidates)
+               + N * (4 * kk + 8))
+    s_gbs = s_bytes / (head["ms_search"] * 1e-3) / 1e9
+    search_roofline = {"kernel": "search_kernel: one search", "bound": "hbm", "achieved": s_gbs, "peak": peak,
+                       "unit": "GB/s", "frac": s_gbs / peak, "peak_source": peak_src, "algorithmic_bytes": s_bytes,
+                       "grid_candidates": int(inf.search_grid_candidates),
+                       "data_candidates": int(inf.search_data_candidates),
+                       "basis": "4 B per grid candidate + 16 B per datum screened + (4k + 8) B per node written",
+                       "note": "latency bound: the rank gathers hit L2 (profiles/kernels_c3_200x200x50_fp32.md)",
+                       "ms": head["ms_search"]}
+
     cpu = None
     if not args.no_cpu:
         v, cores, sample, _ = cpu_sample(wl, args.cpu_nodes)
@@ -793,6 +810,7 @@ def main():
         "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
         "roofline": roofline,
         "solve_roofline": solve_roofline,
+        "search_roofline": search_roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(head["launches"]) // max(1, args.steps),

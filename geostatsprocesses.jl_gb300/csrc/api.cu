@@ -76,6 +76,7 @@ struct sgs_plan {
     bool prepared = false;
     bool sweep_timed = false;     // ev[5]/ev[6] bracket the last sweep
     unsigned long long* d_sum_m = nullptr;
+    unsigned long long* d_stats = nullptr;  // [3] search candidates (grid, data), prior nodes
     float* d_nn = nullptr;        // warm-start network parameters
     float* d_winit = nullptr;     // warm-start predictions [N][k]
     int32_t* d_done = nullptr;    // dataflow sweep: per-node epoch flags
@@ -892,6 +893,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         if ((rc = dalloc(P, &P->d_status, N))) return rc;
         if ((rc = dalloc(P, &P->d_scratch, 16))) return rc;
         if ((rc = dalloc(P, &P->d_sum_m, 1))) return rc;
+        if ((rc = dalloc(P, &P->d_stats, 3))) return rc;
         if ((rc = dalloc(P, &P->d_wl1, 1))) return rc;
     }
     cudaStream_t st = P->stream;
@@ -922,6 +924,8 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     sa.cnt = P->d_cnt;
     sa.ngrid = P->d_ngrid;
     sa.data_only = P->data_only;
+    sa.scanned = P->d_stats;
+    CK(P, cudaMemsetAsync(P->d_stats, 0, 3 * sizeof(unsigned long long), st));
     CK(P, cudaEventRecord(P->ev[0], st));
     LAUNCH(P, 1, launch_search(sa, st));
     CK(P, cudaEventRecord(P->ev[1], st));
@@ -1058,6 +1062,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         LAUNCH(P, 1, launch_cok_solve(s, cok_args(P), st));
     }
     CK(P, cudaEventRecord(P->ev[4], st));
+    LAUNCH(P, 1, launch_count_nonzero(N, P->d_status, P->d_stats + 2, P->nsm, st));
     CK(P, cudaStreamSynchronize(st));
     dfree(P, d_lcount);
     dfree(P, d_lfill);
@@ -1066,14 +1071,13 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     P->info.ms_solve = elapsed(P->ev[3], P->ev[4]);
     P->info.nlevels = P->nlevels;
     {
-        std::vector<int8_t> st8(N);
-        CK(P, cudaMemcpy(st8.data(), P->d_status, N, cudaMemcpyDeviceToHost));
-        unsigned long long sm = 0;
+        unsigned long long sm = 0, stats[3] = {0, 0, 0};
         CK(P, cudaMemcpy(&sm, P->d_sum_m, sizeof(sm), cudaMemcpyDeviceToHost));
-        P->info.d2h_bytes += N + sizeof(sm);
-        int64_t np = 0;
-        for (int64_t i = 0; i < N; ++i) np += st8[i] != 0;
-        P->info.n_prior = np;
+        CK(P, cudaMemcpy(stats, P->d_stats, sizeof(stats), cudaMemcpyDeviceToHost));
+        P->info.d2h_bytes += sizeof(sm) + sizeof(stats);
+        P->info.search_grid_candidates = (int64_t)stats[0];
+        P->info.search_data_candidates = (int64_t)stats[1];
+        P->info.n_prior = (int64_t)stats[2];
         P->info.sum_grid_neighbors = (int64_t)sm;
     }
     P->prepared = true;

@@ -301,6 +301,12 @@ __global__ void count_nonzero_kernel(int64_t n, const int8_t* __restrict__ v, un
     if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
 
+cudaError_t launch_count_nonzero(int64_t n, const int8_t* v, unsigned long long* out, int nsm, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    count_nonzero_kernel<<<nsm * 4, 256, 0, s>>>(n, v, out);
+    return cudaGetLastError();
+}
+
 }  // namespace sgs
 
 // ---------------------------------------------------------------------------

@@ -101,6 +101,11 @@ struct SearchArgs {
     int32_t* cnt;                // N
     int32_t* ngrid;              // N: grid neighbours among them
     int data_only;               // 1: data candidates only (kriging from the data)
+    // optional [2] (single-problem search only): candidates examined (grid:
+    // earlier path nodes tested by the early ranks and template entries
+    // inside the grid, each one path rank read; data: bucket entries
+    // screened), summed once per warp
+    unsigned long long* scanned;
 };
 
 // Longest wait of the dependency-level kernels for one neighbour's level.
@@ -301,6 +306,8 @@ cudaError_t launch_solve_fp64_into_fp32(const SolveArgs& a, const SweepTables<fl
 // batches of domains (doms: device descriptors, noff: ndom + 1 global node
 // offsets, order: level-ordered global node ids; the positions to solve are
 // list[desc[1] .. desc[1] + desc[0]), desc on the device)
+// *out += the number of nonzero entries of v[0, n) (device counter)
+cudaError_t launch_count_nonzero(int64_t n, const int8_t* v, unsigned long long* out, int nsm, cudaStream_t s);
 cudaError_t launch_search_batch(const SearchArgs* doms, const int64_t* noff, int ndom, int64_t total, int nsm,
                                 cudaStream_t s);
 cudaError_t launch_solve_fp32_batch(int nmax, const SolveArgs* doms, const int64_t* noff, int ndom,

@@ -75,8 +75,11 @@ struct SearchSmem {
     int32_t* roff;    // [32] their offsets in the concatenated candidate list
 };
 
-// The neighbour row of node g of the problem described by `a`.
-__device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane, const SearchSmem& sm) {
+// The neighbour row of node g of the problem described by `a`; with COUNT,
+// adds the candidates it examined to ex_grid / ex_data (warp-uniform).
+template <bool COUNT>
+__device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane, const SearchSmem& sm,
+                                            unsigned long long& ex_grid, unsigned long long& ex_data) {
     long long* gd2 = sm.gd2;
     int32_t* gidx = sm.gidx;
     long long* dd2 = sm.dd2;
@@ -104,6 +107,7 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
             // kept by (d2, node id): the order of the template (d2, linear
             // offset), since for a fixed node the linear offset orders ids
             int nbuf = 0;
+            if (COUNT) ex_grid += (unsigned long long)t;
             for (int base = 0; base < t; base += 32) {
                 const int j = base + lane;
                 int c = 0, c0 = 0, c1 = 0, c2 = 0;
@@ -165,7 +169,10 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
             }
             int rk[SCAN_STEPS];
 #pragma unroll
-            for (int h = 0; h < SCAN_STEPS; ++h) rk[h] = in[h] ? a.rank[c[h]] : 0;
+            for (int h = 0; h < SCAN_STEPS; ++h) {
+                rk[h] = in[h] ? a.rank[c[h]] : 0;
+                if (COUNT) ex_grid += __popc(__ballot_sync(FULL_MASK, in[h]));
+            }
 #pragma unroll
             for (int h = 0; h < SCAN_STEPS; ++h) {
                 if (ng >= k) break;  // warp-uniform
@@ -287,6 +294,7 @@ __device__ __forceinline__ void search_node(const SearchArgs& a, int g, int lane
                     if (lane >= o) incl += y;
                 }
                 const int total = __shfl_sync(FULL_MASK, incl, 31);
+                if (COUNT) ex_data += (unsigned long long)total;
                 sm.rstart[lane] = rs;
                 sm.roff[lane] = incl - len;
                 __syncwarp();
@@ -382,8 +390,13 @@ __global__ void __launch_bounds__(SEARCH_WARPS * 32) search_kernel(const SearchA
     // Nodes go in id order, so the warps of a block take neighbouring cells
     // and share the rank and data cache lines they scan; the result of a
     // node depends only on its path rank, not on when it is processed.
+    unsigned long long ex_grid = 0, ex_data = 0;
     for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < a.grid.N; gg += nwarps)
-        search_node(a, (int)gg, lane, sm);
+        search_node<true>(a, (int)gg, lane, sm, ex_grid, ex_data);
+    if (a.scanned && lane == 0) {
+        atomicAdd(&a.scanned[0], ex_grid);
+        atomicAdd(&a.scanned[1], ex_data);
+    }
 }
 
 // Every node of a batch of domains: global node ids [noff[d], noff[d+1])
@@ -397,6 +410,7 @@ search_batch_kernel(const SearchArgs* __restrict__ doms, const int64_t* __restri
     const int64_t total = noff[ndom];
     const int64_t nwarps = (int64_t)gridDim.x * SEARCH_WARPS;
     int64_t lo = 0, hi = 0;
+    unsigned long long ex_grid = 0, ex_data = 0;  // not counted for batches
     for (int64_t gg = (int64_t)blockIdx.x * SEARCH_WARPS + wib; gg < total; gg += nwarps) {
         if (gg < lo || gg >= hi) {
             const int d = find_domain(noff, ndom, gg);
@@ -406,7 +420,7 @@ search_batch_kernel(const SearchArgs* __restrict__ doms, const int64_t* __restri
             warp_copy_struct(&s_dom[wib], &doms[d], lane);
             __syncwarp();
         }
-        search_node(s_dom[wib], (int)(gg - lo), lane, sm);
+        search_node<false>(s_dom[wib], (int)(gg - lo), lane, sm, ex_grid, ex_data);
     }
 }
 

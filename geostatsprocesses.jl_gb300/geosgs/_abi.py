@@ -134,6 +134,8 @@ class SgsInfo(C.Structure):
         ("weight_l1_max", C.c_double),
         ("values_fp64", C.c_int32),
         ("reserved", C.c_int32),
+        ("search_grid_candidates", C.c_int64),
+        ("search_data_candidates", C.c_int64),
     ]
 
 

@@ -159,6 +159,10 @@ typedef struct sgs_info {
                                  SGS_FP32_VALUE_L1_LIMIT); sgs_plan_simulate_device
                                  then takes double arrays                          */
     int32_t reserved;
+    int64_t search_grid_candidates; /* candidates the last search examined, each one
+                                       path-rank read: earlier path nodes tested by
+                                       the first ranks, template offsets inside the grid */
+    int64_t search_data_candidates; /* data bucket entries it screened */
 } sgs_info;
 
 /* SGS_PREC_FP32_REFINE stores values in FP32 while weight_l1_max stays below

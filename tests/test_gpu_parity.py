@@ -269,6 +269,28 @@ def test_level_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
     G.close()
 
 
+def test_search_candidate_counts(geosgs_lib):
+    """The search counts the candidates it examines (the byte basis of its
+    roofline): at least every neighbour it keeps, grid and data apart, and
+    the prior count read back from the device matches the status array."""
+    wl = workloads.small(dim=3, n=24, nz=8, k=16, ndata=30, vario="exp", ranges=(8.0, 5.0, 3.0),
+                         rotation=geosgs.RotZ(30.0), ball=geosgs.MetricBall((8.0, 5.0, 3.0), geosgs.RotZ(30.0)),
+                         precision="fp32")
+    p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+    G = gpu_plan(p, keep)
+    info = G.info()
+    idx, cnt = G.neighbors()
+    _, _, st = G.weights()
+    G.close()
+    rows = [idx[g, :cnt[g]] for g in range(idx.shape[0])]
+    n_grid = sum(int(np.sum(r < G.N)) for r in rows)
+    n_data = sum(int(np.sum(r >= G.N)) for r in rows)
+    assert n_grid > 0 and n_data > 0
+    assert info.search_grid_candidates >= n_grid
+    assert info.search_data_candidates >= n_data
+    assert info.n_prior == int(np.count_nonzero(st))
+
+
 def test_device_memory_pool_reuse_and_trim(geosgs_lib):
     """Plans draw device memory from the library's pool: a destroyed plan's
     memory stays with the pool (device free memory does not come back), the
