@@ -35,6 +35,11 @@ struct sgs_plan {
     int nsm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
+    // learned warm start: the prediction runs on a second stream, started
+    // right after the search, concurrently with the dependency levels
+    cudaStream_t pred_stream = nullptr;
+    cudaEvent_t pred_done = nullptr;
+    bool pred_pending = false;
     // problem
     GridDev grid{};
     MetricDev metric{};
@@ -137,6 +142,12 @@ int cuda_err(sgs_plan* p, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_err(plan, e_, #call); \
         (plan)->info.launches += (n);                        \
     } while (0)
+
+// plan scratch words: [0, 16) level-phase counters, flags and solve counters
+// (cleared together before the level kernels), kPredErr the prediction's
+// error flag
+constexpr int kPredErr = 16;
+constexpr int kScratchWords = 20;
 
 template <typename T>
 int dalloc(sgs_plan* p, T** out, size_t count) {
@@ -430,6 +441,8 @@ extern "C" void sgs_plan_destroy(sgs_plan* p) {
     if (p->stream) cudaStreamSynchronize(p->stream);
     for (auto& e : p->ev)
         if (e) cudaEventDestroy(e);
+    if (p->pred_done) cudaEventDestroy(p->pred_done);
+    if (p->pred_stream) cudaStreamDestroy(p->pred_stream);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }
@@ -778,12 +791,14 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 // Warm-start predictions [N][k] of the plan's network for every system: BF16
 // on the tensor cores (tcgen05) or FP32 on the CUDA cores.  The tensor-core
-// kernel's error flag is scratch[12] (read by the caller after a sync).
+// kernel's error flag is scratch[kPredErr] (read by the caller after a sync),
+// outside the words the level phase clears, since the prediction can run
+// beside it.
 static int run_predict(sgs_plan* P, float* out, bool tensor_cores, cudaStream_t st) {
     if (tensor_cores) {
-        CK(P, cudaMemsetAsync(P->d_scratch + 12, 0, sizeof(int32_t), st));
+        CK(P, cudaMemsetAsync(P->d_scratch + kPredErr, 0, sizeof(int32_t), st));
         LAUNCH(P, 1, launch_nn_predict_tc(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn, out,
-                                          P->d_scratch + 12, P->nsm, st));
+                                          P->d_scratch + kPredErr, P->nsm, st));
     } else {
         LAUNCH(P, 1, launch_nn_predict_plan(P->grid, P->vario, P->d_nbr, P->d_cnt, P->k, P->d_dxyz, P->d_nn, out,
                                             st));
@@ -833,11 +848,16 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     s.nfallback = nfb;
     unsigned long long* nwarm = reinterpret_cast<unsigned long long*>(P->d_scratch + 8);  // scratch[8..9]
     if (P->warm_start && P->d_nn) {
-        // learned warm start: predictions for every node, then the solve
-        // refines from them
+        // learned warm start: predictions for every node (launched after the
+        // search by sgs_plan_prepare, or here), then the solve refines from them
         int rc;
-        if (!P->d_winit && (rc = dalloc(P, &P->d_winit, (size_t)P->N * P->k))) return rc;
-        if ((rc = run_predict(P, P->d_winit, !(P->flags & SGS_FLAG_NN_FP32), P->stream))) return rc;
+        if (P->pred_pending) {
+            CK(P, cudaStreamWaitEvent(P->stream, P->pred_done, 0));
+            P->pred_pending = false;
+        } else {
+            if (!P->d_winit && (rc = dalloc(P, &P->d_winit, (size_t)P->N * P->k))) return rc;
+            if ((rc = run_predict(P, P->d_winit, !(P->flags & SGS_FLAG_NN_FP32), P->stream))) return rc;
+        }
         CK(P, cudaMemsetAsync(nwarm, 0, sizeof(unsigned long long), P->stream));
         s.w_init = P->d_winit;
         s.n_warm = nwarm;
@@ -855,7 +875,7 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
     CK(P, cudaMemcpyAsync(&h, nfb, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
     if (s.n_warm) CK(P, cudaMemcpyAsync(&hw, nwarm, sizeof(hw), cudaMemcpyDeviceToHost, P->stream));
     int32_t htc = 0;
-    if (s.n_warm) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + 12, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
+    if (s.n_warm) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + kPredErr, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
     CK(P, cudaStreamSynchronize(P->stream));
     P->info.d2h_bytes += sizeof(int32_t) + (s.n_warm ? sizeof(hw) + sizeof(htc) : 0);
     if (htc) return set_err(P, SGS_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait exceeded its bound");
@@ -891,7 +911,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         if ((rc = dalloc(P, &P->d_level, N))) return rc;
         if ((rc = dalloc(P, &P->d_order, N))) return rc;
         if ((rc = dalloc(P, &P->d_status, N))) return rc;
-        if ((rc = dalloc(P, &P->d_scratch, 16))) return rc;
+        if ((rc = dalloc(P, &P->d_scratch, kScratchWords))) return rc;
         if ((rc = dalloc(P, &P->d_sum_m, 1))) return rc;
         if ((rc = dalloc(P, &P->d_stats, 3))) return rc;
         if ((rc = dalloc(P, &P->d_wl1, 1))) return rc;
@@ -929,6 +949,18 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
     CK(P, cudaEventRecord(P->ev[0], st));
     LAUNCH(P, 1, launch_search(sa, st));
     CK(P, cudaEventRecord(P->ev[1], st));
+
+    // ---- learned warm start: predictions need only the neighbour rows, so
+    // they run beside the dependency levels on a second stream ----
+    if (P->warm_start && P->d_nn && P->precision != SGS_PREC_FP64) {
+        if (!P->pred_stream) CK(P, cudaStreamCreateWithFlags(&P->pred_stream, cudaStreamNonBlocking));
+        if (!P->pred_done) CK(P, cudaEventCreateWithFlags(&P->pred_done, cudaEventDisableTiming));
+        if (!P->d_winit && (rc = dalloc(P, &P->d_winit, (size_t)N * k))) return rc;
+        CK(P, cudaStreamWaitEvent(P->pred_stream, P->ev[1], 0));
+        if ((rc = run_predict(P, P->d_winit, !(P->flags & SGS_FLAG_NN_FP32), P->pred_stream))) return rc;
+        CK(P, cudaEventRecord(P->pred_done, P->pred_stream));
+        P->pred_pending = true;
+    }
 
     // ---- dependency levels and level order ----
     CK(P, cudaMemsetAsync(P->d_level, 0xff, N * sizeof(int32_t), st));
@@ -1587,7 +1619,7 @@ extern "C" int sgs_plan_predict_device(sgs_plan* P, float* out, int32_t tensor_c
     int rc;
     if ((rc = run_predict(P, out, tensor_cores != 0, st))) return rc;
     int32_t htc = 0;
-    if (tensor_cores) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + 12, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    if (tensor_cores) CK(P, cudaMemcpyAsync(&htc, P->d_scratch + kPredErr, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CK(P, cudaStreamSynchronize(st));
     if (htc) return set_err(P, SGS_ERR_TIMEOUT, "tensor-core inference: an MMA completion wait exceeded its bound");
     return SGS_OK;
