@@ -489,8 +489,11 @@ def time_batch(bw, args, torch, ws, precision):
     barrier(ws)
     ms = e0.elapsed_time(e1) / args.steps
     inf = B.info()
+    # nodes of the domains that keep FP64 values (the sweep's value rows are
+    # 8 bytes per realization there, 4 elsewhere)
+    n_fp64 = int(sum(int(B.sizes[d]) for d in range(len(B.sizes)) if B.domain_values_fp64(d)))
     res = dict(ms=max_over_ranks(ws, ms), launches=inf.launches - launches0, graphs=inf.graph_launches - graphs0,
-               info=inf, sweep_config=cfg, sweep_tried=tried, s_create=t_create,
+               info=inf, sweep_config=cfg, sweep_tried=tried, s_create=t_create, nodes_fp64=n_fp64,
                phases={k: statistics.mean(v) for k, v in ph.items()})
     B.close()
     del V
@@ -572,11 +575,12 @@ def main_batch(args, torch, ws, rank, uuid):
     inf = fast["info"]
     sum_m = int(inf.sum_grid_neighbors)
     Rp = (R + 3) // 4 * 4
-    # neighbour row reads + value writes (rows of Rp values), and per grid
-    # neighbour an int32 index and a (hi, lo) weight, per node its id, count,
-    # CSR row start, (hi, lo) b0 and sigma
-    sv = 8 if inf.values_fp64 else 4
-    alg_bytes = (sum_m + N) * Rp * sv + sum_m * 12 + N * 32
+    # neighbour row reads + value writes (rows of Rp values: 8-byte values in
+    # the domains that keep FP64, 4-byte elsewhere), and per grid neighbour an
+    # int32 index and a (hi, lo) weight, per node its id, count, CSR row
+    # start, (hi, lo) b0 and sigma
+    m64, n64 = int(inf.sum_grid_neighbors_fp64), int(fast["nodes_fp64"])
+    alg_bytes = (sum_m - m64 + N - n64) * Rp * 4 + (m64 + n64) * Rp * 8 + sum_m * 12 + N * 32
     try:
         peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
     except Exception:
@@ -600,9 +604,12 @@ def main_batch(args, torch, ws, rank, uuid):
         "n_fp64_fallback": int(inf.n_fp64_fallback), "bin_systems": [int(x) for x in inf.bin_systems],
         "device_gb": inf.device_bytes / 1e9, "s_create": round(fast["s_create"], 2),
         "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
-        "roofline": {"kernel": "sweep_flow_kernel<float, CSR> (one persistent dataflow launch)", "bound": "hbm",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": None, "algorithmic_bytes": alg_bytes, "ms": ms_sweep},
+        "roofline": {"kernel": ("sweep_flow_kernel<float / double, CSR> (one dataflow launch per value precision)"
+                                if 0 < n64 < N else
+                                "sweep_flow_kernel<%s, CSR> (one dataflow launch)" % ("double" if n64 else "float")),
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None, "algorithmic_bytes": alg_bytes,
+                     "nodes_fp64_values": n64, "ms": ms_sweep},
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(fast["launches"]) // max(1, args.steps),
         "graph_launches_per_step": fast["graphs"] / max(1, args.steps), "clocks": clk,
         "sweep_config": fast["sweep_config"],

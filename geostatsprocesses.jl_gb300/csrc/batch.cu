@@ -292,6 +292,18 @@ __global__ void sum_kernel(int64_t n, const int32_t* __restrict__ v, unsigned lo
     if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
 
+// *out += sum of m[p] over the table positions whose node has class 1 (its
+// domain keeps FP64 values)
+__global__ void sum_class_kernel(int64_t n, const int32_t* __restrict__ m, const int32_t* __restrict__ node,
+                                 const uint8_t* __restrict__ cls, unsigned long long* __restrict__ out) {
+    unsigned long long s = 0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+        if (cls[node[p]]) s += (unsigned long long)m[p];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
+}
+
 __global__ void count_nonzero_kernel(int64_t n, const int8_t* __restrict__ v, unsigned long long* __restrict__ out) {
     unsigned long long s = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -935,6 +947,21 @@ extern "C" int sgs_batch_prepare(sgs_batch* B) {
         }
         B->info.values_fp64 = values_fp64(B) ? 1 : 0;
         B->info.domains_fp64 = B->precision == SGS_PREC_FP64 ? B->ndom : nfp64;
+        // grid neighbours of the FP64-value domains' nodes (value traffic of
+        // the sweep per precision class)
+        if (B->mixed) {
+            BCK(B, cudaMemsetAsync(B->d_sums + 3, 0, sizeof(unsigned long long), st));
+            sum_class_kernel<<<B->nsm * 4, 256, 0, st>>>(B->Ntot, B->t32.m, B->t32.node, B->d_cls, B->d_sums + 3);
+            BCK(B, cudaGetLastError());
+            B->info.launches++;
+            unsigned long long s64 = 0;
+            BCK(B, cudaMemcpyAsync(&s64, B->d_sums + 3, sizeof(s64), cudaMemcpyDeviceToHost, st));
+            BCK(B, cudaStreamSynchronize(st));
+            B->info.d2h_bytes += sizeof(s64);
+            B->info.sum_grid_neighbors_fp64 = (int64_t)s64;
+        } else {
+            B->info.sum_grid_neighbors_fp64 = values_fp64(B) ? (int64_t)su[1] : 0;
+        }
     }
     B->info.nlevels = hs[0] + 1;
     B->info.sum_grid_neighbors = (int64_t)su[1];

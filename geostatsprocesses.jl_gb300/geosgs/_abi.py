@@ -162,6 +162,7 @@ class SgsBatchInfo(C.Structure):
         ("weight_l1_max", C.c_double),
         ("values_fp64", C.c_int32),
         ("domains_fp64", C.c_int32),
+        ("sum_grid_neighbors_fp64", C.c_int64),
     ]
 
 

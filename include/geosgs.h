@@ -364,6 +364,8 @@ typedef struct sgs_batch_info {
     int32_t domains_fp64;       /* domains whose values are FP64: with
                                    SGS_PREC_FP32_REFINE, only those whose weights
                                    exceed SGS_FP32_VALUE_L1_LIMIT                   */
+    int64_t sum_grid_neighbors_fp64; /* the part of sum_grid_neighbors that belongs
+                                   to the nodes of FP64-value domains              */
 } sgs_batch_info;
 
 /* Validate every problem (the first invalid one is named in the error) and

@@ -119,6 +119,17 @@ def test_batch_promotes_amplifying_weights(oracle_mod, geosgs_lib):
     assert info.values_fp64 == 1 and info.weight_l1_max > 10.0
     fp64 = [B.domain_values_fp64(d) for d in range(len(probs))]
     assert fp64[-1] and not all(fp64) and info.domains_fp64 == sum(fp64)
+    # the FP64 domains' share of the sweep's grid neighbours: the rows of
+    # every kriged node of those domains, from the neighbour tables
+    m64 = 0
+    for d in range(len(probs)):
+        if fp64[d]:
+            idx, cnt = B.neighbors(d)
+            _, _, st = B.weights(d)
+            n = int(B.sizes[d])
+            m64 += sum(int(np.sum(idx[g, :cnt[g]] < n)) for g in range(n) if st[g] == 0)
+    assert 0 < info.sum_grid_neighbors_fp64 < info.sum_grid_neighbors
+    assert info.sum_grid_neighbors_fp64 == m64
     R = bw.nreals
     zs = [np.random.default_rng(200 + d).standard_normal((R, int(B.sizes[d]))) for d in range(len(probs))]
     vals = B.simulate(R, z=zs)

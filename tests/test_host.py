@@ -86,7 +86,7 @@ int main(void){
    offsetof(sgs_problem, mean), offsetof(sgs_problem, ball), offsetof(sgs_problem, path),
    offsetof(sgs_problem, flags), sizeof(sgs_info), offsetof(sgs_info, ms_sweep),
    sizeof(sgs_sweep_config), offsetof(sgs_sweep_config, ms));
- printf("%zu\n", offsetof(sgs_info, search_data_candidates));
+ printf("%zu %zu\n", offsetof(sgs_info, search_data_candidates), offsetof(sgs_batch_info, sum_grid_neighbors_fp64));
  printf("%zu %zu %zu\n", sizeof(sgs_batch_info), offsetof(sgs_batch_info, ms_search),
    offsetof(sgs_batch_info, device_bytes));
  return 0;}
@@ -100,7 +100,7 @@ int main(void){
     P, I, W, B = _abi.SgsProblem, _abi.SgsInfo, _abi.SgsSweepConfig, _abi.SgsBatchInfo
     want = [C.sizeof(P), P.variogram.offset, P.mean.offset, P.ball.offset, P.path.offset, P.flags.offset,
             C.sizeof(I), I.ms_sweep.offset, C.sizeof(W), W.ms.offset, I.search_data_candidates.offset,
-            C.sizeof(B), B.ms_search.offset, B.device_bytes.offset]
+            B.sum_grid_neighbors_fp64.offset, C.sizeof(B), B.ms_search.offset, B.device_bytes.offset]
     assert got == want
 
 
