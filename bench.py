@@ -771,7 +771,8 @@ def main():
 
     head_steps = wlh.method.refine_steps + (1 if params is not None else 0)
     solve_roofline = solve_roof(head, head_steps, fp32_peak, fp32_src,
-                                "solve_fp32_kernel<NMAX> (+ lag table, prediction, FP64 fallbacks): one solve phase")
+                                "solve_fp32_kernel<NMAX> (+ lag table, the rest of the prediction, FP64 fallbacks): "
+                                "one solve phase")
     solve_roofline["nominal_peak"] = fp32_nominal
     solve_roofline["gj_pattern_peak"] = probes.get("gj_pattern_tflops")
 
@@ -797,8 +798,12 @@ def main():
         v, cores, sample, _ = cpu_sample(wl, args.cpu_nodes)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample, "extrapolated": True}
 
-    def phases(res, solve_key="solve"):
-        return {"search": res["ms_search"], "levels": res["ms_levels"], solve_key: res["ms_solve"],
+    def phases(res, learned=False):
+        # with the learned warm start the prediction runs on a second stream
+        # beside the dependency levels, and the solve waits for what is left
+        return {"search": res["ms_search"],
+                ("levels_beside_prediction" if learned else "levels"): res["ms_levels"],
+                ("solve_after_prediction" if learned else "solve"): res["ms_solve"],
                 "sweep": res["ms_sweep"]}
 
     value = ws * N * R / (head["ms"] * 1e-3)
@@ -811,7 +816,7 @@ def main():
         "arm": {"form": "learned warm start + FP32" if params is not None else "FP32",
                 "precision": "FP32 Gauss-Jordan inverse + double-FP32 refinement, FP64 Cholesky fallback",
                 "warm_start": params is not None, "refine_steps": head_steps},
-        "phases_ms": phases(head, "solve_incl_prediction" if params is not None else "solve"),
+        "phases_ms": phases(head, params is not None),
         "nlevels": int(inf.nlevels), "n_prior": int(inf.n_prior), "n_fp64_fallback": int(inf.n_fp64_fallback),
         "warm_start_accepted": int(inf.n_warm_accepted),
         "values_fp64": int(inf.values_fp64), "weight_l1_max": inf.weight_l1_max,
