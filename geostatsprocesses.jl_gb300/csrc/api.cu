@@ -1126,10 +1126,7 @@ static int check_flow_error(sgs_plan* P) {
     return SGS_OK;
 }
 
-// keep_err: leave the dataflow error word of an earlier sweep set (a sweep
-// of further realizations after it, checked once at the end)
-static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, void* V, cudaStream_t st,
-                     bool keep_err = false) {
+static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, void* V, cudaStream_t st) {
     (void)R;
     const sgs_sweep_config& c = P->sweep;
     P->last_sweep_mode = c.mode;
@@ -1172,7 +1169,7 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
         const int hi = std::max(lo, std::min(c.level_hi, P->nlevels));
         const int64_t plo = P->h_loff[lo], phi = P->h_loff[hi];
         const int32_t epoch = ++P->flow_epoch;
-        CK(P, cudaMemsetAsync(P->d_flow, 0, (keep_err ? 1 : 2) * sizeof(unsigned long long), st));
+        CK(P, cudaMemsetAsync(P->d_flow, 0, 2 * sizeof(unsigned long long), st));
         auto flow = [&](int64_t p0, int64_t p1) -> int {
             FlowArgs f{};
             f.item0 = p0 * H;
@@ -1351,11 +1348,13 @@ static int simulate_pipelined(sgs_plan* P, int R, uint64_t seed, double* out) {
         return rc ? rc : cuda_err(P, e, "pipelined sweep");
     }
     P->info.launches++;
-    // part b, swept while part a's output crosses the link; no host read in
-    // between (a small device-to-host copy would queue behind part a's
-    // output on the copy engine): part b keeps part a's dataflow error word,
-    // so a failed wait in part a stops part b at once and is reported below
-    if ((e = draws(Ra / 4, Rpb)) != cudaSuccess || (rc = run_sweep(P, Rb, Rpb, zr, seed, Vb, st, true)) ||
+    // a failed dependency wait of part a must not be cleared by part b's sweep
+    if ((e = cudaEventSynchronize(part_done[0])) != cudaSuccess || (rc = check_flow_error(P))) {
+        cleanup();
+        return rc ? rc : cuda_err(P, e, "pipelined sweep");
+    }
+    // part b, swept while part a's output crosses the link
+    if ((e = draws(Ra / 4, Rpb)) != cudaSuccess || (rc = run_sweep(P, Rb, Rpb, zr, seed, Vb, st)) ||
         (e = cudaEventRecord(part_done[1], st)) != cudaSuccess || (e = cudaEventRecord(P->ev[6], st)) != cudaSuccess ||
         (rc = so.enqueue(Vb, Rpb, Rb, Ra, out, ts, part_done[1]))) {
         cleanup();

@@ -235,11 +235,9 @@ def test_pipelined_seeded_output(R, geosgs_lib):
     """Seeded draws into page-locked memory with R >= 64 run as two parts of
     the realizations (the first part's output on the copy engines while the
     second part is swept, each part swept from its realizations' draw rows):
-    the values agree with one seeded sweep written through pageable memory
-    within 1e-6 (the shorter rows of a part can select a per-level kernel
-    that sums the neighbours in another order, as the sweep forms do), with
-    FP32 and with FP64 values, for even and uneven splits; the staged and
-    direct one-sweep forms equal the pageable result bit for bit."""
+    the values equal those of one seeded sweep written through pageable
+    memory, bit for bit, with FP32 and with FP64 values, for even and uneven
+    splits; the staged and direct one-sweep forms agree too."""
     import ctypes as C
 
     torch = pytest.importorskip("torch")
@@ -247,17 +245,18 @@ def test_pipelined_seeded_output(R, geosgs_lib):
     for precision in ("fp32", "fp64"):
         wl = workloads.small(n=40, k=12, ndata=10, vario="exp", nugget=0.05, precision=precision)
         p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
+        results = []
         for flags in (0, _abi.SGS_FLAG_OUTPUT_STAGED, _abi.SGS_FLAG_OUTPUT_DIRECT):
             p.flags = flags
             G = gpu_plan(p, keep)
             ref = G.simulate(R, seed=11)  # pageable output: one sweep
             out = torch.empty((R, G.N), dtype=torch.float64, pin_memory=True)
             G._check(G.lib.sgs_plan_simulate(G.h, R, None, 11, C.cast(out.data_ptr(), dp)))
-            if flags == 0:
-                assert rel_err(out.numpy(), ref) <= VALUE_TOL
-            else:
-                np.testing.assert_array_equal(out.numpy(), ref)
+            np.testing.assert_array_equal(out.numpy(), ref)
+            results.append(out.numpy().copy())
             G.close()
+        np.testing.assert_array_equal(results[0], results[1])
+        np.testing.assert_array_equal(results[0], results[2])
 
 
 def test_bounded_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
