@@ -718,8 +718,7 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     P->precision = pr->precision;
     P->refine_steps = pr->refine_steps;
     P->warm_start = pr->warm_start;
-    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32 | SGS_FLAG_OUTPUT_STAGED |
-                      SGS_FLAG_OUTPUT_DIRECT))
+    if (pr->flags & ~(SGS_FLAG_ONE_LAUNCH_SWEEP | SGS_FLAG_LEVEL_SWEEP | SGS_FLAG_NN_FP32 | SGS_FLAG_OUTPUT_STAGED))
         return set_err(P, SGS_ERR_ARG, "unknown flags");
     if ((pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) && (pr->flags & SGS_FLAG_LEVEL_SWEEP))
         return set_err(P, SGS_ERR_ARG, "SGS_FLAG_ONE_LAUNCH_SWEEP and SGS_FLAG_LEVEL_SWEEP exclude each other");
@@ -1228,154 +1227,6 @@ static int run_sweep(sgs_plan* P, int R, int Rp, const void* z, uint64_t seed, v
     return SGS_OK;
 }
 
-// Realization-major FP64 output through the copy engines: chunks of
-// realizations of a row array are transposed (on a given stream) into two
-// device buffers in turn, each copied to the page-locked host array by a
-// copy stream while the next chunk is transposed.  Parts of the output (row
-// arrays holding realizations [r0, r0 + R) each) are enqueued one by one.
-struct StagedOut {
-    sgs_plan* P = nullptr;
-    double* sb[2] = {nullptr, nullptr};
-    cudaStream_t cs = nullptr;
-    cudaEvent_t made[2] = {nullptr, nullptr}, moved[2] = {nullptr, nullptr};
-    int64_t rc_n = 1, i = 0;
-    cudaError_t err = cudaSuccess;
-
-    int init(sgs_plan* p, int R) {
-        P = p;
-        const int64_t stage_bytes = (int64_t)1 << 28;
-        rc_n = std::max<int64_t>(1, std::min<int64_t>(R, stage_bytes / (P->N * (int64_t)sizeof(double))));
-        int rc;
-        if ((rc = dalloc(P, &sb[0], (size_t)P->N * rc_n)) || (rc = dalloc(P, &sb[1], (size_t)P->N * rc_n))) return rc;
-        if ((err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)
-            return cuda_err(P, err, "staged output stream");
-        for (int b = 0; b < 2; ++b)
-            if ((err = cudaEventCreateWithFlags(&made[b], cudaEventDisableTiming)) != cudaSuccess ||
-                (err = cudaEventCreateWithFlags(&moved[b], cudaEventDisableTiming)) != cudaSuccess)
-                return cuda_err(P, err, "staged output events");
-        return SGS_OK;
-    }
-    // rows V (Rp values per node, realizations [r0, r0 + R) of the output);
-    // ts waits for `ready` (when given) before the first transpose
-    int enqueue(const void* V, int Rp, int R, int64_t r0, double* out, cudaStream_t ts, cudaEvent_t ready) {
-        const int64_t N = P->N;
-        if (ready) CK(P, cudaStreamWaitEvent(ts, ready, 0));
-        for (int64_t q = 0; q < R; q += rc_n, ++i) {
-            const int rn = (int)std::min<int64_t>(rc_n, R - q);
-            const int b = (int)(i & 1);
-            if (i >= 2) CK(P, cudaStreamWaitEvent(ts, moved[b], 0));  // buffer free again
-            if (values_fp64(P))
-                LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V + q, N, rn, Rp, P->mean, sb[b], ts));
-            else
-                LAUNCH(P, 1, launch_rows_to_out_fp32((const float*)V + q, N, rn, Rp, P->mean, sb[b], ts));
-            CK(P, cudaEventRecord(made[b], ts));
-            CK(P, cudaStreamWaitEvent(cs, made[b], 0));
-            CK(P, cudaMemcpyAsync(out + (r0 + q) * N, sb[b], (size_t)N * rn * sizeof(double), cudaMemcpyDeviceToHost,
-                                  cs));
-            CK(P, cudaEventRecord(moved[b], cs));
-            P->info.d2h_bytes += (int64_t)N * rn * sizeof(double);
-        }
-        return SGS_OK;
-    }
-    int finish() {
-        if (cs) CK(P, cudaStreamSynchronize(cs));
-        return SGS_OK;
-    }
-    ~StagedOut() {
-        if (cs) cudaStreamSynchronize(cs);
-        for (int b = 0; b < 2; ++b) {
-            if (made[b]) cudaEventDestroy(made[b]);
-            if (moved[b]) cudaEventDestroy(moved[b]);
-        }
-        if (cs) cudaStreamDestroy(cs);
-        if (P) {
-            dfree(P, sb[0]);
-            dfree(P, sb[1]);
-        }
-    }
-};
-
-// Seeded simulation into page-locked host memory in two parts of the
-// realizations, so that the first part's output crosses the link on the
-// copy engines while the second part is swept.  Each part is swept from the
-// draw rows of its realizations (the Philox normals the seeded sweep would
-// draw for them), so the values are those of one sweep over all R.
-static int simulate_pipelined(sgs_plan* P, int R, uint64_t seed, double* out) {
-    const int64_t N = P->N;
-    const bool f64 = values_fp64(P);
-    const size_t es = f64 ? sizeof(double) : sizeof(float);
-    // first part: a multiple of 32 realizations (128-byte aligned row halves)
-    const int Ra = std::max(32, (R / 2) / 32 * 32), Rb = R - Ra;
-    const int Rpa = Ra, Rpb = (Rb + 3) / 4 * 4;
-    cudaStream_t st = P->stream;
-    int rc;
-    unsigned char *Va = nullptr, *Vb = nullptr, *zr = nullptr;
-    if ((rc = dalloc(P, &Va, (size_t)N * Rpa * es)) || (rc = dalloc(P, &Vb, (size_t)N * Rpb * es)) ||
-        (rc = dalloc(P, &zr, (size_t)N * std::max(Rpa, Rpb) * es)))
-        return rc;
-    cudaEvent_t part_done[2] = {nullptr, nullptr};
-    cudaStream_t ts = nullptr;
-    StagedOut so;
-    auto cleanup = [&]() {
-        if (ts) {
-            cudaStreamSynchronize(ts);
-            cudaStreamDestroy(ts);
-        }
-        for (auto& e : part_done)
-            if (e) cudaEventDestroy(e);
-    };
-    auto draws = [&](int q0, int Rp) -> cudaError_t {
-        return f64 ? launch_draws_to_rows_fp64(seed, N, q0, Rp, (double*)zr, P->nsm, st)
-                   : launch_draws_to_rows_fp32(seed, N, q0, Rp, (float*)zr, P->nsm, st);
-    };
-    cudaError_t e = cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking);
-    for (auto& ev : part_done)
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (e != cudaSuccess) {
-        cleanup();
-        return cuda_err(P, e, "pipelined output set-up");
-    }
-    if ((rc = so.init(P, std::max(Ra, Rb)))) {
-        cleanup();
-        return rc;
-    }
-    CK(P, cudaEventRecord(P->ev[5], st));
-    // part a: draws, sweep; its output starts as soon as the sweep ends
-    if ((e = draws(0, Rpa)) != cudaSuccess || (rc = run_sweep(P, Ra, Rpa, zr, seed, Va, st)) ||
-        (e = cudaEventRecord(part_done[0], st)) != cudaSuccess ||
-        (rc = so.enqueue(Va, Rpa, Ra, 0, out, ts, part_done[0]))) {
-        cleanup();
-        return rc ? rc : cuda_err(P, e, "pipelined sweep");
-    }
-    P->info.launches++;
-    // a failed dependency wait of part a must not be cleared by part b's sweep
-    if ((e = cudaEventSynchronize(part_done[0])) != cudaSuccess || (rc = check_flow_error(P))) {
-        cleanup();
-        return rc ? rc : cuda_err(P, e, "pipelined sweep");
-    }
-    // part b, swept while part a's output crosses the link
-    if ((e = draws(Ra / 4, Rpb)) != cudaSuccess || (rc = run_sweep(P, Rb, Rpb, zr, seed, Vb, st)) ||
-        (e = cudaEventRecord(part_done[1], st)) != cudaSuccess || (e = cudaEventRecord(P->ev[6], st)) != cudaSuccess ||
-        (rc = so.enqueue(Vb, Rpb, Rb, Ra, out, ts, part_done[1]))) {
-        cleanup();
-        return rc ? rc : cuda_err(P, e, "pipelined sweep");
-    }
-    P->info.launches++;
-    if ((rc = so.finish())) {
-        cleanup();
-        return rc;
-    }
-    cleanup();
-    CK(P, cudaStreamSynchronize(st));
-    if ((rc = check_flow_error(P))) return rc;
-    P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
-    P->sweep_timed = false;
-    dfree(P, Va);
-    dfree(P, Vb);
-    dfree(P, zr);
-    return SGS_OK;
-}
-
 extern "C" int sgs_plan_simulate_device(sgs_plan* P, int32_t R, const void* z_dev, uint64_t seed, void* vals_dev,
                                         void* stream) {
     if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
@@ -1397,11 +1248,6 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     if (!P->prepared) return set_err(P, SGS_ERR_STATE, "simulate before prepare");
     if (R < 1 || !out) return set_err(P, SGS_ERR_ARG, "invalid nreals or output");
     CK(P, cudaSetDevice(P->device));
-    // seeded draws into page-locked memory: two parts of the realizations,
-    // the first part's output on the copy engines during the second's sweep
-    if (!z && R >= 64 && pinned_device_view(out) &&
-        !(P->flags & (SGS_FLAG_OUTPUT_STAGED | SGS_FLAG_OUTPUT_DIRECT)))
-        return simulate_pipelined(P, R, seed, out);
     const int64_t N = P->N;
     const int Rp = (R + 3) / 4 * 4;
     const size_t es = values_fp64(P) ? sizeof(double) : sizeof(float);
@@ -1428,10 +1274,48 @@ extern "C" int sgs_plan_simulate(sgs_plan* P, int32_t R, const double* z, uint64
     // address, else in chunks of realizations through a device buffer
     double* dout = pinned_device_view(out);
     if (dout && (P->flags & SGS_FLAG_OUTPUT_STAGED)) {
-        // chunks of realizations transposed on the plan's stream, moved by
-        // the copy engines
-        StagedOut so;
-        if ((rc = so.init(P, R)) || (rc = so.enqueue(V, Rp, R, 0, out, st, nullptr)) || (rc = so.finish())) return rc;
+        // chunks of realizations transposed on the plan's stream into two
+        // device buffers in turn, each copied out by the copy engines on a
+        // second stream while the next chunk is transposed
+        const int64_t stage_bytes = (int64_t)1 << 28;
+        const int64_t rc_n = std::max<int64_t>(1, std::min<int64_t>(R, stage_bytes / (N * (int64_t)sizeof(double))));
+        double* sb[2] = {nullptr, nullptr};
+        if ((rc = dalloc(P, &sb[0], (size_t)N * rc_n)) || (rc = dalloc(P, &sb[1], (size_t)N * rc_n))) {
+            dfree(P, sb[0]);
+            return rc;
+        }
+        cudaStream_t cs = nullptr;
+        cudaEvent_t made[2] = {nullptr, nullptr}, moved[2] = {nullptr, nullptr};
+        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+        for (int b = 0; ok && b < 2; ++b)
+            ok = cudaEventCreateWithFlags(&made[b], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&moved[b], cudaEventDisableTiming) == cudaSuccess;
+        int64_t i = 0;
+        for (int64_t r0 = 0; ok && r0 < R; r0 += rc_n, ++i) {
+            const int rn = (int)std::min<int64_t>(rc_n, R - r0);
+            const int b = (int)(i & 1);
+            if (i >= 2) ok = ok && cudaStreamWaitEvent(st, moved[b], 0) == cudaSuccess;  // buffer free again
+            const cudaError_t e = values_fp64(P)
+                ? launch_rows_to_out_fp64((const double*)V + r0, N, rn, Rp, P->mean, sb[b], st)
+                : launch_rows_to_out_fp32((const float*)V + r0, N, rn, Rp, P->mean, sb[b], st);
+            ok = ok && e == cudaSuccess && cudaEventRecord(made[b], st) == cudaSuccess &&
+                 cudaStreamWaitEvent(cs, made[b], 0) == cudaSuccess &&
+                 cudaMemcpyAsync(out + r0 * N, sb[b], (size_t)N * rn * sizeof(double), cudaMemcpyDeviceToHost, cs) ==
+                     cudaSuccess &&
+                 cudaEventRecord(moved[b], cs) == cudaSuccess;
+            P->info.launches++;
+            P->info.d2h_bytes += (int64_t)N * rn * sizeof(double);
+        }
+        ok = ok && cudaStreamSynchronize(cs) == cudaSuccess;
+        const cudaError_t err = cudaGetLastError();
+        for (int b = 0; b < 2; ++b) {
+            if (made[b]) cudaEventDestroy(made[b]);
+            if (moved[b]) cudaEventDestroy(moved[b]);
+        }
+        if (cs) cudaStreamDestroy(cs);
+        dfree(P, sb[0]);
+        dfree(P, sb[1]);
+        if (!ok) return cuda_err(P, err != cudaSuccess ? err : cudaErrorUnknown, "staged output");
     } else if (dout) {
         if (values_fp64(P))
             LAUNCH(P, 1, launch_rows_to_out_fp64((const double*)V, N, R, Rp, P->mean, dout, st));

@@ -346,8 +346,6 @@ cudaError_t launch_flow_mark(const int32_t* node, int64_t p0, int64_t p1, int H,
                              int32_t epoch, cudaStream_t s);
 int sweep_flow_max_blocks_per_sm(bool fp64, int G, bool tight);
 // host z (R x N, realization-major double) on device -> node-major [N][Rp] of T
-cudaError_t launch_draws_to_rows_fp32(uint64_t seed, int64_t N, int q0, int Rp, float* z, int nsm, cudaStream_t s);
-cudaError_t launch_draws_to_rows_fp64(uint64_t seed, int64_t N, int q0, int Rp, double* z, int nsm, cudaStream_t s);
 cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s);
 cudaError_t launch_z_to_rows_fp64(const double* zin, int64_t N, int R, int Rp, double* z, cudaStream_t s);
 // node-major centred values -> realization-major double with the mean added

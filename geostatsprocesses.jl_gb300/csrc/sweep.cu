@@ -868,34 +868,6 @@ static cudaError_t rows_out(const T* V, int64_t N, int R, int Rp, double mu, dou
     return cudaGetLastError();
 }
 
-// The seeded draws of realization chunks [q0, q0 + Rp / 4) as rows of Rp
-// values per node (z rows for a sweep over that part of the realizations):
-// the same Philox normals the seeded sweep draws in-kernel for those chunks.
-template <typename T>
-__global__ void draws_to_rows_kernel(uint64_t seed, int64_t N, int q0, int Rp, T* __restrict__ z) {
-    const int cpn = Rp >> 2;
-    const int64_t total = N * cpn;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t g = i / cpn;
-        const int c = (int)(i - g * cpn);
-        const float4 f = normals4(seed, g, q0 + c);
-        T* o = z + g * Rp + 4 * c;
-        o[0] = (T)f.x;
-        o[1] = (T)f.y;
-        o[2] = (T)f.z;
-        o[3] = (T)f.w;
-    }
-}
-
-cudaError_t launch_draws_to_rows_fp32(uint64_t seed, int64_t N, int q0, int Rp, float* z, int nsm, cudaStream_t s) {
-    draws_to_rows_kernel<float><<<nsm * 8, 256, 0, s>>>(seed, N, q0, Rp, z);
-    return cudaGetLastError();
-}
-cudaError_t launch_draws_to_rows_fp64(uint64_t seed, int64_t N, int q0, int Rp, double* z, int nsm, cudaStream_t s) {
-    draws_to_rows_kernel<double><<<nsm * 8, 256, 0, s>>>(seed, N, q0, Rp, z);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_z_to_rows_fp32(const double* zin, int64_t N, int R, int Rp, float* z, cudaStream_t s) {
     return z_rows<float>(zin, N, R, Rp, z, s);
 }

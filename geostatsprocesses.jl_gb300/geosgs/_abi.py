@@ -34,7 +34,6 @@ SGS_FLAG_ONE_LAUNCH_SWEEP = 1
 SGS_FLAG_LEVEL_SWEEP = 2
 SGS_FLAG_NN_FP32 = 4
 SGS_FLAG_OUTPUT_STAGED = 8
-SGS_FLAG_OUTPUT_DIRECT = 16
 
 SGS_NN_FEATURES = 8
 SGS_NN_PARAMS = 2401

@@ -71,19 +71,9 @@ extern "C" {
 #define SGS_FLAG_NN_FP32          4  /* warm-start inference in FP32 on the CUDA cores
                                         instead of BF16 on the tensor cores */
 #define SGS_FLAG_OUTPUT_STAGED    8  /* sgs_plan_simulate into page-locked memory:
-                                        one sweep, then chunks transposed into
-                                        device buffers and moved by the copy
-                                        engines (overlapped), instead of the
-                                        default below */
-#define SGS_FLAG_OUTPUT_DIRECT   16  /* sgs_plan_simulate into page-locked memory:
-                                        one sweep, then kernels write the host
-                                        array directly.  Default without either
-                                        flag: seeded draws (z NULL) with nreals
-                                        >= 64 run as two parts of the
-                                        realizations, the first part's output
-                                        moved by the copy engines while the
-                                        second part is swept (same values);
-                                        otherwise as this flag */
+                                        transpose chunks into device buffers and
+                                        move them with the copy engines (overlapped),
+                                        instead of kernels writing host memory */
 
 /* ---- per-node solve status (sgs_plan_weights) --------------------------- */
 #define SGS_NODE_KRIGED       0  /* conditional draw from simple kriging          */

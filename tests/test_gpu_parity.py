@@ -230,35 +230,6 @@ def test_simulate_into_pinned_host_memory(staged, geosgs_lib):
         G.close()
 
 
-@pytest.mark.parametrize("R", [64, 100, 130])
-def test_pipelined_seeded_output(R, geosgs_lib):
-    """Seeded draws into page-locked memory with R >= 64 run as two parts of
-    the realizations (the first part's output on the copy engines while the
-    second part is swept, each part swept from its realizations' draw rows):
-    the values equal those of one seeded sweep written through pageable
-    memory, bit for bit, with FP32 and with FP64 values, for even and uneven
-    splits; the staged and direct one-sweep forms agree too."""
-    import ctypes as C
-
-    torch = pytest.importorskip("torch")
-    dp = C.POINTER(C.c_double)
-    for precision in ("fp32", "fp64"):
-        wl = workloads.small(n=40, k=12, ndata=10, vario="exp", nugget=0.05, precision=precision)
-        p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, wl.method)
-        results = []
-        for flags in (0, _abi.SGS_FLAG_OUTPUT_STAGED, _abi.SGS_FLAG_OUTPUT_DIRECT):
-            p.flags = flags
-            G = gpu_plan(p, keep)
-            ref = G.simulate(R, seed=11)  # pageable output: one sweep
-            out = torch.empty((R, G.N), dtype=torch.float64, pin_memory=True)
-            G._check(G.lib.sgs_plan_simulate(G.h, R, None, 11, C.cast(out.data_ptr(), dp)))
-            np.testing.assert_array_equal(out.numpy(), ref)
-            results.append(out.numpy().copy())
-            G.close()
-        np.testing.assert_array_equal(results[0], results[1])
-        np.testing.assert_array_equal(results[0], results[2])
-
-
 def test_bounded_wait_gives_up_and_the_context_survives(oracle_mod, geosgs_lib):
     """The dataflow sweep's dependency wait, run on a flag that nothing sets
     (sgs_selftest_bounded_wait), gives up after its limit and reports it; the
