@@ -52,7 +52,6 @@ struct sgs_plan {
     int flags = 0;
     int32_t* d_loff = nullptr;    // device level offsets (nlevels + 1)
     int64_t N = 0, D = 0;
-    std::vector<int32_t> h_path;
     std::vector<TmplEntry> h_tmpl;
     std::vector<double> h_tmpl_d2;
     int tmpl_ext[3] = {0, 0, 0};
@@ -451,7 +450,7 @@ extern "C" void sgs_plan_destroy(sgs_plan* p) {
 // reference's ArgumentError / @assert), the neighbourhood metric, the path
 // and its ranks, the sorted offset template and the data buckets.  Shared by
 // plans and batches of domains.
-int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
+int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, bool path_ranks) {
 #define HERR(msg)              \
     do {                       \
         err = (msg);           \
@@ -544,9 +543,9 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
     // path and ranks: rank[path[t]] = t, then a check that every rank
     // points back (a path with a repeated or out-of-range entry fails it);
     // large grids in parallel
-    H.path.resize(H.N);
-    H.rank.assign(H.N, -1);
-    {
+    if (path_ranks) {
+        H.path.resize(H.N);
+        H.rank.assign(H.N, -1);
         const int64_t N = H.N;
         const int nt = N >= ((int64_t)1 << 20) ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
         std::vector<int> bad(nt, 0);
@@ -704,7 +703,7 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     HostDomain H;
     {
         std::string err;
-        const int rc = host_domain(pr, H, err);
+        const int rc = host_domain(pr, H, err, false);  // path ranks on the device, below
         if (rc != SGS_OK) return set_err(P, rc, err);
     }
     P->grid = H.grid;
@@ -726,7 +725,6 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     P->sweep.mode = (pr->flags & SGS_FLAG_ONE_LAUNCH_SWEEP) ? SGS_SWEEP_COOPERATIVE
                     : (pr->flags & SGS_FLAG_LEVEL_SWEEP)   ? SGS_SWEEP_LEVELS
                                                            : SGS_SWEEP_FLOW;
-    P->h_path = std::move(H.path);
     P->h_tmpl = std::move(H.tmpl);
     P->h_tmpl_d2 = std::move(H.tmpl_d2);
     for (int j = 0; j < 3; ++j) {
@@ -749,8 +747,19 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     for (auto& ev : P->ev) CK(P, cudaEventCreate(&ev));
 
     int rc;
-    if ((rc = upload(P, &P->d_path, P->h_path.data(), P->N))) return rc;
-    if ((rc = upload(P, &P->d_rank, H.rank.data(), P->N))) return rc;
+    // the path as given (or the linear one), its ranks built and checked on
+    // the device: rank[path[t]] = t, and the path a permutation of the nodes
+    int32_t* d_perr = nullptr;
+    if ((rc = dalloc(P, &P->d_rank, P->N)) || (rc = dalloc(P, &d_perr, 1))) return rc;
+    if (pr->path) {
+        if ((rc = upload(P, &P->d_path, pr->path, P->N))) return rc;
+    } else if ((rc = dalloc(P, &P->d_path, P->N))) {
+        return rc;
+    }
+    CK(P, cudaMemsetAsync(P->d_rank, 0xff, (size_t)P->N * sizeof(int32_t), P->stream));
+    CK(P, cudaMemsetAsync(d_perr, 0, sizeof(int32_t), P->stream));
+    LAUNCH(P, 2, launch_path_ranks(pr->path ? P->d_path : nullptr, P->N, P->d_path, P->d_rank, d_perr, P->nsm,
+                                   P->stream));
     if ((rc = upload(P, &P->d_tmpl, P->h_tmpl.data(), P->h_tmpl.size()))) return rc;
     if ((rc = upload(P, &P->d_tmpl_d2, P->h_tmpl_d2.data(), P->h_tmpl_d2.size()))) return rc;
     if ((rc = upload(P, &P->d_dxyz, H.xyz.data(), H.xyz.size()))) return rc;
@@ -759,7 +768,11 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     if ((rc = upload(P, &P->d_did, H.did.data(), H.did.size()))) return rc;
     if ((rc = upload(P, &P->d_bstart, H.bstart.data(), H.bstart.size()))) return rc;
     if ((rc = upload(P, &P->d_dxyz_f, H.xf.data(), H.xf.size()))) return rc;
+    int32_t perr = 0;
+    CK(P, cudaMemcpyAsync(&perr, d_perr, sizeof(int32_t), cudaMemcpyDeviceToHost, P->stream));
     CK(P, cudaStreamSynchronize(P->stream));
+    dfree(P, d_perr);
+    if (perr) return set_err(P, SGS_ERR_ARG, "path is not a permutation of the grid nodes");
 
     P->info.nnodes = P->N;
     P->info.ndata = P->D;

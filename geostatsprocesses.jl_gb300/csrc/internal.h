@@ -266,8 +266,16 @@ struct HostDomain {
     int nb[3] = {1, 1, 1};
     double bw[3] = {1, 1, 1};
 };
-// Validates *pr and fills H; SGS_OK or SGS_ERR_ARG with err set.
-int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err);
+// Validates *pr and fills H; SGS_OK or SGS_ERR_ARG with err set.  With
+// path_ranks false the path is left to the caller (H.path and H.rank stay
+// empty): plans build and check the ranks on the device (launch_path_ranks).
+int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, bool path_ranks = true);
+// rank[path[t]] = t for a path of N nodes on the device (path NULL: the
+// linear path, written into path_out), checking that the path is a
+// permutation of [0, N): *err (zeroed by the caller) is set otherwise.
+// path_out may equal path.
+cudaError_t launch_path_ranks(const int32_t* path, int64_t N, int32_t* path_out, int32_t* rank, int32_t* err,
+                              int nsm, cudaStream_t s);
 // The geometry fields of a domain's SearchArgs (device pointers left as they are).
 void search_args_of(const HostDomain& H, SearchArgs& sa);
 

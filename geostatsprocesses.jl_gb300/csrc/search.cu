@@ -487,6 +487,41 @@ __global__ void __launch_bounds__(256) levels_kernel(const LevelArgs a) {
     if (lane == 0) atomicMax(a.maxlevel, wmax);
 }
 
+// rank[path[t]] = t (rank preset to -1; a NULL path is the linear one and is
+// written out), then a second pass: every entry in range, and every rank
+// pointing back to its t — a repeated node leaves one of its ranks pointing
+// elsewhere, and a node never visited is then impossible (N entries).
+__global__ void path_rank_scatter_kernel(const int32_t* __restrict__ path, int64_t N, int32_t* __restrict__ path_out,
+                                         int32_t* __restrict__ rank, int32_t* err) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = path ? (int64_t)path[t] : t;
+        if (!path) path_out[t] = (int32_t)t;
+        if (g < 0 || g >= N) {
+            atomicOr(err, 1);
+            continue;
+        }
+        rank[g] = (int32_t)t;
+    }
+}
+
+__global__ void path_rank_check_kernel(const int32_t* __restrict__ path, int64_t N, const int32_t* __restrict__ rank,
+                                       int32_t* err) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = path[t];
+        if (g >= 0 && g < N && rank[g] != (int32_t)t) atomicOr(err, 2);
+    }
+}
+
+cudaError_t launch_path_ranks(const int32_t* path, int64_t N, int32_t* path_out, int32_t* rank, int32_t* err, int nsm,
+                              cudaStream_t s) {
+    if (N <= 0) return cudaSuccess;
+    path_rank_scatter_kernel<<<nsm * 8, 256, 0, s>>>(path, N, path_out, rank, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    path_rank_check_kernel<<<nsm * 8, 256, 0, s>>>(path_out, N, rank, err);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_levels(const LevelArgs& a, int nsm, cudaStream_t s) {
     levels_kernel<<<nsm * 8, 256, 0, s>>>(a);
     return cudaGetLastError();

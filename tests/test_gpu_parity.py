@@ -339,6 +339,25 @@ def test_error_codes(geosgs_lib):
     with pytest.raises(geosgs.GeoSGSError) as e:
         geosgs.Plan(p, (keep, bad))
     assert e.value.code == _abi.SGS_ERR_ARG
+    # the path ranks are built and checked on the device: a node outside the
+    # grid, a repeated node (with one node missing) and a valid reversed path
+    for case, expect in (("outside", _abi.SGS_ERR_ARG), ("repeat", _abi.SGS_ERR_ARG), ("reversed", 0)):
+        path = np.arange(99, -1, -1, dtype=np.int32)
+        if case == "outside":
+            path[17] = 100
+        elif case == "repeat":
+            path[17] = path[18]
+        p.path = path.ctypes.data_as(C.POINTER(C.c_int32))
+        if expect:
+            with pytest.raises(geosgs.GeoSGSError) as e:
+                geosgs.Plan(p, (keep, path))
+            assert e.value.code == expect, case
+            assert "permutation" in str(e.value)
+        else:
+            G = geosgs.Plan(p, (keep, path)).prepare()
+            lv, _ = G.levels()
+            G.close()
+            assert lv[path[0]] == 0
 
 
 SWEEP_FORMS = [
