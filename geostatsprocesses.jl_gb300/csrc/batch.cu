@@ -579,7 +579,7 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
         std::vector<std::thread> th;
         for (int t = 0; t < nt; ++t)
             th.emplace_back([&, t]() {
-                for (int d = t; d < nd; d += nt) rcs[d] = host_domain(&pr[d], H[d], errs[d]);
+                for (int d = t; d < nd; d += nt) rcs[d] = host_domain(&pr[d], H[d], errs[d], false);
             });
         for (auto& x : th) x.join();
     }
@@ -626,7 +626,9 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
     BCK(B, cudaMallocHost(&B->h_seed, sizeof(uint64_t)));
 
     // arenas
-    HostArena<int32_t> path(B->Ntot), rank(B->Ntot), did(B->Dtot), bstart(boff[nd]);
+    // path arena: local node ids per domain, as given (or the linear path);
+    // the ranks are built and checked on the device
+    HostArena<int32_t> path(B->Ntot), did(B->Dtot), bstart(boff[nd]);
     HostArena<TmplEntry> tmpl(toff[nd]);
     HostArena<double> td2(toff[nd]), xyz(3 * B->Dtot), val(B->Dtot), xyzb(3 * B->Dtot);
     HostArena<float4> xf(B->Dtot);
@@ -639,8 +641,9 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
             th.emplace_back([&, t]() {
                 for (int d = t; d < nd; d += nt) {
                     const HostDomain& h = H[d];
-                    std::copy(h.path.begin(), h.path.end(), path.data() + B->noff[d]);
-                    std::copy(h.rank.begin(), h.rank.end(), rank.data() + B->noff[d]);
+                    int32_t* pd = path.data() + B->noff[d];
+                    if (pr[d].path) std::copy(pr[d].path, pr[d].path + h.N, pd);
+                    else for (int64_t t = 0; t < h.N; ++t) pd[t] = (int32_t)t;
                     std::copy(h.tmpl.begin(), h.tmpl.end(), tmpl.data() + toff[d]);
                     std::copy(h.tmpl_d2.begin(), h.tmpl_d2.end(), td2.data() + toff[d]);
                     std::copy(h.xyz.begin(), h.xyz.end(), xyz.data() + 3 * doff[d]);
@@ -660,7 +663,22 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
     float4* d_xf;
     float2* d_lut;
     if ((rc = bupload(B, &B->d_path, path))) return rc;
-    if ((rc = bupload(B, &d_rank, rank))) return rc;
+    if ((rc = bupload(B, &B->d_noff, B->noff))) return rc;
+    {
+        int32_t* d_bad = nullptr;
+        if ((rc = balloc(B, &d_rank, B->Ntot)) || (rc = balloc(B, &d_bad, 1))) return rc;
+        const int32_t nd32 = nd;
+        BCK(B, cudaMemsetAsync(d_rank, 0xff, (size_t)B->Ntot * sizeof(int32_t), B->stream));
+        BCK(B, cudaMemcpyAsync(d_bad, &nd32, sizeof(int32_t), cudaMemcpyHostToDevice, B->stream));
+        BCK(B, launch_batch_path_ranks(B->d_path, B->d_noff, nd, B->Ntot, d_rank, d_bad, B->nsm, B->stream));
+        B->info.launches += 2;
+        int32_t bad = nd;
+        BCK(B, cudaMemcpyAsync(&bad, d_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, B->stream));
+        BCK(B, cudaStreamSynchronize(B->stream));
+        bfree(B, d_bad);
+        if (bad < nd)
+            return berr(B, SGS_ERR_ARG, "domain " + std::to_string(bad) + ": path is not a permutation of the grid nodes");
+    }
     if ((rc = bupload(B, &d_tmpl, tmpl))) return rc;
     if ((rc = bupload(B, &d_td2, td2))) return rc;
     if ((rc = bupload(B, &d_xyz, xyz))) return rc;
@@ -747,7 +765,6 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
 
         ld[d] = LevelDom{B->noff[d], B->nbr0[d], (int32_t)h.N, h.k};
     }
-    if ((rc = bupload(B, &B->d_noff, B->noff))) return rc;
     if ((rc = bupload(B, &B->d_search, B->search))) return rc;
     if ((rc = bupload(B, &B->d_solve, B->solve))) return rc;
     if ((rc = bupload(B, &B->d_ldom, ld))) return rc;

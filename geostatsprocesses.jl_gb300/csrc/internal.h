@@ -276,6 +276,11 @@ int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, bool pat
 // path_out may equal path.
 cudaError_t launch_path_ranks(const int32_t* path, int64_t N, int32_t* path_out, int32_t* rank, int32_t* err,
                               int nsm, cudaStream_t s);
+// The same over a batch's path arena (local ids per domain, domains by the
+// offsets off[0..nd]); *bad_domain (preset to nd) takes the smallest domain
+// whose path is not a permutation.
+cudaError_t launch_batch_path_ranks(const int32_t* path, const int64_t* off, int nd, int64_t total, int32_t* rank,
+                                    int32_t* bad_domain, int nsm, cudaStream_t s);
 // The geometry fields of a domain's SearchArgs (device pointers left as they are).
 void search_args_of(const HostDomain& H, SearchArgs& sa);
 

@@ -522,6 +522,44 @@ cudaError_t launch_path_ranks(const int32_t* path, int64_t N, int32_t* path_out,
     return cudaGetLastError();
 }
 
+// The same for the path arena of a batch of domains: entry i of domain d
+// (global ids [off[d], off[d+1])) holds a local node id; rank entries are
+// local too.  *bad_domain (preset to nd by the caller) takes the smallest
+// domain whose path is not a permutation of its nodes.
+__global__ void batch_rank_scatter_kernel(const int32_t* __restrict__ path, const int64_t* __restrict__ off, int nd,
+                                          int32_t* __restrict__ rank, int32_t* bad_domain) {
+    const int64_t total = off[nd];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int d = find_domain(off, nd, i);
+        const int64_t o = off[d], n = off[d + 1] - o, g = path[i];
+        if (g < 0 || g >= n) {
+            atomicMin(bad_domain, d);
+            continue;
+        }
+        rank[o + g] = (int32_t)(i - o);
+    }
+}
+
+__global__ void batch_rank_check_kernel(const int32_t* __restrict__ path, const int64_t* __restrict__ off, int nd,
+                                        const int32_t* __restrict__ rank, int32_t* bad_domain) {
+    const int64_t total = off[nd];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int d = find_domain(off, nd, i);
+        const int64_t o = off[d], n = off[d + 1] - o, g = path[i];
+        if (g >= 0 && g < n && rank[o + g] != (int32_t)(i - o)) atomicMin(bad_domain, d);
+    }
+}
+
+cudaError_t launch_batch_path_ranks(const int32_t* path, const int64_t* off, int nd, int64_t total, int32_t* rank,
+                                    int32_t* bad_domain, int nsm, cudaStream_t s) {
+    if (total <= 0) return cudaSuccess;
+    batch_rank_scatter_kernel<<<nsm * 8, 256, 0, s>>>(path, off, nd, rank, bad_domain);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    batch_rank_check_kernel<<<nsm * 8, 256, 0, s>>>(path, off, nd, rank, bad_domain);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_levels(const LevelArgs& a, int nsm, cudaStream_t s) {
     levels_kernel<<<nsm * 8, 256, 0, s>>>(a);
     return cudaGetLastError();
