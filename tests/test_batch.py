@@ -47,7 +47,8 @@ def test_c5_generator_is_seeded_and_in_range():
 
 
 def test_batch_argument_errors():
-    """Validation happens before any device work (runs without a GPU)."""
+    """Argument validation happens before any device work (runs without a
+    GPU); the paths are checked on the device (see below)."""
     from geosgs import _build
 
     _build.build()
@@ -67,6 +68,33 @@ def test_batch_argument_errors():
     with pytest.raises(geosgs.GeoSGSError) as e:
         geosgs.Batch(probs)
     assert e.value.code == _abi.SGS_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_batch_path_checked_on_the_device(geosgs_lib):
+    """The path ranks of a batch are built and checked on the device: a
+    domain whose path repeats a node (or leaves the domain) is rejected with
+    SGS_ERR_ARG naming the first such domain; a valid batch then works."""
+    import ctypes as C
+
+    bw = workloads.c5_small(ndomains=3)
+    for case in ("repeat", "outside"):
+        probs = problems_of(bw, "fp32")
+        p2, keep2 = probs[2]
+        n = int(np.prod([p2.dims[j] for j in range(p2.dim)]))
+        path = np.arange(n - 1, -1, -1, dtype=np.int32)
+        if case == "repeat":
+            path[3] = path[4]
+        else:
+            path[5] = n
+        p2.path = path.ctypes.data_as(C.POINTER(C.c_int32))
+        probs[2] = (p2, (keep2, path))
+        with pytest.raises(geosgs.GeoSGSError) as e:
+            geosgs.Batch(probs)
+        assert e.value.code == _abi.SGS_ERR_ARG and "domain 2" in str(e.value) and "permutation" in str(e.value)
+    B = geosgs.Batch(problems_of(bw, "fp32")).prepare()
+    assert B.info().nnodes == bw.nodes()
+    B.close()
 
 
 @pytest.mark.gpu
