@@ -268,8 +268,13 @@ cudaError_t device_pool(int device, cudaMemPool_t* pool, cudaStream_t* as) {
         // mapping them anew each time costs milliseconds)
         uint64_t keep = UINT64_MAX;
         e = cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+        // the allocation stream belongs to the pool's device
+        int cur = 0;
         cudaStream_t st = nullptr;
+        if (e == cudaSuccess) e = cudaGetDevice(&cur);
+        if (e == cudaSuccess && cur != device) e = cudaSetDevice(device);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (cur != device) cudaSetDevice(cur);
         if (e != cudaSuccess) {
             cudaMemPoolDestroy(mp);
             return e;
