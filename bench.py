@@ -88,8 +88,8 @@ def measure_peaks() -> dict:
 
 
 def solve_flops(sizes, refine_steps: int) -> float:
-    """Algorithmic FLOPs of the kriging systems on the survey's basis, per
-    system of n neighbours: n(n+1)/2 covariance evaluations, n^3/3 for the
+    """Algorithmic FLOPs of the kriging systems, counted for a Cholesky-based
+    solve whatever algorithm runs, per system of n neighbours: n(n+1)/2 covariance evaluations, n^3/3 for the
     Cholesky factorization, 2 n^2 for the two triangular solves, per
     refinement step 2 n^2 (residual) + 2 n^2 (correction), 2 n for the
     variance; sizes[n] = number of systems with n neighbours."""
@@ -742,7 +742,7 @@ def main():
         if probes.get("d2h_copy_gbs"):
             e2e["d2h_copy_gbs"] = probes["d2h_copy_gbs"]
 
-    # the solve (kernel b), bound by the FP32 pipe, on the survey's FLOP
+    # the solve (kernel b), bound by the FP32 pipe, on the algorithmic FLOP
     # basis (factorization n^3/3, not the cost of the algorithm run); the
     # executed Gauss-Jordan count (2 n^3 + 8 n^2) is reported beside it
     sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
@@ -776,7 +776,7 @@ def main():
     solve_roofline["nominal_peak"] = fp32_nominal
     solve_roofline["gj_pattern_peak"] = probes.get("gj_pattern_tflops")
 
-    # the search (kernel a) on the survey's byte basis: a path-rank read (4 B)
+    # the search (kernel a) on its algorithmic byte basis: a path-rank read (4 B)
     # per grid candidate examined (earlier path nodes tested by the first
     # ranks, template offsets inside the grid), the FP32 coordinates (16 B) of
     # every datum screened, and the row written (k int32 slots, count and
