@@ -375,8 +375,10 @@ struct sgs_batch {
     SweepTables<double> t64{};
     bool allocated = false, prepared = false;
     // graphs
-    cudaGraphExec_t prep_exec = nullptr;
-    int64_t prep_nodes = 0;
+    // prepare graphs: [1] the whole sequence, [0] everything after the
+    // search (the first prepare, whose table-sizing search already ran)
+    cudaGraphExec_t prep_exec[2] = {nullptr, nullptr};
+    int64_t prep_nodes[2] = {0, 0};
     cudaGraphExec_t sweep_exec = nullptr;
     int64_t sweep_nodes = 0;
     int sweep_Rp = 0;
@@ -547,7 +549,8 @@ extern "C" void sgs_batch_destroy(sgs_batch* b) {
     // device-pointer entry points): wait for the device, as a synchronous
     // free would
     cudaDeviceSynchronize();
-    if (b->prep_exec) cudaGraphExecDestroy(b->prep_exec);
+    for (auto& e : b->prep_exec)
+        if (e) cudaGraphExecDestroy(e);
     if (b->sweep_exec) cudaGraphExecDestroy(b->sweep_exec);
     for (auto& x : b->bufs) pool_free(x.p, b->stream);
     if (b->stream) cudaStreamSynchronize(b->stream);
@@ -799,13 +802,17 @@ extern "C" int sgs_batch_create(const sgs_problem* problems, int32_t ndomains, s
 // on the device, so it is captured once and replayed.  The phase events are
 // recorded as external event nodes (a plain record inside a capture only
 // marks a dependency), so they time the replayed graph.
-static int enqueue_prepare(sgs_batch* B, int64_t& launched) {
+// with_search false: the sequence after the neighbour search (its results
+// already in place)
+static int enqueue_prepare(sgs_batch* B, int64_t& launched, bool with_search) {
     cudaStream_t st = B->stream;
     const int64_t N = B->Ntot;
     const int nd = B->ndom;
-    BCK(B, cudaEventRecordWithFlags(B->ev[0], st, cudaEventRecordExternal));
-    BLAUNCH(B, launch_search_batch(B->d_search, B->d_noff, nd, N, B->nsm, st));
-    BCK(B, cudaEventRecordWithFlags(B->ev[1], st, cudaEventRecordExternal));
+    if (with_search) {
+        BCK(B, cudaEventRecordWithFlags(B->ev[0], st, cudaEventRecordExternal));
+        BLAUNCH(B, launch_search_batch(B->d_search, B->d_noff, nd, N, B->nsm, st));
+        BCK(B, cudaEventRecordWithFlags(B->ev[1], st, cudaEventRecordExternal));
+    }
     // levels and level order
     BCK(B, cudaMemsetAsync(B->d_level, 0xff, N * sizeof(int32_t), st));
     BCK(B, cudaMemsetAsync(B->d_scratch, 0, 4 * sizeof(int32_t), st));
@@ -863,9 +870,14 @@ extern "C" int sgs_batch_prepare(sgs_batch* B) {
     cudaStream_t st = B->stream;
     int rc;
     int64_t launched = 0;
+    bool searched = false;
     if (!B->allocated) {
-        // size the packed sweep tables: one search, then the grid-neighbour sum
+        // size the packed sweep tables: one search, then the grid-neighbour
+        // sum; this prepare then runs the rest of the sequence only
+        BCK(B, cudaEventRecord(B->ev[0], st));
         BLAUNCH(B, launch_search_batch(B->d_search, B->d_noff, B->ndom, B->Ntot, B->nsm, st));
+        BCK(B, cudaEventRecord(B->ev[1], st));
+        searched = true;
         BCK(B, cudaMemsetAsync(B->d_sums, 0, sizeof(unsigned long long), st));
         sum_kernel<<<B->nsm * 4, 256, 0, st>>>(B->Ntot, B->d_ngrid, B->d_sums);
         BLAUNCH(B, cudaGetLastError());
@@ -896,27 +908,28 @@ extern "C" int sgs_batch_prepare(sgs_batch* B) {
         B->info.launches += launched;
         launched = 0;
     }
-    if (!B->prep_exec) {
+    const int gi = searched ? 0 : 1;
+    if (!B->prep_exec[gi]) {
         cudaGraph_t g = nullptr;
         BCK(B, cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-        rc = enqueue_prepare(B, launched);
+        rc = enqueue_prepare(B, launched, !searched);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
             return rc;
         }
         if (ce != cudaSuccess) return bcuda(B, ce, "cudaStreamEndCapture (prepare)");
-        ce = cudaGraphInstantiate(&B->prep_exec, g, 0);
+        ce = cudaGraphInstantiate(&B->prep_exec[gi], g, 0);
         cudaGraphDestroy(g);
         if (ce != cudaSuccess) {
-            B->prep_exec = nullptr;
+            B->prep_exec[gi] = nullptr;
             return bcuda(B, ce, "cudaGraphInstantiate (prepare)");
         }
-        B->prep_nodes = launched;
+        B->prep_nodes[gi] = launched;
     }
-    BCK(B, cudaGraphLaunch(B->prep_exec, st));
+    BCK(B, cudaGraphLaunch(B->prep_exec[gi], st));
     B->info.graph_launches++;
-    B->info.launches += B->prep_nodes;
+    B->info.launches += B->prep_nodes[gi];
     // statistics (after the graph)
     BCK(B, cudaMemsetAsync(B->d_sums + 2, 0, sizeof(unsigned long long), st));
     count_nonzero_kernel<<<B->nsm * 4, 256, 0, st>>>(B->Ntot, B->d_status, B->d_sums + 2);
