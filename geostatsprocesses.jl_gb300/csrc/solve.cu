@@ -605,54 +605,29 @@ __device__ __forceinline__ void solve32_system(const SolveArgs& a, const SweepTa
                 for (int o = 16; o > 0; o >>= 1) wmax = fmaxf(wmax, __shfl_xor_sync(FULL_MASK, wmax, o));
                 bool early = false;
                 for (int s = 0;; ++s) {
-                    // residual r = c - K w in double-FP32, own rows.  The first
-                    // residual of a warm start is plain FP32: the start (a
-                    // prediction, ~30 % off) only needs a correction as good
-                    // as the FP32 inverse makes it (~1e-5), and the residual
-                    // that is tested and enters the variance is a later one
-                    const bool coarse = s == 0 && a.w_init && steps >= 2;
+                    // residual r = c - K w in double-FP32, own rows
                     float r0 = 0.0f, r1 = 0.0f;
                     // row i of the packed triangle: entries t_i + j for j <= i,
                     // then down column i (j (j + 1) / 2 + i) for j > i
                     if (i0 < n) {
-                        if (coarse) {
-                            float r = c[i0].hi;
-                            int jt = 0;  // j (j + 1) / 2
-                            for (int j = 0; j < n; ++j) {
-                                r = __fmaf_rn(-K[j <= i0 ? t0 + j : jt + i0].hi, w[j].hi, r);
-                                jt += j + 1;
-                            }
-                            r0 = r;
-                        } else {
-                            DFAcc acc;
-                            acc.init(c[i0]);
-                            int jt = 0;
-                            for (int j = 0; j < n; ++j) {
-                                acc.add_prod(df_neg(K[j <= i0 ? t0 + j : jt + i0]), w[j]);
-                                jt += j + 1;
-                            }
-                            r0 = acc.value().hi;
+                        DFAcc acc;
+                        acc.init(c[i0]);
+                        int jt = 0;  // j (j + 1) / 2
+                        for (int j = 0; j < n; ++j) {
+                            acc.add_prod(df_neg(K[j <= i0 ? t0 + j : jt + i0]), w[j]);
+                            jt += j + 1;
                         }
+                        r0 = acc.value().hi;
                     }
                     if (TWO && i1 < n) {
-                        if (coarse) {
-                            float r = c[i1].hi;
-                            int jt = 0;
-                            for (int j = 0; j < n; ++j) {
-                                r = __fmaf_rn(-K[j <= i1 ? t1 + j : jt + i1].hi, w[j].hi, r);
-                                jt += j + 1;
-                            }
-                            r1 = r;
-                        } else {
-                            DFAcc acc;
-                            acc.init(c[i1]);
-                            int jt = 0;
-                            for (int j = 0; j < n; ++j) {
-                                acc.add_prod(df_neg(K[j <= i1 ? t1 + j : jt + i1]), w[j]);
-                                jt += j + 1;
-                            }
-                            r1 = acc.value().hi;
+                        DFAcc acc;
+                        acc.init(c[i1]);
+                        int jt = 0;
+                        for (int j = 0; j < n; ++j) {
+                            acc.add_prod(df_neg(K[j <= i1 ? t1 + j : jt + i1]), w[j]);
+                            jt += j + 1;
                         }
+                        r1 = acc.value().hi;
                     }
                     sw0 = w0;
                     sw1 = w1;
