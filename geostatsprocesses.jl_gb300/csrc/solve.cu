@@ -352,10 +352,12 @@ cudaError_t launch_solve_fp64(const SolveArgs& a, const SweepTables<double>& t, 
 // 1e-3 (near-singular: the canonical 1e-10 decision needs FP64) or whose
 // refinement does not contract is queued for the FP64 kernel.
 constexpr int SOLVE32_WARPS = 2;
-// resident blocks per SM the FP32 solve is compiled for: 6 x 2 warps at up to
-// 168 registers a thread fill the register file; systems of up to 64
-// neighbours hold two rows of 64 registers and get 4 blocks (255 registers)
-constexpr int solve32_min_blocks(int nmax) { return nmax > 48 ? 4 : 6; }
+// resident blocks per SM the FP32 solve is compiled for.  Systems of up to 48
+// neighbours: 7 x 2 warps at 128 registers a thread (a few spilled values,
+// measured 7 % faster than 6 blocks at 168 registers without spills, and
+// ahead of 8 blocks); up to 32 neighbours: 8 blocks at under 100 registers;
+// up to 64 neighbours hold two rows of 64 registers and get 4 blocks
+constexpr int solve32_min_blocks(int nmax) { return nmax > 48 ? 4 : (nmax > 32 ? 7 : 8); }
 
 template <int NMAX>
 struct Smem32 {
