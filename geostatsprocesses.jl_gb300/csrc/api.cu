@@ -455,7 +455,7 @@ extern "C" void sgs_plan_destroy(sgs_plan* p) {
 // reference's ArgumentError / @assert), the neighbourhood metric, the path
 // and its ranks, the sorted offset template and the data buckets.  Shared by
 // plans and batches of domains.
-int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, bool path_ranks) {
+int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err) {
 #define HERR(msg)              \
     do {                       \
         err = (msg);           \
@@ -545,40 +545,8 @@ int sgs::host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, boo
         HERR("unknown search kind");
     }
 
-    // path and ranks: rank[path[t]] = t, then a check that every rank
-    // points back (a path with a repeated or out-of-range entry fails it);
-    // large grids in parallel
-    if (path_ranks) {
-        H.path.resize(H.N);
-        H.rank.assign(H.N, -1);
-        const int64_t N = H.N;
-        const int nt = N >= ((int64_t)1 << 20) ? std::max(1, std::min(16, (int)std::thread::hardware_concurrency())) : 1;
-        std::vector<int> bad(nt, 0);
-        auto run = [&](int w, int pass) {
-            const int64_t t0 = N * w / nt, t1 = N * (w + 1) / nt;
-            for (int64_t t = t0; t < t1; ++t) {
-                const int64_t g = pr->path ? pr->path[t] : t;
-                if (pass == 0) {
-                    if (g < 0 || g >= N) {
-                        bad[w] = 1;
-                        continue;
-                    }
-                    H.path[t] = (int32_t)g;
-                    __atomic_store_n(&H.rank[g], (int32_t)t, __ATOMIC_RELAXED);
-                } else if (H.rank[g] != (int32_t)t) {
-                    bad[w] = 1;
-                }
-            }
-        };
-        for (int pass = 0; pass < 2; ++pass) {
-            std::vector<std::thread> th;
-            for (int w = 1; w < nt; ++w) th.emplace_back(run, w, pass);
-            run(0, pass);
-            for (auto& x : th) x.join();
-            for (int w = 0; w < nt; ++w)
-                if (bad[w]) HERR("path is not a permutation of the grid nodes");
-        }
-    }
+    // the path is checked on the device, where its ranks are built
+    // (launch_path_ranks, launch_batch_path_ranks)
 
     // template: cell offsets inside the neighbourhood in canonical order
     int64_t e[3] = {0, 0, 0};
@@ -708,7 +676,7 @@ static int plan_init(sgs_plan* P, const sgs_problem* pr) {
     HostDomain H;
     {
         std::string err;
-        const int rc = host_domain(pr, H, err, false);  // path ranks on the device, below
+        const int rc = host_domain(pr, H, err);  // path ranks on the device, below
         if (rc != SGS_OK) return set_err(P, rc, err);
     }
     P->grid = H.grid;

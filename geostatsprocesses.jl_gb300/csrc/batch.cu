@@ -582,7 +582,7 @@ static int batch_init(sgs_batch* B, const sgs_problem* pr, int nd) {
         std::vector<std::thread> th;
         for (int t = 0; t < nt; ++t)
             th.emplace_back([&, t]() {
-                for (int d = t; d < nd; d += nt) rcs[d] = host_domain(&pr[d], H[d], errs[d], false);
+                for (int d = t; d < nd; d += nt) rcs[d] = host_domain(&pr[d], H[d], errs[d]);
             });
         for (auto& x : th) x.join();
     }

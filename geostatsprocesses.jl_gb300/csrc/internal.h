@@ -255,7 +255,6 @@ struct HostDomain {
     double mean = 0.0;
     int k = 0, nmin = 1;
     int64_t N = 0, D = 0;
-    std::vector<int32_t> path, rank;      // path rank -> node, node -> path rank
     std::vector<TmplEntry> tmpl;          // offsets sorted by (d2, linear offset)
     std::vector<double> tmpl_d2;
     int tmpl_ext[3] = {0, 0, 0};          // largest |offset| per axis
@@ -266,10 +265,10 @@ struct HostDomain {
     int nb[3] = {1, 1, 1};
     double bw[3] = {1, 1, 1};
 };
-// Validates *pr and fills H; SGS_OK or SGS_ERR_ARG with err set.  With
-// path_ranks false the path is left to the caller (H.path and H.rank stay
-// empty): plans build and check the ranks on the device (launch_path_ranks).
-int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err, bool path_ranks = true);
+// Validates *pr and fills H; SGS_OK or SGS_ERR_ARG with err set.  The path
+// is left to the caller: plans and batches build and check its ranks on the
+// device (launch_path_ranks, launch_batch_path_ranks).
+int host_domain(const sgs_problem* pr, HostDomain& H, std::string& err);
 // rank[path[t]] = t for a path of N nodes on the device (path NULL: the
 // linear path, written into path_out), checking that the path is a
 // permutation of [0, N): *err (zeroed by the caller) is set otherwise.
