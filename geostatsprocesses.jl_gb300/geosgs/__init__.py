@@ -23,23 +23,28 @@ from .model import (
     MetricBall,
     NestedVariogram,
     RandomPath,
+    ShiftedPath,
+    SourcePath,
     RotX,
     RotY,
     RotZ,
     SphericalTransiogram,
     SphericalVariogram,
     georef,
+    nearest_nodes,
+    traverse,
 )
 from .plan import Batch, Plan
 from .problem import build_problem, clamped_neighbors
-from .simulation import (GPUSEQSIM, Ensemble, FieldSimulationMethod, expectedvalue, mean, posterior, preprocess,
-                         rand, randsingle)
+from .simulation import (GPUSEQSIM, Ensemble, FieldSimulationMethod, defaultsimulation, expectedvalue, mean, posterior,
+                         preprocess, rand, randsingle)
 
 __all__ = [
     "ArgumentError", "Batch", "CartesianGrid", "Ensemble", "ExplicitPath", "ExponentialVariogram",
     "FieldSimulationMethod", "GPUSEQSIM", "GaussianProcess", "GaussianVariogram", "GeoSGSError",
     "GeoTable", "ExponentialTransiogram", "GaussianTransiogram", "IndicatorProcess", "SphericalTransiogram",
     "LinearCoregionalization", "LinearPath", "MetricBall", "NestedVariogram", "Plan", "RandomPath", "RotX", "RotY", "RotZ",
-    "SphericalVariogram", "build_problem", "clamped_neighbors", "georef", "load_library", "trim_memory",
+    "ShiftedPath", "SourcePath", "SphericalVariogram", "build_problem", "clamped_neighbors", "defaultsimulation",
+    "georef", "load_library", "nearest_nodes", "traverse", "trim_memory",
     "expectedvalue", "mean", "posterior", "preprocess", "rand", "randsingle",
 ]

@@ -5,7 +5,8 @@ variograms / MetricBall    GeoStatsFunctions 0.15 / Meshes 0.57 (the reference's
                            dependencies): practical-range spherical, exponential
                            and gaussian variograms with nugget, anisotropy by a
                            rotated ellipsoid
-CartesianGrid, paths       Meshes 0.57 CartesianGrid, LinearPath, RandomPath
+CartesianGrid, paths       Meshes 0.57 CartesianGrid, LinearPath, RandomPath,
+                           ShiftedPath, SourcePath, traverse
 georef / GeoTable          GeoTables: values + point coordinates
 
 Only what the GPU SEQSIM path consumes is mirrored.
@@ -435,3 +436,151 @@ class ExplicitPath:
         if self.perm.shape != (n,):
             raise ArgumentError("path length does not match the domain")
         return self.perm
+
+
+class ShiftedPath:
+    """Meshes' ShiftedPath(path, offset): the order of `path` rotated so that
+    it starts at its entry `offset` (0-based; a negative offset counts from
+    the end) and wraps around to the entries before it."""
+
+    def __init__(self, path, offset: int):
+        self.path = path
+        self.offset = int(offset)
+
+    def order(self, domain):
+        p = traverse(domain, self.path)
+        return np.roll(p, -self.offset) if p.size else p
+
+
+# rows of one k-d tree query (bounds the query's index and distance arrays)
+_QUERY_ROWS = 1 << 20
+
+
+def _sorted_source_distances(tree, src_xyz, xyz, k):
+    """For each row of `xyz`, its Euclidean distances to its k nearest sources
+    in ascending order: neighbours from the k-d tree, distances recomputed
+    from the centroids in one FP64 order (squared coordinate differences
+    summed in axis order, then the square root)."""
+    out = np.empty((xyz.shape[0], k), dtype=np.float64)
+    for r0 in range(0, xyz.shape[0], _QUERY_ROWS):
+        x = xyz[r0: r0 + _QUERY_ROWS]
+        _, nb = tree.query(x, k=k)
+        nb = np.asarray(nb).reshape(x.shape[0], k)
+        diff = x[:, None, :] - src_xyz[nb]
+        s = diff[..., 0] * diff[..., 0]
+        for a in range(1, x.shape[1]):
+            s = s + diff[..., a] * diff[..., a]
+        out[r0: r0 + _QUERY_ROWS] = np.sort(np.sqrt(s), axis=1)
+    return out
+
+
+def _lexsort_rows(keys, ids, group=None):
+    """Indices ordering the rows of `keys` lexicographically (first column
+    first), then by `ids`; within `group` first when given."""
+    cols = [ids] + [keys[:, j] for j in reversed(range(keys.shape[1]))]
+    if group is not None:
+        cols.append(group)
+    return np.lexsort(tuple(cols))
+
+
+class SourcePath:
+    """Meshes' SourcePath(sources): the sources first, in the given order,
+    then the other nodes growing outwards from them.
+
+    Meshes 0.57 (a dependency the reference does not vendor) fits a k-d tree
+    to the sources' centroids, queries every other element for its distances
+    to all the sources, sorted ascending, and orders the elements by these
+    distance vectors compared lexicographically (the nearest source decides,
+    then the second nearest, and so on) in a stable sort over element order.
+    This restatement computes the same keys in FP64 and lets node id settle
+    what the vectors leave tied.  It refines lazily: the order is first taken
+    on each node's few nearest distances, and only runs of nodes still tied
+    get further columns, doubling until the ties break or every source is
+    used.  Sources are 0-based node ids.  The reference builds this path for
+    IndicatorProcess with data (src/simulation/field.jl:168-180)."""
+
+    def __init__(self, sources):
+        self.sources = np.asarray(sources, dtype=np.int64).reshape(-1)
+
+    def order(self, domain):
+        from scipy.spatial import cKDTree
+
+        n = domain.nelements()
+        src = self.sources
+        if src.size == 0:
+            raise ArgumentError("SourcePath needs at least one source")
+        if np.any(src < 0) or np.any(src >= n):
+            raise ArgumentError("sources must be valid locations")
+        if np.unique(src).size != src.size:
+            raise ArgumentError("non-unique sources")
+        others = np.setdiff1d(np.arange(n, dtype=np.int64), src)
+        if others.size == 0:
+            return src.astype(np.int32)
+        xyz = domain.centroids()
+        src_xyz = np.ascontiguousarray(xyz[src])
+        tree = cKDTree(src_xyz)
+        K = src.size
+        k = min(K, 4)
+        keys = _sorted_source_distances(tree, src_xyz, xyz[others], k)
+        order = _lexsort_rows(keys, others)
+        pos, run = _tied_runs(keys[order], np.zeros(others.size, dtype=np.int64))
+        while pos.size and k < K:
+            k = min(K, 2 * k)
+            mem = others[order[pos]]
+            keys = _sorted_source_distances(tree, src_xyz, xyz[mem], k)
+            o = _lexsort_rows(keys, mem, run)
+            order[pos] = order[pos][o]
+            sub, run = _tied_runs(keys[o], run[o])
+            pos = pos[sub]
+        return np.concatenate([src, others[order]]).astype(np.int32)
+
+
+def _tied_runs(keys, group):
+    """Rows (of sorted `keys`) that equal a neighbour row of the same group,
+    and a run id for each of them."""
+    same = np.all(keys[1:] == keys[:-1], axis=1) & (group[1:] == group[:-1])
+    tied = np.zeros(keys.shape[0], dtype=bool)
+    tied[1:] |= same
+    tied[:-1] |= same
+    starts = np.ones(keys.shape[0], dtype=bool)
+    starts[1:] = ~same
+    rid = np.cumsum(starts) - 1
+    sel = np.nonzero(tied)[0]
+    return sel, rid[sel]
+
+
+def traverse(domain, path) -> np.ndarray:
+    """The nodes of `domain` in the order `path` visits them, 0-based (Meshes'
+    traverse(domain, path), called once per realization at seqsim.jl:98)."""
+    perm = path_order(domain, path)
+    return np.arange(domain.nelements(), dtype=np.int32) if perm is None else np.asarray(perm, dtype=np.int32)
+
+
+def path_order(domain, path):
+    """What the library takes as the path: None for the linear order,
+    otherwise the permutation."""
+    if hasattr(path, "order"):
+        return path.order(domain)
+    return path.permutation(domain.nelements())
+
+
+def nearest_nodes(domain, coords) -> np.ndarray:
+    """The grid node whose centroid is nearest to each point (Meshes'
+    KNearestSearch(domain, 1), src/simulation/field.jl:173-177).  On a
+    regular grid the nearest centroid minimises each axis apart; equal
+    distances go to the lower cell on that axis, so to the lowest node id."""
+    c = np.asarray(coords, dtype=np.float64)
+    if c.ndim == 1:
+        c = c[:, None]
+    if c.shape[1] != domain.dim:
+        raise ArgumentError("point and grid dimensions differ")
+    node = np.zeros(c.shape[0], dtype=np.int64)
+    mult = 1
+    for j in range(domain.dim):
+        o, s, d = domain.origin[j], domain.spacing[j], domain.dims[j]
+        i0 = np.clip(np.floor((c[:, j] - o) / s).astype(np.int64), 0, d - 1)
+        cand = np.clip(i0[:, None] + np.array([-1, 0, 1]), 0, d - 1)
+        dist = np.abs(c[:, j][:, None] - (o + (cand + 0.5) * s))
+        node += cand[np.arange(c.shape[0]), np.argmin(dist, axis=1)] * mult
+        mult *= d
+    return node

@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, IndicatorProcess, MetricBall
+from .model import ArgumentError, CartesianGrid, GaussianProcess, GeoTable, IndicatorProcess, MetricBall, path_order
 
 _PREC = {"fp64": _abi.SGS_PREC_FP64, "fp32": _abi.SGS_PREC_FP32_REFINE}
 
@@ -108,7 +108,7 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
     p.device = int(getattr(method, "device", 0))
     p.flags = ((_abi.SGS_FLAG_ONE_LAUNCH_SWEEP if getattr(method, "one_launch_sweep", False) else 0)
                | (_abi.SGS_FLAG_LEVEL_SWEEP if getattr(method, "level_sweep", False) else 0))
-    perm = method.path.permutation(domain.nelements())
+    perm = path_order(domain, method.path)
     if perm is not None:
         perm = np.ascontiguousarray(perm, dtype=np.int32)
         keep.append(perm)

@@ -2,6 +2,7 @@
 
 rand(...)                 src/simulation/field.jl:47-124
 FieldSimulationMethod     src/simulation/field.jl:135
+defaultsimulation         src/simulation/field.jl:152-180
 preprocess / randsingle   src/simulation/field/seqsim.jl:50-156 (SEQSIM's pair)
 Ensemble                  src/ensembles.jl:10-52 (container + per-node mean/var)
 
@@ -32,7 +33,7 @@ import numpy as np
 from . import _abi
 from .model import (ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess, GeoTable, IndicatorProcess,
                     LinearCoregionalization,
-                    LinearPath, RandomPath)
+                    LinearPath, RandomPath, SourcePath, nearest_nodes)
 from .plan import Batch, Plan
 from .problem import build_problem, indicator_levels
 
@@ -186,6 +187,20 @@ def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc)
     return {preproc.var: col}
 
 
+def defaultsimulation(process, domain, *, data=None) -> GPUSEQSIM:
+    """The method `rand` uses when none is given (src/simulation/field.jl:
+    152-180).  The reference picks FFTSIM or LUSIM for some Gaussian cases;
+    this package provides the SEQSIM method only, so a GaussianProcess gets
+    GPUSEQSIM with SEQSIM's defaults.  An IndicatorProcess gets the
+    reference's path: linear without data; with data, a SourcePath that starts
+    at the grid nodes nearest to the data, each node once, in data order."""
+    if isinstance(process, IndicatorProcess) and data is not None:
+        nodes = nearest_nodes(domain, data.coords)
+        _, first = np.unique(nodes, return_index=True)
+        return GPUSEQSIM(path=SourcePath(nodes[np.sort(first)]))
+    return GPUSEQSIM()
+
+
 def _rng_of(x):
     if x is None:
         return np.random.default_rng()
@@ -213,7 +228,7 @@ def rand(*args, data=None, method=None, init=None, workers=None, async_=False,
         raise ArgumentError("rand(process, ...) takes a GaussianProcess or an IndicatorProcess")
     nreals = args[2] if len(args) == 3 else None
     rng = rng if rng is not None else _rng_of(None)
-    smethod = method if method is not None else GPUSEQSIM()
+    smethod = method if method is not None else defaultsimulation(process, domain, data=data)
     if not isinstance(smethod, GPUSEQSIM):
         raise ArgumentError("this package provides the GPUSEQSIM method only")
     if workers not in (None, [0], (0,)):

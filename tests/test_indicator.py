@@ -106,6 +106,40 @@ def test_rand_indicator_api(geosgs_lib):
     assert len(ens) == 3 and set(ens[0]["C"].tolist()) == {"a", "b", "c"}
 
 
+@pytest.mark.gpu
+def test_default_method_with_data_grows_from_the_data(oracle_mod, geosgs_lib):
+    """With data and no method, `rand` simulates an IndicatorProcess along the
+    reference's SourcePath (src/simulation/field.jl:168-180): the GPU follows
+    that path with categories identical to the oracle's on the same uniforms.
+    The path's first node sits on the first datum and has only data as
+    neighbours, so it takes that datum's category in every realization
+    (nugget 0).  Later data nodes need not: a system holding a datum and the
+    simulated node on the same centre is singular, and the node draws from
+    the prior as the reference's failed fit does."""
+    grid = geosgs.CartesianGrid((48, 40))
+    rng = np.random.default_rng(11)
+    cells = rng.choice(grid.nelements(), size=25, replace=False)
+    xyz = grid.centroids()[cells]
+    labels = rng.integers(0, 3, cells.size)
+    labels[:3] = [0, 1, 2]
+    data = geosgs.georef({"C": labels}, xyz)
+    proc = geosgs.IndicatorProcess(geosgs.SphericalTransiogram(range=9.0, proportions=(0.5, 0.3, 0.2)))
+    method = geosgs.defaultsimulation(proc, grid, data=data)
+    np.testing.assert_array_equal(method.path.sources, cells)
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    levels, dcat = gproblem.indicator_levels(proc, data)
+    G = geosgs.Plan(p, keep).set_indicator(proc.prob, dcat).prepare()
+    u = rng.uniform(0.0, 1.0, (8, G.N))
+    got = G.simulate_indicator(8, u=u)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    np.testing.assert_array_equal(got, O.simulate_indicator(8, proc.prob, dcat, u=u))
+    np.testing.assert_array_equal(got[:, cells[0]], np.full(8, dcat[0]))
+    G.close()
+    ens = geosgs.rand(np.random.default_rng(2), proc, grid, 2, data=data)
+    assert set(ens[0]["C"].tolist()) <= {0, 1, 2}
+    assert ens[0]["C"][cells[0]] == labels[0] and ens[1]["C"][cells[0]] == labels[0]
+
+
 # ---- full simple cokriging: linear models of coregionalization ----
 def lmc_model(L=3):
     """A non-separable indicator covariance: a short spherical structure and a
