@@ -18,7 +18,8 @@ RandomPath, each realization follows its own permutation, drawn one after
 another from the path's generator as the reference's
 `traverse(domain, path)` does on every realization (seqsim.jl:98): the
 realizations then run as a batch of independent problems (sgs_batch_*), one
-per realization, with their own neighbour tables and kriging systems.
+per realization, with their own neighbour tables and kriging systems.  An
+IndicatorProcess runs them as one plan per realization, in turn.
 
 mean / expectedvalue / posterior   src/expectation/field.jl:17-42 and
                                    src/expectation/field/gaussian.jl:5-25
@@ -96,6 +97,7 @@ class _Preproc:
     nreals: int = 1
     batches: Any = None  # per-realization paths: [(Batch, first realization, count)]
     levels: Any = None   # indicator simulation: category labels
+    indicator_paths: Any = None  # per-realization indicator paths: (process, domain, data, method, perms)
 
     def close(self):
         if self.plan is not None:
@@ -118,17 +120,14 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     (seqsim.jl:267-271 always uses ExplicitInit with data appended)."""
     seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
     if isinstance(process, IndicatorProcess):
-        if method.path_per_realization:
-            raise ArgumentError("per-realization paths are available for GaussianProcess")
-        levels, dcat = indicator_levels(process, data)
-        problem, keep = build_problem(process, domain, data, method)
-        plan = Plan(problem, keep)
-        if isinstance(process.func, LinearCoregionalization):  # full simple cokriging
-            plan.set_indicator_cokriging(process.prob, process.func.coef, dcat)
+        levels, _ = indicator_levels(process, data)
+        if method.path_per_realization and isinstance(method.path, RandomPath):
+            pre = _Preproc(plan=None, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+            pre.indicator_paths = (process, domain, data, method,
+                                   method.path.permutations(domain.nelements(), nreals))
         else:
-            plan.set_indicator(process.prob, dcat)
-        plan.prepare()
-        pre = _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+            pre = _Preproc(plan=_indicator_plan(process, domain, data, method), var=_varname(process, data),
+                           seed=seed, z=z, nreals=nreals)
         pre.levels = levels
         return pre
     if method.path_per_realization and isinstance(method.path, RandomPath):
@@ -137,6 +136,43 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     problem, keep = build_problem(process, domain, data, method)
     plan = Plan(problem, keep).prepare()
     return _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
+
+
+def _indicator_plan(process, domain, data, method):
+    """A prepared plan of an IndicatorProcess: the separable path, or full
+    simple cokriging for a linear model of coregionalization."""
+    _, dcat = indicator_levels(process, data)
+    problem, keep = build_problem(process, domain, data, method)
+    plan = Plan(problem, keep)
+    try:
+        if isinstance(process.func, LinearCoregionalization):
+            plan.set_indicator_cokriging(process.prob, process.func.coef, dcat)
+        else:
+            plan.set_indicator(process.prob, dcat)
+        plan.prepare()
+    except BaseException:
+        plan.close()
+        raise
+    return plan
+
+
+def _per_realization_indicator(pre):
+    """Categories of realizations that each follow their own permutation:
+    one plan per realization, created, prepared, simulated and destroyed in
+    turn (one plan's tables on the device at a time).  Realization r draws
+    with seed + r, or takes row r of the given uniforms."""
+    process, domain, data, method, perms = pre.indicator_paths
+    n = domain.nelements()
+    u = None if pre.z is None else np.asarray(pre.z, dtype=np.float64).reshape(pre.nreals, n)
+    out = np.empty((pre.nreals, n), dtype=np.int32)
+    for r in range(pre.nreals):
+        m = GPUSEQSIM(**{**method.__dict__, "path": ExplicitPath(perms[r]), "path_per_realization": False})
+        plan = _indicator_plan(process, domain, data, m)
+        try:
+            out[r] = plan.simulate_indicator(1, u=None if u is None else u[r:r + 1], seed=pre.seed + r)[0]
+        finally:
+            plan.close()
+    return out
 
 
 # node budget of one batch of per-realization problems (about 500 bytes of
@@ -165,7 +201,10 @@ def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc)
     simulates the whole block of `preproc.nreals` realizations on the GPU."""
     if preproc.block is None:
         if preproc.levels is not None:
-            cats = preproc.plan.simulate_indicator(preproc.nreals, u=preproc.z, seed=preproc.seed)
+            if preproc.indicator_paths is not None:
+                cats = _per_realization_indicator(preproc)
+            else:
+                cats = preproc.plan.simulate_indicator(preproc.nreals, u=preproc.z, seed=preproc.seed)
             preproc.block = np.asarray(preproc.levels, dtype=object if isinstance(preproc.levels[0], str)
                                        else None)[cats]
         elif preproc.batches is not None:

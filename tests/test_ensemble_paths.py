@@ -77,3 +77,34 @@ def test_per_realization_paths_match_oracle(precision, oracle_mod, geosgs_lib):
         p, keep = geosgs.build_problem(wl.process, wl.domain, wl.data, m)
         O = oracle_mod.OraclePlan(p, keep).prepare()
         assert rel_err(ens[r]["Z"][None, :], O.simulate(1, z[r:r + 1])) <= VALUE_TOL, r
+
+
+@pytest.mark.gpu
+def test_per_realization_indicator_paths_match_oracle(oracle_mod, geosgs_lib):
+    """An IndicatorProcess with per-realization paths: realization r follows
+    the r-th permutation of the RandomPath's generator, categories identical
+    to the oracle's on that permutation and the same uniforms."""
+    from geosgs import problem as gproblem
+
+    wl = workloads.small(n=26, k=10, ndata=14, vario="sph", nugget=0.0, seed=4)
+    R = 3
+    rng = np.random.default_rng(8)
+    labels = rng.integers(0, 3, wl.data.nrow())
+    labels[:3] = [0, 1, 2]
+    data = geosgs.georef({"C": labels}, wl.data.coords)
+    proc = geosgs.IndicatorProcess(geosgs.SphericalTransiogram(range=6.0, proportions=(0.5, 0.3, 0.2)))
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(17), maxneighbors=10, path_per_realization=True)
+    u = rng.uniform(0.0, 1.0, (R, wl.domain.nelements()))
+    ens = geosgs.rand(np.random.default_rng(1), proc, wl.domain, R, data=data, method=method, z=u)
+    perms = geosgs.RandomPath(17).permutations(wl.domain.nelements(), R)
+    levels, dcat = gproblem.indicator_levels(proc, data)
+    for r in range(R):
+        m = geosgs.GPUSEQSIM(path=geosgs.ExplicitPath(perms[r]), maxneighbors=10)
+        p, keep = geosgs.build_problem(proc, wl.domain, data, m)
+        O = oracle_mod.OraclePlan(p, keep).prepare()
+        want = np.asarray(levels)[O.simulate_indicator(1, proc.prob, dcat, u=u[r:r + 1])[0]]
+        np.testing.assert_array_equal(ens[r]["C"], want)
+    # the shared-path form differs: every realization on the first permutation
+    shared = geosgs.rand(np.random.default_rng(1), proc, wl.domain, R, data=data, z=u,
+                         method=geosgs.GPUSEQSIM(path=geosgs.RandomPath(17), maxneighbors=10))
+    np.testing.assert_array_equal(shared[0]["C"], ens[0]["C"])
