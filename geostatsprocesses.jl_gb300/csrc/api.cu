@@ -102,6 +102,15 @@ struct sgs_plan {
     double cok_tau = 0.0;
     int32_t *d_cok_m = nullptr, *d_cok_idx = nullptr;
     double *d_cok_w = nullptr, *d_cok_cst = nullptr;
+    int cok_L = 0;                // L the cokriging tables were allocated for
+    // multivariate Gaussian simulation (sgs_plan_set_multivariate): the same
+    // systems with the variables' means and the data's values, plus each
+    // position's factor of its conditional covariance
+    bool mv = false;
+    int mv_nvars = 0;
+    double mv_mean[IND_MAX_CAT] = {};
+    double* d_mv_dval = nullptr;  // [D][L]
+    double* d_mv_fac = nullptr;   // [N][L][L]
     // FP32 refinement whose weights amplify the rounding of FP32 values: the
     // sweep keeps FP64 values, from FP64 copies of the (hi, lo) tables
     unsigned int* d_wl1 = nullptr;
@@ -872,16 +881,29 @@ static int run_solve(sgs_plan* P, double* w_full, double* sigma_full) {
 
 static CokArgs cok_args(const sgs_plan* P) {
     CokArgs c{};
-    c.ncat = P->ind_ncat;
-    for (int l = 0; l < IND_MAX_CAT; ++l) c.prob[l] = P->ind_prob[l];
+    c.ncat = P->mv ? P->mv_nvars : P->ind_ncat;
+    for (int l = 0; l < IND_MAX_CAT; ++l) c.prob[l] = P->mv ? P->mv_mean[l] : P->ind_prob[l];
     c.coef = P->d_cok_coef;
     c.data_cat = P->d_ind_cat;
+    c.data_val = P->d_mv_dval;
     c.tau = P->cok_tau;
     c.m = P->d_cok_m;
     c.idx = P->d_cok_idx;
     c.w = P->d_cok_w;
     c.cst = P->d_cok_cst;
+    c.fac = P->d_mv_fac;
     return c;
+}
+
+static void free_cok_tables(sgs_plan* P) {
+    dfree(P, P->d_cok_m);
+    dfree(P, P->d_cok_idx);
+    dfree(P, P->d_cok_w);
+    dfree(P, P->d_cok_cst);
+    dfree(P, P->d_mv_fac);
+    P->d_cok_m = P->d_cok_idx = nullptr;
+    P->d_cok_w = P->d_cok_cst = P->d_mv_fac = nullptr;
+    P->cok_L = 0;
 }
 
 extern "C" int sgs_plan_prepare(sgs_plan* P) {
@@ -1056,15 +1078,19 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
             LAUNCH(P, 1, launch_tables_to_fp64(P->t32, P->t64p, N, N * (int64_t)k, st));
         }
     }
-    if (P->cok) {
+    if (P->cok || P->mv) {
         // cokriging systems of every position (they replace the nodes' status)
-        const int L = P->ind_ncat;
+        const int L = P->mv ? P->mv_nvars : P->ind_ncat;
+        if (P->d_cok_m && P->cok_L != L) free_cok_tables(P);
         if (!P->d_cok_m) {
             if ((rc = dalloc(P, &P->d_cok_m, N))) return rc;
             if ((rc = dalloc(P, &P->d_cok_idx, (size_t)N * k))) return rc;
             if ((rc = dalloc(P, &P->d_cok_w, (size_t)N * k * L * L))) return rc;
             if ((rc = dalloc(P, &P->d_cok_cst, (size_t)N * L))) return rc;
+            P->cok_L = L;
         }
+        if (P->mv && !P->d_mv_fac)
+            if ((rc = dalloc(P, &P->d_mv_fac, (size_t)N * L * L))) return rc;
         SolveArgs s{};
         s.grid = P->grid;
         s.vario = P->vario;
@@ -1077,7 +1103,7 @@ extern "C" int sgs_plan_prepare(sgs_plan* P) {
         s.N = P->N;
         s.data_xyz = P->d_dxyz;
         s.status = P->d_status;
-        LAUNCH(P, 1, launch_cok_solve(s, cok_args(P), st));
+        LAUNCH(P, 1, launch_cok_solve(s, cok_args(P), P->mv, st));
     }
     CK(P, cudaEventRecord(P->ev[4], st));
     LAUNCH(P, 1, launch_count_nonzero(N, P->d_status, P->d_stats + 2, P->nsm, st));
@@ -1704,6 +1730,7 @@ extern "C" int sgs_plan_set_indicator(sgs_plan* P, int32_t ncat, const double* p
     P->ind_ncat = ncat;
     for (int l = 0; l < IND_MAX_CAT; ++l) P->ind_prob[l] = l < ncat ? prob[l] / s : 0.0;
     P->cok = false;
+    P->mv = false;
     P->prepared = false;
     return SGS_OK;
 }
@@ -1720,14 +1747,7 @@ extern "C" int sgs_plan_set_indicator_cokriging(sgs_plan* P, int32_t ncat, const
     const int old_ncat = P->ind_ncat;
     int rc = sgs_plan_set_indicator(P, ncat, prob, data_cat);
     if (rc) return rc;
-    if (old_ncat != ncat) {  // table sizes change: reallocate at the next prepare
-        dfree(P, P->d_cok_m);
-        dfree(P, P->d_cok_idx);
-        dfree(P, P->d_cok_w);
-        dfree(P, P->d_cok_cst);
-        P->d_cok_m = P->d_cok_idx = nullptr;
-        P->d_cok_w = P->d_cok_cst = nullptr;
-    }
+    if (old_ncat != ncat) free_cok_tables(P);  // table sizes change: reallocate at the next prepare
     // the singular rule's scale: the largest indicator variance
     double vmax = 0.0;
     for (int a = 0; a < ncat; ++a) {
@@ -1801,6 +1821,120 @@ extern "C" int sgs_plan_simulate_indicator(sgs_plan* P, int32_t R, const double*
     LAUNCH(P, 1, launch_cats_to_out(C, N, R, Rp, od, st));
     CK(P, cudaMemcpyAsync(out, od, (size_t)N * R * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     P->info.d2h_bytes += (int64_t)N * R * sizeof(int32_t);
+    CK(P, cudaStreamSynchronize(st));
+    P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
+    cleanup();
+    return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multivariate Gaussian simulation (indicator.cu, the GAUSS form of the
+// cokriging systems): a GaussianProcess whose function is a linear model of
+// coregionalization over the plan's structures.
+extern "C" int sgs_plan_set_multivariate(sgs_plan* P, int32_t nvars, const double* mean, const double* coef,
+                                         const double* data_values) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (nvars < 1 || nvars > IND_MAX_CAT) return set_err(P, SGS_ERR_ARG, "nvars must be in 1..8");
+    if ((int64_t)nvars * P->k > COK_MAX)
+        return set_err(P, SGS_ERR_ARG, "maxneighbors x variables must be at most 64 for cokriging");
+    if (!mean || !coef) return set_err(P, SGS_ERR_ARG, "null means or coregionalization matrices");
+    if (P->D > 0 && !data_values) return set_err(P, SGS_ERR_ARG, "null data values");
+    const int S = P->vario.ns, L = nvars;
+    for (int a = 0; a < L; ++a)
+        if (!std::isfinite(mean[a])) return set_err(P, SGS_ERR_ARG, "means must be finite");
+    for (int s = 0; s < S; ++s)
+        for (int a = 0; a < L; ++a)
+            for (int b = 0; b < L; ++b) {
+                const double v = coef[((size_t)s * L + a) * L + b];
+                if (!std::isfinite(v)) return set_err(P, SGS_ERR_ARG, "coregionalization matrices must be finite");
+                if (v != coef[((size_t)s * L + b) * L + a])
+                    return set_err(P, SGS_ERR_ARG, "coregionalization matrices must be symmetric");
+            }
+    for (int64_t i = 0; i < P->D * L; ++i)
+        if (!std::isfinite(data_values[i])) return set_err(P, SGS_ERR_ARG, "data values must be finite");
+    // the singular rule's scale: the largest variance of a variable
+    double vmax = 0.0;
+    for (int a = 0; a < L; ++a) {
+        double v = 0.0;
+        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + a] * P->vario.st[s].sill;
+        vmax = std::max(vmax, v);
+    }
+    if (!(vmax > 0.0)) return set_err(P, SGS_ERR_ARG, "the model's variances must be positive");
+    CK(P, cudaSetDevice(P->device));
+    int rc;
+    dfree(P, P->d_cok_coef);
+    P->d_cok_coef = nullptr;
+    std::vector<double> cf(coef, coef + (size_t)S * L * L);
+    if ((rc = upload(P, &P->d_cok_coef, cf.data(), cf.size()))) return rc;
+    dfree(P, P->d_mv_dval);
+    P->d_mv_dval = nullptr;
+    if (P->D > 0) {
+        std::vector<double> dv(data_values, data_values + (size_t)P->D * L);
+        if ((rc = upload(P, &P->d_mv_dval, dv.data(), dv.size()))) return rc;
+    }
+    CK(P, cudaStreamSynchronize(P->stream));
+    // leave indicator mode: its per-position sums are not computed any more
+    dfree(P, P->d_ind_wsum);
+    dfree(P, P->d_ind_dsum);
+    P->d_ind_wsum = P->d_ind_dsum = nullptr;
+    P->ind_ncat = 0;
+    P->cok = false;
+    for (int a = 0; a < IND_MAX_CAT; ++a) P->mv_mean[a] = a < L ? mean[a] : 0.0;
+    P->mv_nvars = L;
+    P->cok_tau = kSingularTau * vmax;
+    P->mv = true;
+    P->prepared = false;
+    return SGS_OK;
+}
+
+extern "C" int sgs_plan_simulate_multivariate(sgs_plan* P, int32_t R, const double* z, uint64_t seed, double* out) {
+    if (!P) return set_err(nullptr, SGS_ERR_ARG, "null plan");
+    if (!P->mv) return set_err(P, SGS_ERR_STATE, "no multivariate model set (sgs_plan_set_multivariate)");
+    if (!P->prepared) return set_err(P, SGS_ERR_STATE, "simulate before prepare");
+    if (R < 1 || !out) return set_err(P, SGS_ERR_ARG, "invalid nreals or output");
+    CK(P, cudaSetDevice(P->device));
+    const int L = P->mv_nvars;
+    const int64_t N = P->N, NL = N * L;
+    const int Rp = (R + 3) / 4 * 4;
+    cudaStream_t st = P->stream;
+    int rc;
+    double *V = nullptr, *zin = nullptr, *zr = nullptr, *od = nullptr;
+    auto cleanup = [&]() {
+        dfree(P, V);
+        dfree(P, zin);
+        dfree(P, zr);
+        dfree(P, od);
+    };
+    if ((rc = dalloc(P, &V, (size_t)NL * Rp))) return rc;
+    if (z) {
+        if ((rc = dalloc(P, &zin, (size_t)NL * R)) || (rc = dalloc(P, &zr, (size_t)NL * Rp))) {
+            cleanup();
+            return rc;
+        }
+        CK(P, cudaMemcpyAsync(zin, z, (size_t)NL * R * sizeof(double), cudaMemcpyHostToDevice, st));
+        P->info.h2d_bytes += NL * R * (int64_t)sizeof(double);
+        // nreals x (L N) -> rows [L N][Rp]: row a*N + g holds variable a of node g
+        LAUNCH(P, 1, launch_z_to_rows_fp64(zin, NL, R, Rp, zr, st));
+    }
+    const CokArgs c = cok_args(P);
+    CK(P, cudaEventRecord(P->ev[5], st));
+    for (int l = 0; l < P->nlevels; ++l) {
+        const int64_t p0 = P->h_loff[l], p1 = P->h_loff[l + 1];
+        cudaError_t e = launch_mv_level(c, P->d_order, P->k, N, p0, p1, Rp, zr, seed, V, st);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cuda_err(P, e, "multivariate sweep launch");
+        }
+        if (p1 > p0) P->info.launches++;
+    }
+    CK(P, cudaEventRecord(P->ev[6], st));
+    if ((rc = dalloc(P, &od, (size_t)NL * R))) {
+        cleanup();
+        return rc;
+    }
+    LAUNCH(P, 1, launch_rows_to_out_fp64(V, NL, R, Rp, 0.0, od, st));
+    CK(P, cudaMemcpyAsync(out, od, (size_t)NL * R * sizeof(double), cudaMemcpyDeviceToHost, st));
+    P->info.d2h_bytes += NL * R * (int64_t)sizeof(double);
     CK(P, cudaStreamSynchronize(st));
     P->info.ms_sweep = elapsed(P->ev[5], P->ev[6]);
     cleanup();

@@ -166,13 +166,44 @@ cudaError_t launch_sis_level_fp64(const SweepTables<double>& t, int k, int64_t p
 //   p_t = prob_t + sum_i sum_a Lambda[(i, a), t] (I_a(x_i) - prob_a)
 //       = cst_t + sum_{grid nbrs j} w[j][cat_j][t],
 // the data's terms and every prob term folded into cst.
+//
+// Multivariate Gaussian simulation (GAUSS: a GaussianProcess whose function
+// is such a model, seqsim.jl:277-290 Kriging(f, mu) with an MvNormal prior,
+// predictprob's MvNormal conditional) solves the same systems with the L
+// variables' values in place of indicators:
+//   mu^_t = mu_t + sum_i sum_a Lambda[(i, a), t] (v_a(x_i) - mu_a)
+//   S^    = C(0) - c' Lambda          (c: the right-hand sides, nL x L)
+// and stores the lower Cholesky factor F of S^ (of C(0) for a node drawn from
+// the prior): v = mu^ + F z.  F's rule: a pivot not above tau contributes
+// nothing (its column of F is zero), so a conditional covariance that is zero
+// up to rounding (a node on a datum) draws no noise.
 constexpr int COK_WARPS = 2;
 
-__host__ __device__ constexpr size_t cok_smem_per_warp() {
-    return (size_t)COK_MAX * (COK_MAX + 1) * sizeof(double)  // LHS
-           + (size_t)COK_MAX * IND_MAX_CAT * sizeof(double)  // right-hand sides -> weights
-           + (size_t)COK_MAX * sizeof(double)                // one column being solved
-           + (size_t)KMAX * 4 * sizeof(int);                 // neighbour cells / data ids
+__host__ __device__ constexpr size_t cok_smem_per_warp(bool gauss) {
+    return (size_t)COK_MAX * (COK_MAX + 1) * sizeof(double)                // LHS
+           + (size_t)COK_MAX * IND_MAX_CAT * sizeof(double)                // right-hand sides -> weights
+           + (size_t)COK_MAX * sizeof(double)                              // one column being solved
+           + (gauss ? (size_t)COK_MAX * IND_MAX_CAT * sizeof(double) : 0)  // right-hand sides kept
+           + (size_t)KMAX * 4 * sizeof(int);                               // neighbour cells / data ids
+}
+
+// lower Cholesky factor of the L x L symmetric matrix S (lower triangle,
+// row-major) into F (full L x L, zero above the diagonal); pivots not above
+// tau give zero columns
+__device__ __forceinline__ void mv_factor(const double* S, int L, double tau, double* F) {
+    for (int i = 0; i < L * L; ++i) F[i] = 0.0;
+    for (int j = 0; j < L; ++j) {
+        double d = S[j * L + j];
+        for (int l = 0; l < j; ++l) d -= F[j * L + l] * F[j * L + l];
+        if (!(d > tau)) continue;
+        const double fjj = sqrt(d);
+        F[j * L + j] = fjj;
+        for (int i = j + 1; i < L; ++i) {
+            double t = S[i * L + j];
+            for (int l = 0; l < j; ++l) t -= F[i * L + l] * F[j * L + l];
+            F[i * L + j] = t / fjj;
+        }
+    }
 }
 
 __device__ __forceinline__ double structure_cov(const VarioStructDev& v, int dim, double h0, double h1, double h2) {
@@ -196,14 +227,17 @@ __device__ __forceinline__ void cok_lag(const SolveArgs& a, const int* ca, const
     }
 }
 
+template <bool GAUSS>
 __global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveArgs a, const CokArgs c) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    unsigned char* base = smem + (size_t)wib * cok_smem_per_warp();
+    unsigned char* base = smem + (size_t)wib * cok_smem_per_warp(GAUSS);
     double* A = reinterpret_cast<double*>(base);
     double* rhs = A + COK_MAX * (COK_MAX + 1);
     double* col = rhs + COK_MAX * IND_MAX_CAT;
-    int* cell = reinterpret_cast<int*>(col + COK_MAX);  // [n][4]: c0, c1, c2, data id (-1: grid)
+    double* rhs0 = col + COK_MAX;  // GAUSS: the right-hand sides, kept
+    int* cell = reinterpret_cast<int*>(GAUSS ? rhs0 + COK_MAX * IND_MAX_CAT : rhs0);  // [n][4]: c0, c1, c2,
+                                                                                       // data id (-1: grid)
     const GridDev& G = a.grid;
     const int L = c.ncat, k = a.k, S = a.vario.ns;
     const int nwarps = gridDim.x * COK_WARPS;
@@ -255,6 +289,7 @@ __global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveAr
                         double v = 0.0;
                         for (int s = 0; s < S; ++s) v += c.coef[(s * L + ai) * L + t] * cs[s];
                         rhs[(i * L + ai) * IND_MAX_CAT + t] = v;
+                        if constexpr (GAUSS) rhs0[(i * L + ai) * IND_MAX_CAT + t] = v;
                     }
             }
             __syncwarp();
@@ -269,6 +304,26 @@ __global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveAr
                 __syncwarp();
             }
         }
+        if constexpr (GAUSS) {
+            // conditional covariance C(0) - c' Lambda (the prior's C(0) for a
+            // node without a system), lower triangle into col, then its factor
+            for (int e = lane; e < L * L; e += 32) {
+                const int t = e / L, u = e - t * L;
+                if (u > t) continue;
+                double v = 0.0;
+                for (int s = 0; s < S; ++s) v += c.coef[(s * L + t) * L + u] * a.vario.st[s].sill;
+                if (kriged)
+                    for (int r = 0; r < m; ++r) v -= rhs0[r * IND_MAX_CAT + t] * rhs[r * IND_MAX_CAT + u];
+                col[t * L + u] = v;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                double F[IND_MAX_CAT * IND_MAX_CAT];
+                mv_factor(col, L, c.tau, F);
+                for (int i = 0; i < L * L; ++i) c.fac[pos * L * L + i] = F[i];
+            }
+            __syncwarp();
+        }
         // outputs: grid neighbours compacted in neighbour order, prob and
         // data terms folded into cst
         int mg = 0;
@@ -280,15 +335,28 @@ __global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveAr
                 const bool isgrid = i < n && cell[4 * i + 3] < 0;
                 const unsigned bal = __ballot_sync(FULL_MASK, isgrid);
                 if (i < n) {
-                    const int dcat = isgrid ? -1 : c.data_cat[cell[4 * i + 3]];
-                    for (int t = 0; t < L; ++t) {
-                        double v = 0.0;
-                        for (int ai = 0; ai < L; ++ai) {
-                            const double lam = rhs[(i * L + ai) * IND_MAX_CAT + t];
-                            v -= lam * c.prob[ai];
-                            if (ai == dcat) v += lam;
+                    if constexpr (GAUSS) {
+                        const int d = isgrid ? -1 : cell[4 * i + 3];
+                        for (int t = 0; t < L; ++t) {
+                            double v = 0.0;
+                            for (int ai = 0; ai < L; ++ai) {
+                                const double lam = rhs[(i * L + ai) * IND_MAX_CAT + t];
+                                v -= lam * c.prob[ai];
+                                if (d >= 0) v += lam * c.data_val[(int64_t)d * L + ai];
+                            }
+                            cst[t] += v;
                         }
-                        cst[t] += v;
+                    } else {
+                        const int dcat = isgrid ? -1 : c.data_cat[cell[4 * i + 3]];
+                        for (int t = 0; t < L; ++t) {
+                            double v = 0.0;
+                            for (int ai = 0; ai < L; ++ai) {
+                                const double lam = rhs[(i * L + ai) * IND_MAX_CAT + t];
+                                v -= lam * c.prob[ai];
+                                if (ai == dcat) v += lam;
+                            }
+                            cst[t] += v;
+                        }
                     }
                     if (isgrid) {
                         const int jj = mg + __popc(bal & lanemask_lt());
@@ -316,20 +384,26 @@ __global__ void __launch_bounds__(COK_WARPS * 32) cok_solve_kernel(const SolveAr
     }
 }
 
-cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, cudaStream_t s) {
+template <bool GAUSS>
+static cudaError_t cok_solve(const SolveArgs& a, const CokArgs& c, cudaStream_t s) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const size_t smem = cok_smem_per_warp() * COK_WARPS;
-    cudaError_t e = cudaFuncSetAttribute(cok_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = cok_smem_per_warp(GAUSS) * COK_WARPS;
+    cudaError_t e =
+        cudaFuncSetAttribute(cok_solve_kernel<GAUSS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cok_solve_kernel, COK_WARPS * 32, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cok_solve_kernel<GAUSS>, COK_WARPS * 32, smem);
     if (per_sm < 1) per_sm = 1;
     const int64_t want = (a.P + COK_WARPS - 1) / COK_WARPS;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)nsm * per_sm));
-    cok_solve_kernel<<<blocks, COK_WARPS * 32, smem, s>>>(a, c);
+    cok_solve_kernel<GAUSS><<<blocks, COK_WARPS * 32, smem, s>>>(a, c);
     return cudaGetLastError();
+}
+
+cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, bool gaussian, cudaStream_t s) {
+    return gaussian ? cok_solve<true>(a, c, s) : cok_solve<false>(a, c, s);
 }
 
 // One level: one thread per (position, 4 realizations).
@@ -382,6 +456,96 @@ cudaError_t launch_cok_level(const CokArgs& c, const int32_t* node, int k, int64
     int64_t blocks = ((p1 - p0) * (Rp / 4) + 255) / 256;
     if (blocks > (1 << 20)) blocks = 1 << 20;
     cok_level_kernel<<<(int)blocks, 256, 0, s>>>(c, node, k, p0, p1, Rp, u, seed, C);
+    return cudaGetLastError();
+}
+
+// One level of the multivariate Gaussian sweep: one thread per (position,
+// 4 realizations).  mu^_t = cst_t + sum_j sum_b w[j][b][t] v_b(x_j) over the
+// system's grid neighbours, then v = mu^ + F z with z the given normals or
+// the seeded ones of pseudo-node a*N + g (variable a of node g).
+__global__ void __launch_bounds__(256) mv_level_kernel(const CokArgs c, const int32_t* __restrict__ node, int k,
+                                                       int64_t N, int64_t p0, int64_t p1, int Rp,
+                                                       const double* __restrict__ z, uint64_t seed,
+                                                       double* __restrict__ V) {
+    const int cpn = Rp >> 2, L = c.ncat;
+    const int64_t total = (p1 - p0) * cpn;
+    for (int64_t it = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; it < total;
+         it += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pos = p0 + it / cpn;
+        const int ch = (int)(it % cpn);
+        const int64_t g = node[pos];
+        const int m = c.m[pos];
+        double mu[4][IND_MAX_CAT];
+#pragma unroll
+        for (int t = 0; t < IND_MAX_CAT; ++t) {
+            const double v = t < L ? c.cst[pos * L + t] : 0.0;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) mu[r][t] = v;
+        }
+        for (int j = 0; j < m; ++j) {
+            const int64_t e = pos * k + j;
+            const int64_t nb = c.idx[e];
+            for (int b = 0; b < L; ++b) {
+                const double* vb = V + ((int64_t)b * N + nb) * Rp + 4 * ch;
+                const double v0 = vb[0], v1 = vb[1], v2 = vb[2], v3 = vb[3];
+                const double* wr = c.w + (e * L + b) * L;
+#pragma unroll
+                for (int t = 0; t < IND_MAX_CAT; ++t)
+                    if (t < L) {
+                        const double wt = wr[t];
+                        mu[0][t] += wt * v0;
+                        mu[1][t] += wt * v1;
+                        mu[2][t] += wt * v2;
+                        mu[3][t] += wt * v3;
+                    }
+            }
+        }
+        double zz[4][IND_MAX_CAT];
+#pragma unroll
+        for (int a = 0; a < IND_MAX_CAT; ++a) {
+            if (a < L) {
+                if (z) {
+                    const double* za = z + ((int64_t)a * N + g) * Rp + 4 * ch;
+                    zz[0][a] = za[0];
+                    zz[1][a] = za[1];
+                    zz[2][a] = za[2];
+                    zz[3][a] = za[3];
+                } else {
+                    const float4 f = normals4(seed, (int64_t)a * N + g, ch);
+                    zz[0][a] = f.x;
+                    zz[1][a] = f.y;
+                    zz[2][a] = f.z;
+                    zz[3][a] = f.w;
+                }
+            } else {
+                zz[0][a] = zz[1][a] = zz[2][a] = zz[3][a] = 0.0;
+            }
+        }
+        const double* F = c.fac + pos * L * L;
+#pragma unroll
+        for (int t = 0; t < IND_MAX_CAT; ++t) {
+            if (t < L) {
+#pragma unroll
+                for (int u = 0; u < IND_MAX_CAT; ++u)
+                    if (u <= t) {
+                        const double f = F[t * L + u];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) mu[r][t] += f * zz[r][u];
+                    }
+                double* vt = V + ((int64_t)t * N + g) * Rp + 4 * ch;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) vt[r] = mu[r][t];
+            }
+        }
+    }
+}
+
+cudaError_t launch_mv_level(const CokArgs& c, const int32_t* node, int k, int64_t N, int64_t p0, int64_t p1, int Rp,
+                            const double* z, uint64_t seed, double* V, cudaStream_t s) {
+    if (p1 <= p0) return cudaSuccess;
+    int64_t blocks = ((p1 - p0) * (Rp / 4) + 255) / 256;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    mv_level_kernel<<<(int)blocks, 256, 0, s>>>(c, node, k, N, p0, p1, Rp, z, seed, V);
     return cudaGetLastError();
 }
 

@@ -228,23 +228,35 @@ cudaError_t launch_cats_to_out(const uint8_t* C, int64_t N, int R, int Rp, int32
 // Full simple cokriging of the indicators (indicator.cu) for a linear model
 // of coregionalization C_ab(h) = sum_s coef[s][a][b] C_s(h) over the
 // structures of the plan's variogram.  Unknowns per system: n x L <= COK_MAX.
+// The same systems serve multivariate Gaussian simulation (a GaussianProcess
+// whose function is such a model): there L is the number of variables,
+// `prob` holds their means, the data's L values replace their categories and
+// the solve also factors each node's conditional covariance.
 constexpr int COK_MAX = 64;
 struct CokArgs {
     int ncat;                    // L
-    double prob[IND_MAX_CAT];    // prior probabilities (normalized)
+    double prob[IND_MAX_CAT];    // prior probabilities (normalized); Gaussian: the means
     const double* coef;          // [S][L][L]
-    const int32_t* data_cat;     // [D] data categories
+    const int32_t* data_cat;     // [D] data categories (indicator)
+    const double* data_val;      // [D][L] data values (Gaussian)
     double tau;                  // singular pivot threshold (absolute)
     int32_t* m;                  // [P] grid neighbours of the position's system
     int32_t* idx;                // [P][k] their node ids
     double* w;                   // [P][k][L][L] weight of (grid neighbour j, its category b) for category t
     double* cst;                 // [P][L] prior term and the data's contribution
+    double* fac;                 // [P][L][L] Gaussian: lower Cholesky factor of the conditional
+                                 // covariance (of the prior's for prior nodes), row-major
 };
 // systems of every position (a: geometry, neighbours, order, status; the
 // status of each node is overwritten with its cokriging status)
-cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, cudaStream_t s);
+cudaError_t launch_cok_solve(const SolveArgs& a, const CokArgs& c, bool gaussian, cudaStream_t s);
 cudaError_t launch_cok_level(const CokArgs& c, const int32_t* node, int k, int64_t p0, int64_t p1, int Rp,
                              const double* u, uint64_t seed, uint8_t* C, cudaStream_t s);
+// One level of the multivariate Gaussian sweep.  V: values [L][N][Rp]
+// (variable-major rows of Rp realizations); z: the normals in the same
+// layout, or null for the seeded normals of pseudo-node a*N + g.
+cudaError_t launch_mv_level(const CokArgs& c, const int32_t* node, int k, int64_t N, int64_t p0, int64_t p1, int Rp,
+                            const double* z, uint64_t seed, double* V, cudaStream_t s);
 
 // Host-side description of one problem (api.cu: host_domain): everything
 // sgs_plan_create derives on the host before uploading.

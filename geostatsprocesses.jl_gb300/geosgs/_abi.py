@@ -38,6 +38,7 @@ SGS_FLAG_OUTPUT_STAGED = 8
 SGS_NN_FEATURES = 8
 SGS_NN_PARAMS = 2401
 SGS_IND_MAX_CATEGORIES = 8
+SGS_MV_MAX_VARIABLES = 8
 
 SGS_NODE_KRIGED = 0
 SGS_NODE_PRIOR_NMIN = 1
@@ -210,6 +211,8 @@ EXPORTS = (
     "sgs_plan_set_indicator",
     "sgs_plan_set_indicator_cokriging",
     "sgs_plan_simulate_indicator",
+    "sgs_plan_set_multivariate",
+    "sgs_plan_simulate_multivariate",
     "sgs_ensemble_stats",
     "sgs_ensemble_cdf",
     "sgs_ensemble_quantile",
@@ -315,6 +318,10 @@ def _declare(lib):
     lib.sgs_plan_set_indicator_cokriging.restype = C.c_int
     lib.sgs_plan_simulate_indicator.argtypes = [P, C.c_int32, dp, C.c_uint64, ip]
     lib.sgs_plan_simulate_indicator.restype = C.c_int
+    lib.sgs_plan_set_multivariate.argtypes = [P, C.c_int32, dp, dp, dp]
+    lib.sgs_plan_set_multivariate.restype = C.c_int
+    lib.sgs_plan_simulate_multivariate.argtypes = [P, C.c_int32, dp, C.c_uint64, dp]
+    lib.sgs_plan_simulate_multivariate.restype = C.c_int
     lib.sgs_krige.argtypes = [C.POINTER(SgsProblem), dp, dp]
     lib.sgs_krige.restype = C.c_int
     lib.sgs_ensemble_stats.argtypes = [P, C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_double, P, P, P]

@@ -208,15 +208,34 @@ class NestedVariogram(_Variogram):
 class GaussianProcess:
     """GaussianProcess(func, mean=0) — src/processes/field/gaussian.jl:22-35.
 
-    Univariate only on the GPU path (a variogram and a scalar mean)."""
+    A variogram with a scalar mean, or a multivariate function (a linear
+    model of coregionalization of L variables) with L means (zeros by
+    default, as gaussian.jl:35 gives)."""
 
-    def __init__(self, func, mean: float = 0.0):
+    def __init__(self, func, mean=None):
+        if isinstance(func, LinearCoregionalization):
+            L = func.nvariables
+            m = np.zeros(L) if mean is None else np.asarray(mean, dtype=np.float64).reshape(-1)
+            if m.size != L:  # gaussian.jl:28-30
+                raise ArgumentError(f"mean must have {L} components, received {m.size}")
+            if not np.all(np.isfinite(m)):
+                raise ArgumentError("mean must be finite")
+            self.func = func
+            self.mean = tuple(float(x) for x in m)
+            return
         if not isinstance(func, _Variogram):
-            raise ArgumentError("GaussianProcess on the GPU path takes a variogram")
-        if np.ndim(mean) != 0:
-            raise ArgumentError("mean must be a scalar (univariate process)")
+            raise ArgumentError("GaussianProcess on the GPU path takes a variogram or a linear model of "
+                                "coregionalization")
+        if mean is None:
+            mean = 0.0
+        if np.ndim(mean) != 0 and np.size(mean) != 1:
+            raise ArgumentError(f"mean must have 1 components, received {np.size(mean)}")
         self.func = func
-        self.mean = float(mean)
+        self.mean = float(np.asarray(mean).reshape(-1)[0])
+
+    @property
+    def nvariables(self) -> int:
+        return self.func.nvariables if isinstance(self.func, LinearCoregionalization) else 1
 
 
 class _Transiogram:

@@ -129,6 +129,31 @@ class Plan:
         self.prepared = False
         return self
 
+    def set_multivariate(self, mean, coef, data_values=None):
+        """Multivariate Gaussian simulation: the L variables' means, the
+        coregionalization matrices (S x L x L, one per structure of the plan's
+        variogram) and the data's values (D x L); call before prepare()."""
+        mean = np.ascontiguousarray(np.asarray(mean, dtype=np.float64).reshape(-1))
+        coef = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+        dv = np.ascontiguousarray(np.asarray(data_values if data_values is not None else np.zeros(1),
+                                             dtype=np.float64))
+        self._mv = (mean, coef, dv)
+        self._check(self.lib.sgs_plan_set_multivariate(self.h, mean.size, _dp(mean), _dp(coef), _dp(dv)))
+        self.nvars = mean.size
+        self.prepared = False
+        return self
+
+    def simulate_multivariate(self, nreals: int, z=None, seed: int = 0) -> np.ndarray:
+        """nreals x L x N values (realization-major, then variable, then node);
+        z in the same layout or None for the seeded normals."""
+        out = np.empty((nreals, self.nvars, self.N), dtype=np.float64)
+        zp = None
+        if z is not None:
+            z = np.ascontiguousarray(np.asarray(z, dtype=np.float64).reshape(nreals, self.nvars, self.N))
+            zp = _dp(z)
+        self._check(self.lib.sgs_plan_simulate_multivariate(self.h, nreals, zp, C.c_uint64(seed), _dp(out)))
+        return out
+
     def simulate_indicator(self, nreals: int, u=None, seed: int = 0) -> np.ndarray:
         """nreals x N realization-major category indices (int32)."""
         out = np.empty((nreals, self.N), dtype=np.int32)

@@ -32,6 +32,18 @@ def indicator_levels(process: IndicatorProcess, data: GeoTable | None):
     return list(levels), cat.astype(np.int32)
 
 
+def multivariate_data(process: GaussianProcess, data: GeoTable | None) -> np.ndarray:
+    """The data's values of a multivariate process, D x L (columns in table
+    order, one per variable)."""
+    L = process.nvariables
+    if data is None or data.nrow() == 0:
+        return np.zeros((0, L))
+    cols = [np.asarray(v, dtype=np.float64) for v in data.values.values()]
+    if len(cols) != L:
+        raise ArgumentError(f"the data must have {L} variable(s), one per variable of the process")
+    return np.ascontiguousarray(np.stack(cols, axis=1))
+
+
 def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method):
     """Return (sgs_problem, keepalive) — keepalive owns the arrays it points to.
     An IndicatorProcess becomes the problem of its common correlogram, with
@@ -57,8 +69,9 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
     if data is not None and data.nrow() > 0:
         if data.coords.shape[1] != dim:
             raise ArgumentError("data coordinates do not match the domain's dimension")
-        if len(data.values) != 1:
-            raise ArgumentError("the GPU path simulates one variable")
+        nv = process.nvariables if isinstance(process, GaussianProcess) else 1
+        if len(data.values) != nv:
+            raise ArgumentError(f"the data must have {nv} variable(s), one per variable of the process")
         xy = np.ascontiguousarray(data.coords, dtype=np.float64)
         if flat:
             xy = np.ascontiguousarray(np.column_stack([xy[:, 0], np.full(xy.shape[0], 0.5)]))
@@ -80,7 +93,8 @@ def build_problem(process, domain: CartesianGrid, data: GeoTable | None, method)
         keep.append(more)
         p.nstructures = len(st) - 1
         p.structures = C.cast(more, C.POINTER(_abi.SgsVariogram))
-    p.mean = process.mean
+    # a multivariate process keeps its means beside the plan (sgs_plan_set_multivariate)
+    p.mean = process.mean if np.ndim(process.mean) == 0 else 0.0
     p.minneighbors = int(method.minneighbors)
     p.maxneighbors = int(method.maxneighbors)
     nb = method.neighborhood

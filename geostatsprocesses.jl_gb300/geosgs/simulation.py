@@ -19,7 +19,10 @@ another from the path's generator as the reference's
 `traverse(domain, path)` does on every realization (seqsim.jl:98): the
 realizations then run as a batch of independent problems (sgs_batch_*), one
 per realization, with their own neighbour tables and kriging systems.  An
-IndicatorProcess runs them as one plan per realization, in turn.
+IndicatorProcess or a multivariate GaussianProcess runs them as one plan per
+realization, in turn.  A multivariate GaussianProcess (a linear model of
+coregionalization, L means) is simulated by simple cokriging of its variables
+(sgs_plan_set_multivariate); each realization is {variable: values}.
 
 mean / expectedvalue / posterior   src/expectation/field.jl:17-42 and
                                    src/expectation/field/gaussian.jl:5-25
@@ -36,7 +39,7 @@ from .model import (ArgumentError, CartesianGrid, ExplicitPath, GaussianProcess,
                     LinearCoregionalization,
                     LinearPath, RandomPath, SourcePath, nearest_nodes)
 from .plan import Batch, Plan
-from .problem import build_problem, indicator_levels
+from .problem import build_problem, indicator_levels, multivariate_data
 
 
 class FieldSimulationMethod:
@@ -97,7 +100,8 @@ class _Preproc:
     nreals: int = 1
     batches: Any = None  # per-realization paths: [(Batch, first realization, count)]
     levels: Any = None   # indicator simulation: category labels
-    indicator_paths: Any = None  # per-realization indicator paths: (process, domain, data, method, perms)
+    paths: Any = None    # per-realization plans: (process, domain, data, method, perms)
+    vars: Any = None     # multivariate Gaussian simulation: variable names
 
     def close(self):
         if self.plan is not None:
@@ -112,6 +116,18 @@ def _varname(process, data):
     return "field"
 
 
+def _varnames(process, data):
+    """Names of a multivariate process's variables: the data's columns, or
+    field1 .. fieldL (defaultschema, src/processes/field/gaussian.jl:43-48)."""
+    if data is not None and len(data.values) == process.nvariables:
+        return list(data.values)
+    return [f"field{i + 1}" for i in range(process.nvariables)]
+
+
+def _multivariate(process) -> bool:
+    return isinstance(process, GaussianProcess) and process.nvariables > 1
+
+
 def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: CartesianGrid,
                data: GeoTable | None, *, nreals: int = 1, z=None) -> _Preproc:
     """Realization-independent work: problem upload, neighbour search, level
@@ -119,16 +135,17 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     of seqsim.jl:107-131).  `init` is ignored like SEQSIM ignores it
     (seqsim.jl:267-271 always uses ExplicitInit with data appended)."""
     seed = int(rng.integers(0, 2**63 - 1)) if rng is not None else 0
-    if isinstance(process, IndicatorProcess):
-        levels, _ = indicator_levels(process, data)
+    if isinstance(process, IndicatorProcess) or _multivariate(process):
         if method.path_per_realization and isinstance(method.path, RandomPath):
             pre = _Preproc(plan=None, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
-            pre.indicator_paths = (process, domain, data, method,
-                                   method.path.permutations(domain.nelements(), nreals))
+            pre.paths = (process, domain, data, method, method.path.permutations(domain.nelements(), nreals))
         else:
-            pre = _Preproc(plan=_indicator_plan(process, domain, data, method), var=_varname(process, data),
+            pre = _Preproc(plan=_plan_for(process, domain, data, method), var=_varname(process, data),
                            seed=seed, z=z, nreals=nreals)
-        pre.levels = levels
+        if isinstance(process, IndicatorProcess):
+            pre.levels = indicator_levels(process, data)[0]
+        else:
+            pre.vars = _varnames(process, data)
         return pre
     if method.path_per_realization and isinstance(method.path, RandomPath):
         return _Preproc(plan=None, var=_varname(process, data), seed=seed, z=z, nreals=nreals,
@@ -138,17 +155,19 @@ def preprocess(rng, process: GaussianProcess, method: GPUSEQSIM, init, domain: C
     return _Preproc(plan=plan, var=_varname(process, data), seed=seed, z=z, nreals=nreals)
 
 
-def _indicator_plan(process, domain, data, method):
-    """A prepared plan of an IndicatorProcess: the separable path, or full
-    simple cokriging for a linear model of coregionalization."""
-    _, dcat = indicator_levels(process, data)
+def _plan_for(process, domain, data, method):
+    """A prepared plan of an IndicatorProcess (the separable path, or full
+    simple cokriging for a linear model of coregionalization) or of a
+    multivariate GaussianProcess (simple cokriging of its variables)."""
     problem, keep = build_problem(process, domain, data, method)
     plan = Plan(problem, keep)
     try:
-        if isinstance(process.func, LinearCoregionalization):
-            plan.set_indicator_cokriging(process.prob, process.func.coef, dcat)
+        if isinstance(process, GaussianProcess):
+            plan.set_multivariate(process.mean, process.func.coef, multivariate_data(process, data))
+        elif isinstance(process.func, LinearCoregionalization):
+            plan.set_indicator_cokriging(process.prob, process.func.coef, indicator_levels(process, data)[1])
         else:
-            plan.set_indicator(process.prob, dcat)
+            plan.set_indicator(process.prob, indicator_levels(process, data)[1])
         plan.prepare()
     except BaseException:
         plan.close()
@@ -156,23 +175,28 @@ def _indicator_plan(process, domain, data, method):
     return plan
 
 
-def _per_realization_indicator(pre):
-    """Categories of realizations that each follow their own permutation:
-    one plan per realization, created, prepared, simulated and destroyed in
-    turn (one plan's tables on the device at a time).  Realization r draws
-    with seed + r, or takes row r of the given uniforms."""
-    process, domain, data, method, perms = pre.indicator_paths
-    n = domain.nelements()
-    u = None if pre.z is None else np.asarray(pre.z, dtype=np.float64).reshape(pre.nreals, n)
-    out = np.empty((pre.nreals, n), dtype=np.int32)
+def _simulate_plan(plan, process, nreals, z, seed):
+    if isinstance(process, IndicatorProcess):
+        return plan.simulate_indicator(nreals, u=z, seed=seed)
+    return plan.simulate_multivariate(nreals, z=z, seed=seed)
+
+
+def _per_realization_plans(pre):
+    """Realizations that each follow their own permutation: one plan per
+    realization, created, prepared, simulated and destroyed in turn (one
+    plan's tables on the device at a time).  Realization r draws with
+    seed + r, or takes row r of the given uniforms or normals."""
+    process, domain, data, method, perms = pre.paths
+    z = None if pre.z is None else np.asarray(pre.z, dtype=np.float64).reshape(pre.nreals, -1)
+    rows = []
     for r in range(pre.nreals):
         m = GPUSEQSIM(**{**method.__dict__, "path": ExplicitPath(perms[r]), "path_per_realization": False})
-        plan = _indicator_plan(process, domain, data, m)
+        plan = _plan_for(process, domain, data, m)
         try:
-            out[r] = plan.simulate_indicator(1, u=None if u is None else u[r:r + 1], seed=pre.seed + r)[0]
+            rows.append(_simulate_plan(plan, process, 1, None if z is None else z[r:r + 1], pre.seed + r)[0])
         finally:
             plan.close()
-    return out
+    return np.stack(rows)
 
 
 # node budget of one batch of per-realization problems (about 500 bytes of
@@ -200,13 +224,13 @@ def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc)
     """One realization as {var: values} (seqsim.jl:72-156).  The first call
     simulates the whole block of `preproc.nreals` realizations on the GPU."""
     if preproc.block is None:
-        if preproc.levels is not None:
-            if preproc.indicator_paths is not None:
-                cats = _per_realization_indicator(preproc)
-            else:
-                cats = preproc.plan.simulate_indicator(preproc.nreals, u=preproc.z, seed=preproc.seed)
-            preproc.block = np.asarray(preproc.levels, dtype=object if isinstance(preproc.levels[0], str)
-                                       else None)[cats]
+        if preproc.levels is not None or preproc.vars is not None:
+            block = (_per_realization_plans(preproc) if preproc.paths is not None
+                     else _simulate_plan(preproc.plan, process, preproc.nreals, preproc.z, preproc.seed))
+            if preproc.levels is not None:  # category indices -> the categories' labels
+                block = np.asarray(preproc.levels, dtype=object if isinstance(preproc.levels[0], str)
+                                   else None)[block]
+            preproc.block = block
         elif preproc.batches is not None:
             rows = []
             for b, r0, cnt in preproc.batches:
@@ -223,6 +247,8 @@ def randsingle(rng, process, method: GPUSEQSIM, domain, data, preproc: _Preproc)
         raise ArgumentError("more realizations requested than the prepared block holds")
     col = preproc.block[preproc.cursor]
     preproc.cursor += 1
+    if preproc.vars is not None:
+        return {name: col[a] for a, name in enumerate(preproc.vars)}
     return {preproc.var: col}
 
 
@@ -309,7 +335,10 @@ def posterior(process: GaussianProcess, domain: CartesianGrid, data: GeoTable, *
     """(mean, variance) of the process at every node conditioned on the data:
     simple kriging (src/expectation/field/gaussian.jl:21-25), computed on the
     GPU by sgs_krige; NaN where fewer than minneighbors data are found or the
-    system is singular."""
+    system is singular.  Univariate processes only: a multivariate process's
+    posterior needs cokriging from the data, which sgs_krige does not do."""
+    if _multivariate(process):
+        raise ArgumentError("the posterior mean on the GPU path is for univariate processes")
     opts = _KrigingOptions(maxneighbors=maxneighbors, minneighbors=minneighbors, neighborhood=neighborhood,
                            precision=precision, device=device)
     problem, keep = build_problem(process, domain, data, opts)
@@ -330,6 +359,8 @@ def mean(process: GaussianProcess, domain: CartesianGrid, *, data: GeoTable | No
     26-42): the prior mean without data (priormean), simple kriging from the
     data otherwise (posteriormean); {var: values}."""
     if data is None:
+        if _multivariate(process):
+            return {name: np.full(domain.nelements(), mu) for name, mu in zip(_varnames(process, None), process.mean)}
         return {"field": np.full(domain.nelements(), float(process.mean))}
     m, _ = posterior(process, domain, data, **kwargs)
     return {_varname(process, data): m}

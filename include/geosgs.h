@@ -448,6 +448,34 @@ int sgs_plan_set_indicator_cokriging(sgs_plan* plan, int32_t ncat, const double*
 int sgs_plan_set_indicator(sgs_plan* plan, int32_t ncat, const double* prob, const int32_t* data_cat);
 int sgs_plan_simulate_indicator(sgs_plan* plan, int32_t nreals, const double* u, uint64_t seed, int32_t* out);
 
+/* ---- multivariate Gaussian simulation ------------------------------------
+ * A GaussianProcess(func, mean) whose func has nvars > 1 variables, simulated
+ * with SEQSIM (src/processes/field/gaussian.jl:22-35; seqsim.jl:277-290
+ * Kriging(func, mean) with the prior MvNormal(mean, sill(func)), :302-304
+ * predictprob's MvNormal conditional, :335-340 the draw of all variables of a
+ * node at once).  func is a linear model of coregionalization over the
+ * S = 1 + nstructures structures of the plan's variogram:
+ * C_ab(h) = sum_s coef[s][a][b] C_s(h), C_s = sill_s - gamma_s (coef:
+ * S x nvars x nvars, row-major, exactly symmetric).  Each node solves the
+ * simple cokriging system of its n neighbours' nvars values (maxneighbors x
+ * nvars at most 64) in FP64 with Cholesky (a pivot not above 1e-10 x the
+ * largest variance: the node draws from the prior), and draws
+ *   v = mu^ + F z,  mu^_t = mean_t + sum_i sum_a Lambda[(i, a), t] (v_a(x_i) - mean_a),
+ * F the lower Cholesky factor of the conditional covariance C(0) - c' Lambda
+ * (of C(0) for a prior node; a pivot not above the same threshold gives a zero
+ * column, so a node on a datum draws no noise).
+ * sgs_plan_set_multivariate (before sgs_plan_prepare): nvars in 1..8 (1 gives
+ * simple kriging with the one structure set as univariate SEQSIM), the means,
+ * coef, and data_values = problem->ndata x nvars values (the problem's own
+ * data_values are not used).  sgs_plan_simulate_multivariate: out = nreals x
+ * nvars x N values (realization-major, then variable, then node); z in the
+ * same layout, or NULL for Philox4x32-10 normals from `seed` (those of
+ * variable a of node g are the single-variable normals of node a*N + g). */
+#define SGS_MV_MAX_VARIABLES 8
+int sgs_plan_set_multivariate(sgs_plan* plan, int32_t nvars, const double* mean, const double* coef,
+                              const double* data_values);
+int sgs_plan_simulate_multivariate(sgs_plan* plan, int32_t nreals, const double* z, uint64_t seed, double* out);
+
 /* ---- posterior mean (simple kriging from the data) ---------------------
  * Mean and variance of the process at every grid node conditioned on the
  * data alone: the reference's mean(process, domain; data) for a

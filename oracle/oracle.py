@@ -48,6 +48,7 @@ def load():
     lib.oracle_krige.argtypes = [P, dp, dp, C.c_int]
     lib.oracle_simulate_indicator.argtypes = [P, C.c_int32, dp, ip, C.c_int32, dp, C.c_uint64, ip, C.c_int]
     lib.oracle_simulate_cokriging.argtypes = [P, C.c_int32, dp, ip, dp, C.c_int32, dp, C.c_uint64, ip, C.c_int]
+    lib.oracle_simulate_multivariate.argtypes = [P, C.c_int32, dp, dp, dp, C.c_int32, dp, C.c_uint64, dp, C.c_int]
     lib.oracle_uniforms.argtypes = [C.c_uint64, C.c_int64, C.c_int32, dp]
     lib.oracle_uniforms.restype = None
     lib.oracle_neighbors.argtypes = [P, ip, ip]
@@ -151,6 +152,23 @@ class OraclePlan:
             up = _dp(u)
         self._rc(self.lib.oracle_simulate_cokriging(self.h, len(prob), _dp(prob), _ip(dc), _dp(coef), nreals, up,
                                                     seed, _ip(out), nthreads))
+        return out
+
+    def simulate_multivariate(self, nreals, mean, coef, data_values=None, z=None, seed=0, nthreads=0):
+        """nreals x L x N values of a multivariate Gaussian process (linear
+        model of coregionalization, coef: S x L x L; data_values: D x L)."""
+        mean = np.ascontiguousarray(np.asarray(mean, dtype=np.float64).reshape(-1))
+        L = mean.size
+        coef = np.ascontiguousarray(np.asarray(coef, dtype=np.float64))
+        dv = np.ascontiguousarray(np.asarray(data_values if data_values is not None else np.zeros(1),
+                                             dtype=np.float64))
+        out = np.empty((nreals, L, self.N), dtype=np.float64)
+        zp = None
+        if z is not None:
+            z = np.ascontiguousarray(z, dtype=np.float64).reshape(nreals, L, self.N)
+            zp = _dp(z)
+        self._rc(self.lib.oracle_simulate_multivariate(self.h, L, _dp(mean), _dp(coef), _dp(dv), nreals, zp, seed,
+                                                       _dp(out), nthreads))
         return out
 
     def neighbors(self):

@@ -863,27 +863,42 @@ static double structure_cov(const oracle_plan* P, size_t s, const double* h) {
     return v.sill - (v.nugget + (v.sill - v.nugget) * f);
 }
 
-extern "C" int oracle_simulate_cokriging(oracle_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat,
-                                         const double* coef, int32_t R, const double* u, uint64_t seed, int32_t* out,
-                                         int nthreads) {
-    if (!P || !out || R < 0 || ncat < 2 || ncat > 8 || !prob || !coef) return fail(SGS_ERR_ARG, "invalid argument");
-    const int L = ncat, k = P->nmax, S = (int)P->vs.size();
-    if (k * L > 64) return fail(SGS_ERR_ARG, "maxneighbors x categories above 64");
-    double ps = 0.0;
-    for (int l = 0; l < L; ++l) ps += prob[l];
-    std::vector<double> pr(L);
-    for (int l = 0; l < L; ++l) pr[l] = prob[l] / ps;
-    double vmax = 0.0;  // largest variance of an indicator
-    for (int a = 0; a < L; ++a) {
-        double v = 0.0;
-        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + a] * P->vs[s].sill;
-        vmax = std::max(vmax, v);
+// Lower Cholesky factor F (L x L, zero above the diagonal) of the symmetric
+// matrix S (lower triangle read); a pivot not above tau gives a zero column.
+static void mv_factor(const double* S, int L, double tau, double* F) {
+    for (int i = 0; i < L * L; ++i) F[i] = 0.0;
+    for (int j = 0; j < L; ++j) {
+        double d = S[j * L + j];
+        for (int l = 0; l < j; ++l) d -= F[j * L + l] * F[j * L + l];
+        if (!(d > tau)) continue;
+        const double fjj = std::sqrt(d);
+        F[j * L + j] = fjj;
+        for (int i = j + 1; i < L; ++i) {
+            double t = S[i * L + j];
+            for (int l = 0; l < j; ++l) t -= F[i * L + l] * F[j * L + l];
+            F[i * L + j] = t / fjj;
+        }
     }
-    const double tau = kSingularTau * vmax;
-    // per node: status and Lambda (k*L x L), realization-independent
-    std::vector<int8_t> st(P->N, (int8_t)SGS_NODE_PRIOR_NMIN);
-    std::vector<double> lam((size_t)P->N * k * L * L, 0.0);
-    const int nt = nthreads_or_all(nthreads);
+}
+
+// The simple cokriging system of every node: status and Lambda (k*L x L);
+// with `fac`, also the factor of the node's conditional covariance
+// C(0) - c' Lambda (of C(0) for a node drawn from the prior).
+static void cok_systems(oracle_plan* P, int L, const double* coef, double tau, std::vector<int8_t>& st,
+                        std::vector<double>& lam, std::vector<double>* fac, int nt) {
+    const int k = P->nmax, S = (int)P->vs.size();
+    st.assign(P->N, (int8_t)SGS_NODE_PRIOR_NMIN);
+    lam.assign((size_t)P->N * k * L * L, 0.0);
+    std::vector<double> c0((size_t)L * L, 0.0);
+    for (int a = 0; a < L; ++a)
+        for (int b = 0; b < L; ++b)
+            for (int s = 0; s < S; ++s) c0[(size_t)a * L + b] += coef[((size_t)s * L + a) * L + b] * P->vs[s].sill;
+    if (fac) {
+        fac->assign((size_t)P->N * L * L, 0.0);
+        std::vector<double> f0((size_t)L * L);
+        mv_factor(c0.data(), L, tau, f0.data());
+        for (int64_t g = 0; g < P->N; ++g) std::copy(f0.begin(), f0.end(), fac->begin() + (size_t)g * L * L);
+    }
 #pragma omp parallel num_threads(nt)
     {
         std::vector<double> K, c, cs(S);
@@ -953,8 +968,41 @@ extern "C" int oracle_simulate_cokriging(oracle_plan* P, int32_t ncat, const dou
                 }
             }
             st[g] = (int8_t)SGS_NODE_KRIGED;
+            if (fac) {
+                std::vector<double> sg((size_t)L * L);
+                for (int t = 0; t < L; ++t)
+                    for (int u = 0; u <= t; ++u) {
+                        double v = c0[(size_t)t * L + u];
+                        for (int r = 0; r < m; ++r) v -= c[(size_t)r * L + t] * lg[(size_t)r * L + u];
+                        sg[(size_t)t * L + u] = v;
+                    }
+                mv_factor(sg.data(), L, tau, fac->data() + (size_t)g * L * L);
+            }
         }
     }
+}
+
+extern "C" int oracle_simulate_cokriging(oracle_plan* P, int32_t ncat, const double* prob, const int32_t* data_cat,
+                                         const double* coef, int32_t R, const double* u, uint64_t seed, int32_t* out,
+                                         int nthreads) {
+    if (!P || !out || R < 0 || ncat < 2 || ncat > 8 || !prob || !coef) return fail(SGS_ERR_ARG, "invalid argument");
+    const int L = ncat, k = P->nmax, S = (int)P->vs.size();
+    if (k * L > 64) return fail(SGS_ERR_ARG, "maxneighbors x categories above 64");
+    double ps = 0.0;
+    for (int l = 0; l < L; ++l) ps += prob[l];
+    std::vector<double> pr(L);
+    for (int l = 0; l < L; ++l) pr[l] = prob[l] / ps;
+    double vmax = 0.0;  // largest variance of an indicator
+    for (int a = 0; a < L; ++a) {
+        double v = 0.0;
+        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + a] * P->vs[s].sill;
+        vmax = std::max(vmax, v);
+    }
+    const double tau = kSingularTau * vmax;
+    const int nt = nthreads_or_all(nthreads);
+    std::vector<int8_t> st;
+    std::vector<double> lam;
+    cok_systems(P, L, coef, tau, st, lam, nullptr, nt);
     for (int64_t g = 0; g < P->N; ++g) P->status[g] = st[g];
 #pragma omp parallel num_threads(nt)
     {
@@ -998,6 +1046,75 @@ extern "C" int oracle_simulate_cokriging(oracle_plan* P, int32_t ncat, const dou
                 cat[g] = cc;
             }
             for (int64_t g = 0; g < P->N; ++g) out[(size_t)r * P->N + g] = cat[g];
+        }
+    }
+    return SGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multivariate Gaussian simulation: a GaussianProcess(func, mean) whose func
+// is a linear model of coregionalization over the plan's structures
+// (src/processes/field/gaussian.jl:22-35; seqsim.jl:277-290 Kriging(func,
+// mean) and the prior MvNormal(mean, sill(func)); :302-304 predictprob's
+// MvNormal conditional; :335-340 one draw sets all variables of a node).
+// Per node, the simple cokriging system of its n neighbours' L values (the
+// same LHS, right-hand sides and singular rule as the indicator form above):
+//   mu^_t = mean_t + sum_i sum_a Lambda[(i, a), t] (v_a(x_i) - mean_a),
+//   v = mu^ + F z,  F the lower Cholesky factor of C(0) - c' Lambda
+// (of C(0) for a prior node; a pivot not above the singular threshold gives a
+// zero column).  z[(r L + a) N + g], or the normals of pseudo-node a N + g;
+// out[(r L + a) N + g].
+extern "C" int oracle_simulate_multivariate(oracle_plan* P, int32_t nvars, const double* mean, const double* coef,
+                                            const double* data_val, int32_t R, const double* z, uint64_t seed,
+                                            double* out, int nthreads) {
+    if (!P || !out || R < 0 || nvars < 1 || nvars > 8 || !mean || !coef || (P->D > 0 && !data_val))
+        return fail(SGS_ERR_ARG, "invalid argument");
+    const int L = nvars, k = P->nmax, S = (int)P->vs.size();
+    if (k * L > 64) return fail(SGS_ERR_ARG, "maxneighbors x variables above 64");
+    double vmax = 0.0;  // largest variance of a variable
+    for (int a = 0; a < L; ++a) {
+        double v = 0.0;
+        for (int s = 0; s < S; ++s) v += coef[((size_t)s * L + a) * L + a] * P->vs[s].sill;
+        vmax = std::max(vmax, v);
+    }
+    if (!(vmax > 0.0)) return fail(SGS_ERR_ARG, "the model's variances must be positive");
+    const double tau = kSingularTau * vmax;
+    const int nt = nthreads_or_all(nthreads);
+    std::vector<int8_t> st;
+    std::vector<double> lam, fac;
+    cok_systems(P, L, coef, tau, st, lam, &fac, nt);
+    for (int64_t g = 0; g < P->N; ++g) P->status[g] = st[g];
+    const int64_t N = P->N;
+#pragma omp parallel num_threads(nt)
+    {
+        std::vector<double> vals((size_t)(N + P->D) * L), mu(L), zz(L);
+#pragma omp for schedule(dynamic, 1)
+        for (int32_t r = 0; r < R; ++r) {
+            std::fill(vals.begin(), vals.end(), std::nan(""));
+            for (int64_t i = 0; i < P->D * L; ++i) vals[(size_t)N * L + i] = data_val[i];  // ExplicitInit
+            for (int64_t t = 0; t < N; ++t) {
+                const int64_t g = P->path[t];
+                for (int l = 0; l < L; ++l) mu[l] = mean[l];
+                if (st[g] == SGS_NODE_KRIGED) {
+                    const int32_t* nb = &P->nbr[(size_t)g * k];
+                    const double* lg = &lam[(size_t)g * k * L * L];
+                    for (int i = 0; i < P->cnt[g]; ++i)
+                        for (int a = 0; a < L; ++a) {
+                            const double d = vals[(size_t)nb[i] * L + a] - mean[a];
+                            for (int l = 0; l < L; ++l) mu[l] += lg[(size_t)(i * L + a) * L + l] * d;
+                        }
+                }
+                for (int a = 0; a < L; ++a)
+                    zz[a] = z ? z[((size_t)r * L + a) * N + g] : normal_of(seed, (int64_t)a * N + g, r);
+                const double* F = &fac[(size_t)g * L * L];
+                for (int l = 0; l < L; ++l) {
+                    double v = mu[l];
+                    for (int u = 0; u <= l; ++u) v += F[l * L + u] * zz[u];
+                    vals[(size_t)g * L + l] = v;
+                }
+            }
+            for (int a = 0; a < L; ++a)
+                for (int64_t g = 0; g < N; ++g) out[((size_t)r * L + a) * N + g] = vals[(size_t)g * L + a];
         }
     }
     return SGS_OK;
