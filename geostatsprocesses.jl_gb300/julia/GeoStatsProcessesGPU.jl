@@ -184,6 +184,7 @@ end
 
 function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, init, domain, data)
   f = process.func
+  nvariables(f) > 1 && return _preprocess_multivariate(process, method, domain, data)
   dim = embeddim(domain)
   vgs = [SgsVariogram(vtype(g), 0, c * ustrip(sill(g)), c * ustrip(nugget(g)), radii3(g.ball, dim),
                       rot9(rotation(g.ball), dim)) for (c, g) in structures(f)]
@@ -194,6 +195,7 @@ function preprocess(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSI
 end
 
 function randsingle(rng::AbstractRNG, process::GaussianProcess, method::GPUSEQSIM, domain, data, preproc)
+  hasproperty(preproc, :vars) && return _randsingle_multivariate(rng, method, preproc)
   (; plan, var, nelm, block, cursor) = preproc
   # the plan lives on this process's GPU (src/simulation/field.jl:98-100 style check)
   myid() == plan.owner || throw(ArgumentError("GPUSEQSIM realizations must run on the process that prepared them"))
@@ -288,6 +290,50 @@ function randsingle(rng::AbstractRNG, process::IndicatorProcess, method::GPUSEQS
   end
   cursor[] += 1
   (; var => labels[block[][:, cursor[]] .+ 1])
+end
+
+# ---- multivariate Gaussian simulation (gaussian.jl:22-35; seqsim.jl:277-290,
+# 302-304, 335-340) ----
+# A GaussianProcess whose func is a linear model of coregionalization (a
+# NestedCovariance with matrix coefficients, nvariables(f) = L > 1): each node
+# solves the simple cokriging system of its neighbours' L values and draws all
+# L variables at once from the conditional MvNormal (sgs_plan_set_multivariate,
+# sgs_plan_simulate_multivariate).  Every datum holds all L variables.
+function _preprocess_multivariate(process, method, domain, data)
+  f = process.func
+  f isa NestedCovariance || throw(ArgumentError("GPUSEQSIM simulates multivariate processes of a linear model of coregionalization"))
+  L = nvariables(f)
+  L <= 8 || throw(ArgumentError("GPUSEQSIM simulates up to 8 variables"))
+  vgs, coef = _lmc(f, embeddim(domain))
+  length(coef) == length(vgs) * L^2 || throw(ArgumentError("coregionalization matrices must be $L x $L"))
+  mean = Float64.(ustrip.(collect(process.mean)))
+  vars = isnothing(data) ? ntuple(i -> Symbol(:field, i), L) : Tuple(propertynames(values(data)))
+  length(vars) == L || throw(ArgumentError("the data must have $L variables, one per variable of the process"))
+  D = isnothing(data) ? 0 : nrow(data)
+  dv = Float64[]  # D x L, row-major
+  for i in 1:D, v in vars
+    push!(dv, Float64(ustrip(getproperty(values(data), v)[i])))
+  end
+  setmv(plan) = GC.@preserve mean coef dv check(ccall((:sgs_plan_set_multivariate, libgeosgs), Cint,
+                                                      (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                                                      plan.ptr, L, mean, coef, dv), plan.ptr)
+  plan = _plan(vgs, 0.0, method, domain, data, zeros(D); before_prepare=setmv)
+  (; plan, vars, L, nelm=nelements(domain), block=Ref(Array{Float64,3}(undef, 0, 0, 0)), cursor=Ref(0))
+end
+
+function _randsingle_multivariate(rng, method, preproc)
+  (; plan, vars, L, nelm, block, cursor) = preproc
+  myid() == plan.owner || throw(ArgumentError("GPUSEQSIM realizations must run on the process that prepared them"))
+  if cursor[] == size(block[], 3)
+    B = Array{Float64,3}(undef, nelm, L, method.batch)  # N x L x batch: the C side's nreals x L x N
+    check(ccall((:sgs_plan_simulate_multivariate, libgeosgs), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Float64}, UInt64, Ptr{Float64}),
+                plan.ptr, method.batch, C_NULL, rand(rng, UInt64), B), plan.ptr)
+    block[] = B
+    cursor[] = 0
+  end
+  cursor[] += 1
+  NamedTuple{vars}(Tuple(block[][:, a, cursor[]] for a in 1:L))
 end
 
 end # module
