@@ -65,28 +65,91 @@ class GPUSEQSIM(FieldSimulationMethod):
 
 
 class Ensemble:
-    """Realizations of a field process over a domain (src/ensembles.jl:10-16)."""
+    """Realizations of a field process over a domain (src/ensembles.jl:10-16):
+    `Ensemble(domain, reals, fetch=identity)`.  Iteration and indexing (an
+    int, or a list of ints) give `fetch(real)` as {var: values}.  The
+    statistics reduce every variable node by node over the realizations, as
+    the reference's ereduce does (ensembles.jl:42-52, 76-85), on the device
+    (sgs_ensemble_*: the realizations of one variable are uploaded as N rows
+    of nreals FP64 values), and return {var: values}; with `var` given, that
+    variable's values alone.  Variables must be numeric (integer category
+    labels reduce as numbers; string labels raise ArgumentError)."""
 
-    def __init__(self, domain, reals):
+    def __init__(self, domain, reals, fetch=None):
         self.domain = domain
         self.reals = list(reals)
+        self.fetch = fetch if fetch is not None else (lambda real: real)
 
     def __len__(self):
         return len(self.reals)
 
-    def __getitem__(self, i):
-        return self.reals[i]
+    def __iter__(self):
+        return (self.fetch(r) for r in self.reals)
 
-    def _stack(self, var=None):
-        var = var or next(iter(self.reals[0]))
-        return np.stack([r[var] for r in self.reals])
+    def __getitem__(self, i):
+        if isinstance(i, (list, tuple, np.ndarray)):
+            return [self.fetch(self.reals[j]) for j in i]
+        return self.fetch(self.reals[i])
+
+    def variables(self) -> list:
+        """The realizations' variable names (evars, ensembles.jl:72-74)."""
+        return list(self.fetch(self.reals[0]))
+
+    def _rows(self, var):
+        """The realizations of `var` as a CUDA tensor of N rows of nreals FP64
+        values (the node-major layout of sgs_ensemble_*)."""
+        import torch
+
+        cols = [np.asarray(self.fetch(r)[var]) for r in self.reals]
+        if any(c.dtype.kind not in "biuf" for c in cols):
+            raise ArgumentError(f"variable {var} is not numeric")
+        rows = np.ascontiguousarray(np.stack(cols, axis=1), dtype=np.float64)
+        if not torch.cuda.is_available():
+            raise _abi.GeoSGSError(_abi.SGS_ERR_NODEVICE, "ensemble statistics run on the GPU: no CUDA device")
+        return torch.from_numpy(rows).cuda()
+
+    def _reduce(self, f, var):
+        names = [var] if var is not None else self.variables()
+        out = {}
+        for name in names:
+            out[name] = f(self._rows(name)).cpu().numpy()
+        return out[var] if var is not None else out
 
     def mean(self, var=None):
-        """Per-node mean over realizations (src/ensembles.jl:42-52)."""
-        return self._stack(var).mean(axis=0)
+        """Per-node mean over the realizations (ensembles.jl:42)."""
+        from . import ensemble
+
+        return self._reduce(lambda V: ensemble.mean_var(V, len(self))[0], var)
 
     def var(self, var=None):
-        return self._stack(var).var(axis=0, ddof=1)
+        """Per-node variance, n - 1 divisor (ensembles.jl:44)."""
+        from . import ensemble
+
+        return self._reduce(lambda V: ensemble.mean_var(V, len(self))[1], var)
+
+    def cdf(self, x: float, var=None):
+        """Per-node fraction of realizations <= x (ensembles.jl:46)."""
+        from . import ensemble
+
+        return self._reduce(lambda V: ensemble.cdf(V, len(self), [x])[:, 0], var)
+
+    def ccdf(self, x: float, var=None):
+        """Per-node fraction of realizations > x (ensembles.jl:48)."""
+        from . import ensemble
+
+        return self._reduce(lambda V: ensemble.cdf(V, len(self), [x], complement=True)[:, 0], var)
+
+    def quantile(self, p, var=None):
+        """Per-node quantile(s) with linear interpolation between order
+        statistics (ensembles.jl:50-52): one p, or a list of p giving a list
+        of results; at most 1024 realizations."""
+        from . import ensemble
+
+        if np.ndim(p) > 0:
+            return [self.quantile(float(q), var) for q in p]
+        if len(self) > 1024:
+            raise ArgumentError("quantiles on the device take at most 1024 realizations")
+        return self._reduce(lambda V: ensemble.quantile(V, len(self), [float(p)])[:, 0], var)
 
 
 @dataclass

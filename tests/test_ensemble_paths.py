@@ -108,3 +108,40 @@ def test_per_realization_indicator_paths_match_oracle(oracle_mod, geosgs_lib):
     shared = geosgs.rand(np.random.default_rng(1), proc, wl.domain, R, data=data, z=u,
                          method=geosgs.GPUSEQSIM(path=geosgs.RandomPath(17), maxneighbors=10))
     np.testing.assert_array_equal(shared[0]["C"], ens[0]["C"])
+
+
+def test_ensemble_container_api():
+    """Iteration, indexing (an int or a list) and fetch, as src/ensembles.jl:
+    10-35 (no device work)."""
+    grid = geosgs.CartesianGrid((3, 2))
+    reals = [{"a": np.arange(6.0) + r, "b": -np.arange(6.0)} for r in range(4)]
+    ens = geosgs.Ensemble(grid, reals)
+    assert len(ens) == 4 and ens.variables() == ["a", "b"]
+    assert [r["a"][0] for r in ens] == [0.0, 1.0, 2.0, 3.0]
+    assert [r["a"][1] for r in ens[[3, 1]]] == [4.0, 2.0]
+    doubled = geosgs.Ensemble(grid, reals, fetch=lambda real: {k: 2 * v for k, v in real.items()})
+    assert doubled[2]["a"][5] == 14.0
+    with pytest.raises(geosgs.ArgumentError):
+        geosgs.Ensemble(grid, [{"c": np.array(["x", "y"])}])._rows("c")
+
+
+@pytest.mark.gpu
+def test_ensemble_statistics_through_the_public_api(geosgs_lib):
+    """Ensemble.mean/var/cdf/ccdf/quantile of rand's realizations on the
+    device against numpy on the same values, for every variable."""
+    proc = geosgs.GaussianProcess(geosgs.LinearCoregionalization([
+        (np.array([[1.0, 0.3], [0.3, 0.5]]), geosgs.SphericalVariogram(range=5.0))]), [0.5, -1.0])
+    grid = geosgs.CartesianGrid((20, 16))
+    ens = geosgs.rand(np.random.default_rng(4), proc, grid, 9,
+                      method=geosgs.GPUSEQSIM(path=geosgs.RandomPath(2), maxneighbors=12))
+    m, v = ens.mean(), ens.var()
+    assert sorted(m) == ["field1", "field2"]
+    for name in ("field1", "field2"):
+        vals = np.stack([r[name] for r in ens])
+        np.testing.assert_allclose(m[name], vals.mean(axis=0), rtol=0, atol=1e-12)
+        np.testing.assert_allclose(v[name], vals.var(axis=0, ddof=1), rtol=0, atol=1e-12)
+        np.testing.assert_array_equal(ens.cdf(0.25, name), (vals <= 0.25).mean(axis=0))
+        np.testing.assert_array_equal(ens.ccdf(0.25, name), (vals > 0.25).mean(axis=0))
+        q = ens.quantile([0.1, 0.5], name)
+        np.testing.assert_allclose(q[0], np.quantile(vals, 0.1, axis=0), rtol=0, atol=1e-12)
+        np.testing.assert_allclose(q[1], np.quantile(vals, 0.5, axis=0), rtol=0, atol=1e-12)
