@@ -10,7 +10,10 @@ The oracle's restatement (oracle_simulate_multivariate) is pinned on the CPU
 by reductions to the univariate oracle, which the golden fixtures pin: with
 one variable it is univariate SEQSIM on the same structures; with diagonal
 coregionalization matrices each variable is an independent univariate
-simulation of its own sill.  Also checked: a node on a datum, visited first,
+simulation of its own sill.  An independent numpy restatement (the model's
+own variogram functions, numpy.linalg.solve and cholesky) checks the
+cross-covariance terms on a non-diagonal nested model.  Also checked: a node
+on a datum, visited first,
 takes the datum's values in every realization, and prior draws have the
 model's covariance C(0).  The GPU is then compared with the oracle on the
 same normals, within the project's value bar (max |a - b| / max(|b|, 1)
@@ -105,6 +108,61 @@ def test_oracle_diagonal_model_is_independent_univariate_runs(oracle_mod):
         p, keep = geosgs.build_problem(pa, grid, da, method)
         O = oracle_mod.OraclePlan(p, keep).prepare()
         assert rel_err(mv[:, a, :], O.simulate(R, z[:, a, :])) <= 1e-10, a
+
+
+def numpy_multivariate(proc, grid, data, path, nbr, cnt, nmin, z):
+    """An independent restatement of the multivariate loop for small cases:
+    per node in path order, the (nL x nL) cokriging system from the model's
+    own variogram functions, numpy.linalg.solve, the conditional covariance
+    C(0) - c' Lambda and numpy's Cholesky factor."""
+    dim, L = grid.dim, proc.nvariables
+    st, A = proc.func.structures(), proc.func.coef
+    X = grid.centroids() if data is None else np.vstack([grid.centroids(), data.coords])
+    N = grid.nelements()
+
+    def cov(h):  # lags (m x dim) -> m x L x L
+        out = np.zeros((h.shape[0], L, L))
+        for s, g in enumerate(st):
+            out += (g.sill - g.gamma_at(h, dim))[:, None, None] * A[s][None]
+        return out
+
+    mean = np.asarray(proc.mean)
+    C0 = cov(np.zeros((1, dim)))[0]
+    vals = np.full((X.shape[0], L), np.nan)
+    if data is not None:
+        vals[N:] = gproblem.multivariate_data(proc, data)
+    for g in path:
+        n = cnt[g]
+        mu, S = mean.copy(), C0.copy()
+        if n >= nmin:
+            P = X[nbr[g, :n]]
+            K = cov((P[:, None, :] - P[None, :, :]).reshape(-1, dim)).reshape(n, n, L, L)
+            K = K.transpose(0, 2, 1, 3).reshape(n * L, n * L)
+            c = cov(P - X[g]).reshape(n * L, L)
+            lam = np.linalg.solve(K, c)
+            mu = mean + lam.T @ (vals[nbr[g, :n]].reshape(-1) - np.tile(mean, n))
+            S = C0 - c.T @ lam
+        vals[g] = mu + np.linalg.cholesky(S) @ z[:, g]
+    return vals[:N].T
+
+
+def test_oracle_matches_an_independent_numpy_restatement(oracle_mod):
+    """Cross-covariances, nested structures of different ranges and
+    anisotropy, data and prior nodes: the oracle against numpy on the
+    oracle's own neighbour sets (the search is pinned elsewhere)."""
+    grid = geosgs.CartesianGrid((16, 14))
+    rng = np.random.default_rng(21)
+    data = mv_data(rng, 10, grid.dims, 2)
+    proc = geosgs.GaussianProcess(lmc(2, nugget=0.05), [0.3, -0.6])
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(5), maxneighbors=8, minneighbors=3,
+                              neighborhood=geosgs.MetricBall(3.0))
+    z = rng.standard_normal((1, 2, grid.nelements()))
+    O, out = oracle_mv(oracle_mod, proc, grid, data, method, 1, z=z)
+    nbr, cnt = O.neighbors()
+    assert np.any(cnt < 3) and np.any(cnt == 8)  # prior nodes and full systems
+    path = geosgs.RandomPath(5).permutation(grid.nelements())
+    want = numpy_multivariate(proc, grid, data, path, nbr, cnt, 3, z[0])
+    assert rel_err(out[0], want) <= 1e-9
 
 
 def test_oracle_datum_reproduction_and_prior_covariance(oracle_mod):
