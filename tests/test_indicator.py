@@ -7,8 +7,10 @@ shapes (test/field.jl:181-204: two categories without data give the set
 {1, 2}, data labelled [1, 3, 1] give {1, 3}, three proportions give
 {1, 2, 3}, string labels come back as strings), by exact data reproduction
 (a node on a datum takes its category in every realization, nugget 0), and
-by the prior's proportions where no neighbour is found.  The GPU is then
-compared with the oracle fed the same uniforms: categories identical."""
+by the prior's proportions where no neighbour is found; its full simple
+cokriging form by its reduction to the separable path and by an independent
+numpy restatement on a non-separable model.  The GPU is then compared with
+the oracle fed the same uniforms: categories identical."""
 import numpy as np
 import pytest
 
@@ -173,6 +175,55 @@ def test_oracle_cokriging_reduces_to_the_separable_path(oracle_mod):
     u = rng.uniform(0.0, 1.0, (6, O.N))
     np.testing.assert_array_equal(O.simulate_cokriging(6, prob, cok.func.coef, dcat, u=u),
                                   O.simulate_indicator(6, sep.prob, dcat, u=u))
+
+
+def test_oracle_cokriging_matches_an_independent_numpy_restatement(oracle_mod):
+    """A non-separable model (two structures, different ranges and
+    anisotropy) with data of every category: the oracle's categories against
+    numpy on the oracle's neighbour sets — the (nL x nL) system from the
+    model's own variogram functions, numpy.linalg.solve,
+    p = prob + Lambda' (I - prob) clamped and normalized, the inverse cdf at
+    the same uniforms."""
+    L, prob = 3, np.array([0.5, 0.3, 0.2])
+    grid = geosgs.CartesianGrid((18, 15))
+    rng = np.random.default_rng(31)
+    labels = rng.integers(0, L, 12)
+    labels[:L] = np.arange(L)
+    data = geosgs.georef({"C": labels}, rng.uniform(0.0, 1.0, (12, 2)) * [18.0, 15.0])
+    proc = geosgs.IndicatorProcess(lmc_model(L), prob=prob)
+    method = geosgs.GPUSEQSIM(path=geosgs.RandomPath(9), maxneighbors=8, minneighbors=2,
+                              neighborhood=geosgs.MetricBall(3.0))
+    p, keep = geosgs.build_problem(proc, grid, data, method)
+    _, dcat = gproblem.indicator_levels(proc, data)
+    O = oracle_mod.OraclePlan(p, keep).prepare()
+    N = O.N
+    u = rng.uniform(0.0, 1.0, (1, N))
+    got = O.simulate_cokriging(1, prob, proc.func.coef, dcat, u=u)[0]
+    nbr, cnt = O.neighbors()
+    assert np.any(cnt < 2) and np.any(cnt == 8)  # prior nodes and full systems
+    st, A = proc.func.structures(), proc.func.coef
+    X = np.vstack([grid.centroids(), data.coords])
+
+    def cov(h):
+        out = np.zeros((h.shape[0], L, L))
+        for s, g in enumerate(st):
+            out += (g.sill - g.gamma_at(h, 2))[:, None, None] * A[s][None]
+        return out
+
+    cat = np.concatenate([np.full(N, -1), dcat])
+    for g in geosgs.RandomPath(9).permutation(N):
+        n = cnt[g]
+        q = prob.copy()
+        if n >= 2:
+            P = X[nbr[g, :n]]
+            K = cov((P[:, None, :] - P[None, :, :]).reshape(-1, 2)).reshape(n, n, L, L)
+            lam = np.linalg.solve(K.transpose(0, 2, 1, 3).reshape(n * L, n * L), cov(P - X[g]).reshape(n * L, L))
+            onehot = (cat[nbr[g, :n]][:, None] == np.arange(L)[None, :]).astype(float)
+            q = prob + lam.T @ (onehot - prob).reshape(-1)
+        q = np.clip(q, 0.0, 1.0)
+        q = q / q.sum() if q.sum() > 0 else prob
+        cat[g] = min(int(np.searchsorted(np.cumsum(q)[:-1], u[0, g], side="right")), L - 1)
+    np.testing.assert_array_equal(got, cat[:N])
 
 
 def test_oracle_cokriging_proportions(oracle_mod):
