@@ -152,3 +152,18 @@ def test_source_path_reaches_the_problem():
     np.testing.assert_array_equal(got, geosgs.traverse(grid, m.path))
     assert got[0] == grid.linear_index(3, 4) and got[1] == grid.linear_index(8, 1)
     assert isinstance(p, _abi.SgsProblem)
+
+
+def test_paths_on_1d_and_3d_grids():
+    g1 = geosgs.CartesianGrid((9,), origin=(2.0,), spacing=(0.5,))
+    np.testing.assert_array_equal(geosgs.nearest_nodes(g1, [[2.1], [6.4], [-3.0]]), [0, 8, 0])
+    np.testing.assert_array_equal(geosgs.traverse(g1, geosgs.SourcePath([4])), [4, 3, 5, 2, 6, 1, 7, 0, 8])
+    g3 = geosgs.CartesianGrid((5, 4, 3), spacing=(1.0, 2.0, 0.5))
+    pts = np.array([[0.2, 0.1, 0.1], [4.9, 7.9, 1.4], [2.5, 3.0, 0.74]])
+    want = [g3.linear_index(0, 0, 0), g3.linear_index(4, 3, 2), g3.linear_index(2, 1, 1)]
+    np.testing.assert_array_equal(geosgs.nearest_nodes(g3, pts), want)
+    ip = geosgs.IndicatorProcess(geosgs.SphericalTransiogram(range=2.0))
+    m = geosgs.defaultsimulation(ip, g3, data=geosgs.georef({"C": [1, 2, 1]}, pts))
+    np.testing.assert_array_equal(m.path.sources, want)
+    p = geosgs.traverse(g3, m.path)
+    np.testing.assert_array_equal(p, brute_source_order(g3, want))
